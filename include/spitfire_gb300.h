@@ -1,0 +1,293 @@
+/*
+ * spitfire_gb300 -- C ABI of the GB300 (sm_103a) Griffon chemistry hot path.
+ *
+ * Every entry point takes plain pointers and sizes. Batched entry points take DEVICE pointers (memory the
+ * caller allocated on the current CUDA device), a CUDA stream passed as `void *` (a cudaStream_t; NULL is the
+ * legacy default stream) and, where a kernel needs global scratch memory, a caller-provided workspace whose
+ * size the matching *_workspace_size function reports. No batched entry point allocates device memory.
+ * Entry points return 0 (SF_OK) or a status code; sf_last_error() gives the message of the last failure in
+ * the calling thread. Per-item numerical outcomes (e.g. an integration that hit its step cap) are reported in
+ * device int arrays, not by the return code.
+ *
+ * Array layouts (all FP64 unless stated; "state-major" = one contiguous row per state):
+ *   mass fractions   Y[n][ns]
+ *   reactor state    isochoric q[n][ns+1] = [rho, T, Y_0..Y_{ns-2}]; isobaric q[n][ns] = [T, Y_0..Y_{ns-2}]
+ *   Jacobians        one column-major neq x neq block per state, blocks contiguous: J[n][neq*neq]
+ *   rate sensitivity one column-major (ns+1) x (ns+1) block per state (columns rho, T, Y_0..Y_{ns-2};
+ *                    last row unused), as Griffon's prod_rates_primitive_sensitivities writes it
+ *   flamelet values  per flamelet, Griffon's BTDDOD layout: nzi column-major ns x ns diagonal blocks, then
+ *                    (nzi-1)*ns sub-diagonal values, then (nzi-1)*ns super-diagonal values
+ *
+ * Reference interfaces replaced (paths within sandialabs/Spitfire):
+ *   src/spitfire/griffon/griffon.pyx            -- Cython class PyCombustionKernels and py_btddod_* functions
+ *   src/spitfire/griffon/include/combustion_kernels.h and btddod_matrix_kernels.h -- the C++ engine
+ */
+#ifndef SPITFIRE_GB300_H
+#define SPITFIRE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------------------- status */
+enum sf_status {
+  SF_OK = 0,
+  SF_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, unknown option */
+  SF_ERR_MECHANISM = 2,        /* mechanism rejected (e.g. 2 <= n_net <= 8 violated, unknown enum) */
+  SF_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+  SF_ERR_UNSUPPORTED = 4,      /* feature not available on this path (e.g. NASA9 thermo on the GPU) */
+  SF_ERR_WORKSPACE = 5,        /* workspace missing or smaller than *_workspace_size reported */
+  SF_ERR_NO_DEVICE = 6         /* no CUDA device */
+};
+
+/* Message of the last failing call in this thread (empty string if none). */
+const char *sf_last_error(void);
+/* Library version string. */
+const char *sf_version(void);
+
+/* ------------------------------------------------------------------------------------- mechanism description */
+/* Thermodynamic model codes (combustion_kernels.h:43-49 CpType). */
+enum sf_thermo_kind { SF_THERMO_CONST = 1, SF_THERMO_NASA7 = 2, SF_THERMO_NASA9 = 3 };
+/* Reaction rate types (combustion_kernels.h:59-66 RateType). */
+enum sf_rxn_kind { SF_RXN_SIMPLE = 1, SF_RXN_THIRD_BODY = 2, SF_RXN_LINDEMANN = 3, SF_RXN_TROE = 4 };
+
+/*
+ * Flat mechanism description: the data Spitfire passes to Griffon through the 16 mechanism_* setters
+ * (griffon.pyx:234-551, combustion_kernels.h:293-379), gathered into arrays. Species indices refer to the phase
+ * order. Within a reaction, reactants, products, efficiencies and special orders must be listed in ascending
+ * species-NAME order (the std::map<std::string,...> order Griffon iterates in, chemistry_setup.cpp:361-392).
+ *
+ * thermo_coefs[k*20 + j]:
+ *   NASA7: [Tmin, Tmid, Tmax, low a0..a6, high a0..a6]              (raw coefficients, not multiplied by R)
+ *   CONST: [Tmin, Tmax, T0, h0, s0, cp, 0...]
+ * NASA9 species carry their coefficient list in nasa9_coefs with nasa9_offsets[k]..nasa9_offsets[k+1]
+ * (Cantera's flattened form: [n_regions, Tlo, Thi, a0..a8, Tlo, Thi, ...]); nasa9_offsets may be NULL if no
+ * species is NASA9.
+ * Rate constants: k = A T^b exp(-Ea_over_R / T); kfwd is the (high-pressure) forward rate, kflf the low-pressure
+ * rate of falloff reactions. troe = [A, T3, T1, T2].
+ */
+typedef struct sf_mech_desc {
+  int n_species;
+  int n_reactions;
+  int n_elements;
+  double gas_constant;       /* J/kmol/K */
+  double ref_pressure;       /* Pa */
+  double ref_temperature;    /* K */
+  const double *molecular_weights; /* [n_species] kg/kmol */
+  const int *thermo_kind;          /* [n_species] sf_thermo_kind */
+  const double *thermo_coefs;      /* [n_species*20] */
+  const int *nasa9_offsets;        /* [n_species+1] or NULL */
+  const double *nasa9_coefs;
+
+  const int *rxn_kind;          /* [n_reactions] sf_rxn_kind */
+  const int *rxn_reversible;    /* [n_reactions] 0/1 */
+  const double *rxn_kfwd;       /* [n_reactions*3] A, b, Ea/R */
+  const double *rxn_kflf;       /* [n_reactions*3] (falloff only) */
+  const double *rxn_troe;       /* [n_reactions*4] (Troe only) */
+  const double *rxn_default_eff;/* [n_reactions] (third-body / falloff only) */
+  const int *reac_offsets;      /* [n_reactions+1] */
+  const int *reac_species;
+  const int *reac_stoich;
+  const int *prod_offsets;      /* [n_reactions+1] */
+  const int *prod_species;
+  const int *prod_stoich;       /* positive integers */
+  const int *eff_offsets;       /* [n_reactions+1] third-body efficiencies */
+  const int *eff_species;
+  const double *eff_values;
+  const int *order_offsets;     /* [n_reactions+1] special (non-elementary) orders; a reaction with any entry
+                                   here is a *_with_special_orders reaction */
+  const int *order_species;
+  const double *order_values;
+} sf_mech_desc;
+
+typedef struct sf_mech sf_mech; /* opaque: host tables + device blob on one CUDA device */
+
+/* Build a mechanism from a description, running Griffon's ReactionRateData::finalize derivations
+ * (chemistry_setup.cpp:459-732) and uploading the packed blob to the current device.
+ * Replaces PyCombustionKernels.__cinit__ + mechanism_* setters (griffon.pyx:225-551). */
+int sf_mech_create(const sf_mech_desc *desc, sf_mech **out_mech);
+/* Replaces PyCombustionKernels.__dealloc__ (griffon.pyx:228-229). */
+int sf_mech_destroy(sf_mech *mech);
+/* Sizes of a built mechanism; counts[0..5] = reactions by kind: simple, three-body, Lindemann, Troe, dense
+ * (Jacobian rows that need the dense term), special-order. Any output pointer may be NULL. */
+int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *counts6);
+
+/* ------------------------------------------------------------------------------------------- thermodynamics */
+/* what: 0 cp_mix[n], 1 cv_mix[n], 2 enthalpy_mix[n], 3 energy_mix[n], 4 species_cp[n][ns], 5 species_cv[n][ns],
+ *       6 species_enthalpies[n][ns], 7 species_energies[n][ns], 8 mixture_molecular_weight[n],
+ *       9 dcp/dT mix[n] (cp_sens_T), 10 dcp/dT species[n][ns]
+ * Replaces griffon.pyx:684-761 (cp_mix, cv_mix, species_cp, ..., dcpdT_species). */
+int sf_thermo_batch(const sf_mech *mech, int what, int n, const double *T, const double *Y, double *out,
+                    void *stream);
+
+/* --------------------------------------------------------------------------------------------------- kinetics */
+/* Production rates w[n][ns] (kg/m^3/s) at (T, rho, Y).
+ * Replaces PyCombustionKernels.production_rates (griffon.pyx:763-768 -> chemistry_kernels.cpp:29-33). Note the
+ * Cython wrapper passes its first positional argument as T; this entry point names T and rho explicitly. */
+int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const double *rho, const double *Y,
+                              double *out_w, void *stream);
+
+/* Production rates and their sensitivities to (rho, T, Y_0..Y_{ns-2}), out_sens[n][(ns+1)^2].
+ * option: 0 exact dense, 2 exact sparse (identical values), 1 no third-body/falloff sensitivities.
+ * Replaces prod_rates_primitive_sensitivities (griffon.pyx:773-783 -> chemistry_kernels.cpp:464-483). */
+int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const double *T, const double *Y, int option,
+                        double *out_w, double *out_sens, void *stream);
+
+/* ------------------------------------------------------------------------------------------ reactor kernels */
+/* Reactor parameters shared by every state of one batched call (the scalar arguments of
+ * reactor_rhs_isobaric / reactor_rhs_isochoric, griffon.pyx:788-866). */
+typedef struct sf_reactor_params {
+  int configuration;        /* 0 isobaric (q = [T, Y]), 1 isochoric (q = [rho, T, Y]) */
+  int heat_transfer;        /* 0 adiabatic, 1 isothermal, 2 diathermal */
+  int open;                 /* 0 closed, 1 open (mass exchange with a feed) */
+  double pressure;          /* isobaric: thermodynamic pressure (Pa) */
+  double inflow_density;    /* isochoric open reactors */
+  double inflow_temperature;
+  const double *inflow_Y;   /* DEVICE pointer [ns] or NULL when closed */
+  double tau;               /* residence time */
+  double fluid_temperature; /* convection temperature */
+  double surface_temperature; /* radiation temperature */
+  double h_convection;
+  double eps_radiation;
+  double surface_area_to_volume;
+} sf_reactor_params;
+
+/* Right-hand side of n reactors (state-major q, out_rhs). If pressures is non-NULL (isobaric) it gives one
+ * pressure per state and overrides params->pressure.
+ * Replaces reactor_rhs_isobaric / reactor_rhs_isochoric (isobaric_reactor_kernels.cpp:170-219,
+ * isochoric_reactor_kernels.cpp:184-242). */
+int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *params, int n, const double *q,
+                         const double *pressures, double *out_rhs, void *stream);
+
+/* Right-hand side and analytical Jacobian (column-major neq x neq per state). rates_option as in
+ * sf_rates_sens_batch. Replaces reactor_jac_isobaric / reactor_jac_isochoric (isobaric_reactor_kernels.cpp:221-343,
+ * isochoric_reactor_kernels.cpp:244-333). */
+int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *params, int rates_option, int n,
+                         const double *q, const double *pressures, double *out_rhs, double *out_jac, void *stream);
+
+/* The same evaluation in the plain single-state GPU form: one thread per state, the mechanism read from global
+ * memory, Griffon's per-reaction dense scatter into a per-state scratch Jacobian. It exists as the comparison
+ * point for the batched kernels; results are the same to rounding. Needs workspace of
+ * sf_reactor_jac_plain_workspace_size bytes. */
+size_t sf_reactor_jac_plain_workspace_size(const sf_mech *mech, int n);
+int sf_reactor_jac_plain_batch(const sf_mech *mech, const sf_reactor_params *params, int n, const double *q,
+                               const double *pressures, double *out_rhs, double *out_jac, void *workspace,
+                               size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------------------------- Newton algebra */
+/* Factor the Newton iteration matrices A_k = gamma_h[k] * J_k - I (m x m column-major, n of them).
+ * precision: 0 FP64 LU with partial pivoting (as LAPACK dgetrf, reactors.py:340-344); 1 FP32 LU of the same
+ * matrix (A itself kept in FP64 for the residual refinement of sf_newton_solve_batch).
+ * out_A[n][m*m] receives A in FP64; out_lu receives the factors: FP64 [n][m*m] (precision 0) or FP32 [n][m*m]
+ * (precision 1, pass it as a double* of n*m*m/2 doubles); out_piv[n][m] pivots (0-based). out_info[n] (may be
+ * NULL) gets 0 or k+1 for an exactly zero pivot at step k.
+ * Replaces scipy dgetrf in HomogeneousReactor._lapack_setup_wrapper (reactors.py:340-344). */
+int sf_newton_lu_batch(int n, int m, const double *J, const double *gamma_h, int precision, double *out_A,
+                       void *out_lu, int *out_piv, int *out_info, void *stream);
+/* Solve A_k x_k = b_k with the factors of sf_newton_lu_batch. precision 1 runs FP32 triangular solves with
+ * `refine` FP64 residual-refinement sweeps r = b - A x (A from out_A). Replaces scipy dgetrs
+ * (reactors.py:354-356). */
+int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const int *piv, int precision, int refine,
+                          const double *b, double *out_x, void *stream);
+
+/* --------------------------------------------------------------------------------------- batched integration */
+/* Controls of HomogeneousReactor.integrate / odesolve (reactors.py:429-611, integrator.py:229-713) with the
+ * reference defaults: ESDIRK64 (KennedyCarpenterS6P4Q3), simple Newton with frozen Jacobian, PI controller. */
+typedef struct sf_integrate_params {
+  double first_time_step;           /* 1e-6 */
+  double max_time_step;             /* 1e6 */
+  double transient_tolerance;       /* 1e-10 (PI target error) */
+  double nonlinear_tolerance;       /* 1e-12 */
+  int minimum_time_step_count;      /* 40 */
+  int maximum_time_step_count;      /* hard cap on accepted steps (the reference default is unbounded) */
+  int max_nonlinear_iter;           /* 20 */
+  int maximum_steps_per_jacobian;   /* 1 */
+  double stop_at_time;              /* > 0: stop (and land exactly) at this time; <= 0: none */
+  double delta_temperature_ignition;/* > 0: stop when T > T0 + delta (compute_ignition_delay) */
+  double minimum_allowable_residual;/* ignition stop: residual below this marks "will not ignite" */
+  double stop_at_steady;            /* > 0: stop when residual < this */
+  int linear_precision;             /* 0 FP64 LU, 1 FP32 LU + FP64 refinement */
+  int refine_sweeps;                /* refinement sweeps for linear_precision 1 */
+  int rates_option;                 /* 0 dense exact (default), 2 sparse exact */
+  int max_attempts;                 /* cap on step attempts (accepted + failed) per reactor */
+} sf_integrate_params;
+
+/* Per-reactor outcome codes written to out_status. */
+enum sf_integrate_status {
+  SF_INT_RUNNING = 0, SF_INT_DONE = 1, SF_INT_IGNITED = 2, SF_INT_STEADY = 3, SF_INT_MAX_STEPS = 4,
+  SF_INT_NAN = 5, SF_INT_NO_IGNITION = 6
+};
+
+size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
+/* Integrate n independent closed reactors of the same configuration from q0 (state-major; isobaric reactors
+ * may each have their own pressure). One persistent launch works through the batch: each warp takes the next
+ * unfinished reactor from a queue, so reactors with 10x more steps do not stall the rest. Outputs: final states
+ * out_q, final time out_t, per-reactor counters out_counts[n][4] = steps, Newton iterations, Jacobian setups,
+ * failed steps, and status codes. out_t of an ignition run is the ignition delay (the end time of the first
+ * accepted step with T > T0 + delta, reactors.py:774-790). */
+int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *params, const sf_integrate_params *iparams,
+                       int n, const double *q0, const double *pressures, double *out_q, double *out_t,
+                       int *out_counts, int *out_status, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------------------------------ flamelets */
+/* Stencil coefficients (flamelet_kernels.cpp:31-48); host pointers, host computation (setup only). */
+int sf_flamelet_stencils(const sf_mech *mech, const double *dz, int nzi, const double *chi,
+                         const double *inv_lewis, double *out_cmajor, double *out_csub, double *out_csup,
+                         double *out_mcoeff, double *out_ncoeff);
+/* COO indices of the BTDDOD Jacobian (flamelet_kernels.cpp:50-90); host pointers. */
+int sf_flamelet_jac_indices(const sf_mech *mech, int nzi, int *out_rows, int *out_cols);
+
+/* A batch of adiabatic flamelets, each with its own grid size; arrays are concatenated over flamelets.
+ * offsets_z[f] is the first interior point of flamelet f in point-indexed arrays (state has ns values per point,
+ * chi one per point, stencils ns per point, m/n one per point); offsets_z[n_flamelets] = total points.
+ * Value arrays use offsets_v[f] = offset of flamelet f's BTDDOD value block (ns*(nzi*ns + 2*(nzi-1)) each). */
+typedef struct sf_flamelet_batch {
+  int n_flamelets;
+  const int *offsets_z;     /* DEVICE [n_flamelets+1] */
+  const long long *offsets_v; /* DEVICE [n_flamelets+1] */
+  const int *offsets_z_host;  /* HOST copy of offsets_z */
+  double pressure;
+  const double *oxy_state;  /* DEVICE [n_flamelets][ns] boundary state [T, Y_0..Y_{ns-2}] at Z = 0 */
+  const double *fuel_state; /* DEVICE [n_flamelets][ns] boundary state at Z = 1 */
+  const double *cmajor, *csub, *csup; /* DEVICE [points][ns] */
+  const double *mcoeff, *ncoeff, *chi; /* DEVICE [points] */
+  int include_enthalpy_flux;
+  int include_variable_cp;
+} sf_flamelet_batch;
+
+/* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218, adiabatic path). */
+int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, double *out_rhs,
+                          void *stream);
+/* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, adiabatic path, rates option 0/2, exact transform).
+ * If scale_and_offset, J <- prefactor*J - I on the diagonal blocks (flamelet_kernels.cpp:1395-1408). If
+ * out_expeig is non-NULL it receives, per point, an upper bound of max(Re(lambda) - diffterm, 0) of the block
+ * (replacing the dgeev call at flamelet_kernels.cpp:1329-1341; see DESIGN for the bound). */
+int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, int rates_option,
+                          int scale_and_offset, double prefactor, double diffterm, double *out_expeig,
+                          double *out_values, void *stream);
+
+/* Block-Thomas factorization of a batch of BTDDOD matrices, in place (btddod_matrix_kernels.cpp:19-80).
+ * values: DEVICE, layout per flamelet as above; l_values: DEVICE scratch-like output of nzi*ns*ns per flamelet at
+ * point offset offsets_z[f]*ns*ns; pivots: DEVICE int [points][ns]. */
+int sf_btddod_factor_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
+                           const int *offsets_z_host, double *values, double *l_values, int *pivots, void *stream);
+/* Solve with the factors (btddod_matrix_kernels.cpp:82-119). rhs and out_x are point-major [points][ns]. */
+int sf_btddod_solve_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
+                          const int *offsets_z_host, const double *values, const double *l_values,
+                          const int *pivots, const double *rhs, double *out_x, void *stream);
+/* y = A x for a batch of BTDDOD matrices (btddod_matrix_kernels.cpp:121-160). */
+int sf_btddod_matvec_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
+                           const double *values, const double *x, double *out_y, void *stream);
+/* A <- matrix_scale*A + diag_scale*diag(d) (btddod_matrix_kernels.cpp:448-465). */
+int sf_btddod_scale_and_add_diagonal_batch(int n_flamelets, int ns, const int *offsets_z,
+                                           const long long *offsets_v, const int *offsets_z_host, double *values,
+                                           double matrix_scale, const double *diagonal, double diag_scale,
+                                           void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPITFIRE_GB300_H */
