@@ -110,6 +110,10 @@ typedef struct sf_mech sf_mech; /* opaque: host tables + device blob on one CUDA
 int sf_mech_create(const sf_mech_desc *desc, sf_mech **out_mech);
 /* Replaces PyCombustionKernels.__dealloc__ (griffon.pyx:228-229). */
 int sf_mech_destroy(sf_mech *mech);
+/* Device error word of the kernels that use this mechanism: 0, or the first code a kernel recorded
+ * (1 shared-memory staging timed out, 2 invalid input, 3 a bounded wait ran out). Synchronizes the device.
+ * clear != 0 resets it. Returns -1 on a CUDA failure. */
+int sf_device_status(const sf_mech *mech, int clear);
 /* Sizes of a built mechanism; counts[0..5] = reactions by kind: simple, three-body, Lindemann, Troe, dense
  * (Jacobian rows that need the dense term), special-order. Any output pointer may be NULL. */
 int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *counts6);

@@ -1,0 +1,531 @@
+// Batched thermochemistry kernels: production rates, rate sensitivities, reactor right-hand sides and analytical
+// Jacobians (isochoric and isobaric), one state group of G lanes per state.
+//
+// Phases per state (group-synchronous):
+//   P0  load the state; mixture molecular weight and density              (reduction over species)
+//   P1  concentrations and species thermodynamics                         (lanes over species)
+//   P2  reaction rates q_r and, for Jacobians, their derivatives           (lanes over reactions)
+//   P3  species gathers w_i, S_rho_i, S_T_i, P_i, Q_i                      (gather program)
+//   P4  right-hand side, rho/T columns, dense-term coefficients            (lanes over species)
+//   P5  Y-block of the Jacobian and T-row sums                             (gather program)
+//   P6  T row of the Jacobian                                              (lanes over columns)
+// Reference: isochoric_reactor_kernels.cpp:18-333, isobaric_reactor_kernels.cpp:19-343,
+//            chemistry_kernels.cpp:35-483, rates_sensitivities_exact.cpp:33-1028.
+#include "chem_device.cuh"
+#include "sf_internal.h"
+
+namespace sfgb {
+
+enum Mode { MODE_RATES = 0, MODE_SENS = 1, MODE_RHS = 2, MODE_JAC = 3 };
+
+struct KParams {
+  DevMech m;
+  const void *blob;
+  int *status;
+  ScratchLayout L;
+  DevProgram prog_w, prog_full, prog_j;
+  int n;
+  int option;
+  // inputs
+  const double *T, *rho, *Y;      // RATES / SENS
+  const double *q, *pressures;    // RHS / JAC
+  int configuration;              // 0 isobaric, 1 isochoric
+  int heat;                       // 0 adiabatic, 1 isothermal, 2 diathermal
+  double pressure, Tc, Tr, hc, eps, SoV;
+  // outputs
+  double *out_w, *out_S, *out_rhs, *out_J;
+  int groups_per_cta;
+};
+
+template <int G>
+struct JWriter {
+  double *J;
+  int ld;       // leading dimension (neq or ns+1)
+  int roff;     // row offset of species rows
+  int coff;     // column offset of Y columns
+  double scale;
+  __device__ __forceinline__ void operator()(int row, int col, double v) const
+  {
+    J[(size_t)(coff + col) * ld + roff + row] = v * scale;
+  }
+};
+
+template <int G, int MODE>
+__global__ void __launch_bounds__(256) chem_kernel(const KParams p)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar;
+  const DevMech &m = p.m;
+  if (!stage_to_smem(smem, p.blob, m.blob_bytes, &bar, p.status)) return;
+  const Blob b = blob_at(m, smem);
+  const ScratchLayout &L = p.L;
+  const int gid = threadIdx.x / G;
+  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? L.total : L.total_rhs;
+  double *scr = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)gid * scr_doubles;
+  const Group<G> grp;
+  const int lane = grp.lane;
+  const int ns = m.ns, nr = m.nr;
+  constexpr bool JAC = (MODE == MODE_JAC || MODE == MODE_SENS);
+  const bool isochoric = p.configuration == 1;
+  const int neq = isochoric ? ns + 1 : ns;
+
+  for (int st = blockIdx.x * p.groups_per_cta + gid; st < p.n; st += gridDim.x * p.groups_per_cta) {
+    // ---------------- P0: state
+    double T, rho = 0., pres = 0.;
+    const double *qs = nullptr;
+    if (MODE == MODE_RATES || MODE == MODE_SENS) {
+      T = p.T[st];
+      rho = p.rho[st];
+    } else {
+      qs = p.q + (size_t)st * neq;
+      if (isochoric) {
+        rho = qs[0];
+        T = qs[1];
+      } else {
+        T = qs[0];
+        pres = p.pressures ? p.pressures[st] : p.pressure;
+      }
+    }
+    double sy = 0., sim = 0.;
+    if (MODE == MODE_RATES || MODE == MODE_SENS) {
+      for (int i = lane; i < ns; i += G) scr[L.y + i] = p.Y[(size_t)st * ns + i];
+    } else {
+      for (int i = lane; i < ns - 1; i += G) {
+        const double yi = qs[(isochoric ? 2 : 1) + i];
+        scr[L.y + i] = yi;
+        sy += yi;
+      }
+      sy = grp.sum(sy);
+      if (lane == 0) scr[L.y + ns - 1] = 1. - sy;  // extract_y (combustion_kernels.h:526-535)
+    }
+    grp.sync();
+    for (int i = lane; i < ns; i += G) sim += scr[L.y + i] * b.d[m.d_invmw + i];
+    sim = grp.sum(sim);
+    const double mmw = 1. / sim;
+    if (!(MODE == MODE_RATES || MODE == MODE_SENS) && !isochoric) rho = pres * mmw / (T * m.Ru);
+    StateCtx s;
+    s.T = T;
+    s.logT = log(T);
+    s.invT = 1. / T;
+    s.rho = rho;
+    s.invRho = 1. / rho;
+    s.mmw = mmw;
+    s.invM = 1. / mmw;
+    s.ct = rho / mmw;
+    s.log_port = log(m.pref * s.invT * m.invRu);
+    s.option = p.option;
+
+    // ---------------- P1: species
+    double cpmix = 0., cpsens = 0.;
+    for (int i = lane; i < ns; i += G) {
+      const double yi = scr[L.y + i];
+      const double invmw = b.d[m.d_invmw + i];
+      scr[L.C + i] = yi * rho * invmw;
+      const SpeciesThermo th = species_thermo(m, b, i, T, s.logT, s.invT, JAC);
+      scr[L.gRT + i] = th.g * s.invT * m.invRu;
+      if (MODE != MODE_RATES) {
+        scr[L.eh + i] = isochoric ? th.h - m.Ru * T * invmw : th.h;
+        scr[L.cpv + i] = isochoric ? th.cp - m.Ru * invmw : th.cp;
+        cpmix += yi * th.cp;
+      } else {
+        scr[L.eh + i] = 0.;
+      }
+      // gather destinations start at zero: an entry with no contributions (e.g. an inert species) is never
+      // written by the gather program
+      scr[L.w + i] = 0.;
+      if (JAC) {
+        scr[L.dB + i] = th.dB;
+        scr[L.dcp + i] = th.dcp;
+        cpsens += yi * th.dcp;
+        scr[L.Srho + i] = 0.;
+        scr[L.ST + i] = 0.;
+        scr[L.P + i] = 0.;
+        scr[L.Q + i] = 0.;
+      }
+    }
+    cpmix = grp.sum(cpmix);
+    if (JAC) cpsens = grp.sum(cpsens);
+    const double cmix = isochoric ? cpmix - m.Ru / mmw : cpmix;  // cv or cp
+    grp.sync();
+
+    // ---------------- P2: reactions
+    double EA = 0., EB = 0.;
+    for (int r = lane; r < nr; r += G) eval_reaction<JAC>(m, b, L, scr, s, r, &EA, &EB);
+    if (JAC) {
+      EA = grp.sum(EA);
+      EB = grp.sum(EB);
+    }
+    grp.sync();
+
+    // ---------------- P3: species gathers
+    NoJ noj;
+    run_program<G>(JAC ? p.prog_full : p.prog_w, lane, b.d, scr, noj);
+    grp.sync();
+
+    if (MODE == MODE_RATES) {
+      for (int i = lane; i < ns; i += G) p.out_w[(size_t)st * ns + i] = scr[L.w + i];
+      grp.sync();
+      continue;
+    }
+
+    if (MODE == MODE_SENS) {
+      // Griffon's (ns+1)^2 column-major sensitivity block (rates_sensitivities_exact.cpp:1001-1026)
+      const int n1 = ns + 1;
+      double *S = p.out_S + (size_t)st * n1 * n1;
+      for (int i = lane; i < ns; i += G) {
+        p.out_w[(size_t)st * ns + i] = scr[L.w + i];
+        S[i] = scr[L.Srho + i];
+        S[n1 + i] = scr[L.ST + i];
+      }
+      for (int k = lane; k < n1; k += G) S[k * n1 + ns] = 0.;
+      // last-species row: dense part + sparse contributions, computed directly
+      grp.sync();
+      JWriter<G> jw{S, n1, 0, 2, rho};
+      run_program<G>(p.prog_j, lane, b.d, scr, jw);
+      grp.sync();
+      continue;
+    }
+
+    // ---------------- P4: right-hand side and rho/T columns
+    double swe = 0., sre = 0., ste = 0., swc = 0.;
+    for (int i = lane; i < ns; i += G) {
+      const double e = scr[L.eh + i];
+      swe += scr[L.w + i] * e;
+      if (JAC) {
+        sre += scr[L.Srho + i] * e;
+        ste += scr[L.ST + i] * e;
+        swc += scr[L.w + i] * scr[L.cpv + i];
+      }
+    }
+    swe = grp.sum(swe);
+    if (JAC) {
+      sre = grp.sum(sre);
+      ste = grp.sum(ste);
+      swc = grp.sum(swc);
+    }
+    const double invRho = s.invRho;
+    const double iC = 1. / cmix, iRC = 1. / (rho * cmix);
+    double rhsT = -swe / (rho * cmix);
+    double qheat = 0.;
+    if (p.heat == 2)
+      qheat = p.SoV / (rho * cmix) *
+              (p.hc * (p.Tc - T) + p.eps * 5.67e-8 * (p.Tr * p.Tr * p.Tr * p.Tr - T * T * T * T));
+    double *rhs = p.out_rhs + (size_t)st * neq;
+    const int tix = isochoric ? 1 : 0;  // index of T in the state
+    for (int i = lane; i < ns - 1; i += G) rhs[tix + 1 + i] = scr[L.w + i] * invRho;
+    if (lane == 0) {
+      if (isochoric) rhs[0] = 0.;
+      rhs[tix] = p.heat == 1 ? 0. : rhsT + qheat;
+    }
+    if (MODE == MODE_RHS) {
+      grp.sync();
+      continue;
+    }
+
+    double *J = p.out_J + (size_t)st * neq * neq;
+    // primitive rho and T columns of the T row (chem_jac_isochoric / chem_jac_isobaric)
+    const double JTrho = -iRC * sre - invRho * rhsT;
+    const double JTT = -iC * (invRho * (ste + swc) + rhsT * cpsens);
+    const double cpv_last = scr[L.cpv + ns - 1];
+    if (isochoric) {
+      // rows 2+i: rho column invRho*(S_rho - invRho*w), T column invRho*S_T; P, Q unchanged
+      for (int i = lane; i < ns - 1; i += G) {
+        J[2 + i] = invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]);
+        J[neq + 2 + i] = invRho * scr[L.ST + i];
+      }
+    } else {
+      // isobaric transform (isobaric_reactor_kernels.cpp:319-343): T column = PJ_T - rho/T * PJ_rho,
+      // Y columns get (-rho*mmw) * u_k * PJ_rho -> folded into P
+      const double roT = rho / T, nrm = -rho * mmw;
+      for (int i = lane; i < ns - 1; i += G) {
+        const double pjr = invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]);
+        const double pjt = invRho * scr[L.ST + i];
+        J[1 + i] = pjt - roT * pjr;
+        scr[L.P + i] += nrm * pjr;
+      }
+    }
+    for (int k = lane; k < ns; k += G) scr[L.trow + k] = 0.;
+    grp.sync();
+
+    // ---------------- P5: Y block and T-row sums
+    if (isochoric) {
+      JWriter<G> jw{J, neq, 2, 2, 1.};
+      run_program<G>(p.prog_j, lane, b.d, scr, jw);
+    } else {
+      JWriter<G> jw{J, neq, 1, 1, 1.};
+      run_program<G>(p.prog_j, lane, b.d, scr, jw);
+    }
+    grp.sync();
+
+    // ---------------- P6: T row (and the zero rho row of the isochoric Jacobian)
+    const double iso_heat = (p.heat == 1) ? 0. : 1.;
+    if (isochoric) {
+      for (int k = lane; k < ns - 1; k += G) {
+        const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
+        double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
+        if (p.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
+        J[(2 + k) * neq + 1] = v * iso_heat;
+      }
+      for (int k = lane; k < neq; k += G) J[k * neq] = 0.;
+      if (lane == 0) {
+        double j10 = JTrho, j11 = JTT;
+        if (p.heat == 2) {
+          j10 += -qheat / rho;
+          j11 += -iC * cpsens * qheat - p.SoV * iRC * (p.hc + 4. * p.eps * 5.67e-8 * T * T * T);
+        }
+        J[1] = j10 * iso_heat;
+        J[neq + 1] = j11 * iso_heat;
+      }
+    } else {
+      const double roT = rho / T, nrm = -rho * mmw;
+      double pjr = JTrho, pjt = JTT;
+      if (p.heat == 2) {
+        pjr += -qheat / rho;
+        pjt += -iC * cpsens * qheat - p.SoV * iRC * (p.hc + 4. * p.eps * 5.67e-8 * T * T * T);
+      }
+      pjr *= iso_heat;
+      pjt *= iso_heat;
+      for (int k = lane; k < ns - 1; k += G) {
+        const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
+        double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
+        if (p.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
+        J[(1 + k) * ns] = v * iso_heat + nrm * b.d[m.d_u + k] * pjr;
+      }
+      if (lane == 0) J[0] = pjt - roT * pjr;
+    }
+    grp.sync();
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ launchers
+namespace {
+
+int pick_group(const DevMech &m) { return m.nr >= 96 || m.ns >= 24 ? 32 : (m.nr >= 24 ? 16 : 8); }
+
+template <int MODE>
+int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
+{
+  const int G = G_req > 0 ? G_req : pick_group(hm.dm);
+  const auto &progs = hm.programs_for(G);
+  p.m = hm.dm;
+  p.blob = hm.d_blob;
+  p.status = hm.d_status;
+  p.L = hm.sl;
+  p.prog_w = progs.progs[0];
+  p.prog_full = progs.progs[1];
+  p.prog_j = (MODE == MODE_SENS) ? progs.progs[3] : progs.progs[2];
+  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? hm.sl.total : hm.sl.total_rhs;
+  int dev;
+  CUDA_THROW(cudaGetDevice(&dev));
+  int smem_max, nsm;
+  CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const size_t per_group = (size_t)scr_doubles * 8;
+  const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
+  if ((size_t)smem_max <= (size_t)hm.dm.blob_bytes + per_group)
+    throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory kernels");
+  int groups = (int)std::min<size_t>(avail / per_group, 256 / G);
+  groups = std::max(groups, 1);
+  p.groups_per_cta = groups;
+  const size_t smem = hm.dm.blob_bytes + per_group * groups;
+  const int threads = groups * G;
+  void (*kern)(const KParams);
+  switch (G) {
+  case 8: kern = chem_kernel<8, MODE>; break;
+  case 16: kern = chem_kernel<16, MODE>; break;
+  default: kern = chem_kernel<32, MODE>; break;
+  }
+  CUDA_THROW(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks_per_sm = std::max(1, (int)(((size_t)smem_max) / smem));
+  const long long need = ((long long)p.n + groups - 1) / groups;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(need, (long long)nsm * blocks_per_sm));
+  if (p.n == 0) return SF_OK;
+  kern<<<grid, threads, smem, st>>>(p);
+  CUDA_THROW(cudaGetLastError());
+  return SF_OK;
+}
+
+}  // namespace
+
+int chem_launch(HostMech &hm, int mode, KParams &p, cudaStream_t st, int G)
+{
+  switch (mode) {
+  case MODE_RATES: return launch_mode<MODE_RATES>(hm, p, st, G);
+  case MODE_SENS: return launch_mode<MODE_SENS>(hm, p, st, G);
+  case MODE_RHS: return launch_mode<MODE_RHS>(hm, p, st, G);
+  default: return launch_mode<MODE_JAC>(hm, p, st, G);
+  }
+}
+
+}  // namespace sfgb
+
+// ================================================================================================== C ABI
+using namespace sfgb;
+
+namespace {
+thread_local std::string t_err;
+template <class F>
+int guard(F f)
+{
+  try {
+    t_err.clear();
+    return f();
+  } catch (sf_error &e) {
+    t_err = e.what();
+    return e.code;
+  } catch (std::exception &e) {
+    t_err = e.what();
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+}
+int group_override()
+{
+  const char *e = getenv("SF_GROUP_LANES");
+  return e ? atoi(e) : 0;
+}
+}  // namespace
+
+void sfgb::set_error(const std::string &msg) { t_err = msg; }
+
+extern "C" {
+
+const char *sf_last_error(void) { return t_err.c_str(); }
+const char *sf_version(void) { return "spitfire_gb300 0.1 (sm_103a)"; }
+
+int sf_mech_create(const sf_mech_desc *desc, sf_mech **out)
+{
+  return guard([&] {
+    if (!desc || !out) throw sf_error(SF_ERR_INVALID_ARGUMENT, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw sf_error(SF_ERR_NO_DEVICE, "no CUDA device");
+    auto *m = new sf_mech();
+    try {
+      m->m.build(desc);
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    *out = m;
+    return SF_OK;
+  });
+}
+
+int sf_mech_destroy(sf_mech *m)
+{
+  delete m;
+  return SF_OK;
+}
+
+int sf_mech_info(const sf_mech *m, int *ns, int *nr, int *counts)
+{
+  return guard([&] {
+    if (!m) throw sf_error(SF_ERR_INVALID_ARGUMENT, "null mechanism");
+    if (ns) *ns = m->m.dm.ns;
+    if (nr) *nr = m->m.dm.nr;
+    if (counts) {
+      int c[6] = {0, 0, 0, 0, 0, 0};
+      for (const auto &x : m->m.rx) {
+        c[x.kind - 1]++;
+        if (x.dense) c[4]++;
+        if (x.has_orders) c[5]++;
+      }
+      for (int i = 0; i < 6; ++i) counts[i] = c[i];
+    }
+    return SF_OK;
+  });
+}
+
+int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const double *rho, const double *Y,
+                              double *out_w, void *stream)
+{
+  return guard([&] {
+    if (!mech || n < 0 || (n > 0 && (!T || !rho || !Y || !out_w))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    KParams p{};
+    p.n = n;
+    p.T = T;
+    p.rho = rho;
+    p.Y = Y;
+    p.out_w = out_w;
+    p.configuration = 0;
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RATES, p, (cudaStream_t)stream, group_override());
+  });
+}
+
+int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const double *T, const double *Y, int option,
+                        double *out_w, double *out_sens, void *stream)
+{
+  return guard([&] {
+    if (!mech || n < 0 || (n > 0 && (!T || !rho || !Y || !out_w || !out_sens)))
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    if (option < 0 || option > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "rates sensitivity option must be 0, 1 or 2");
+    KParams p{};
+    p.n = n;
+    p.T = T;
+    p.rho = rho;
+    p.Y = Y;
+    p.option = option;
+    p.out_w = out_w;
+    p.out_S = out_sens;
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_SENS, p, (cudaStream_t)stream, group_override());
+  });
+}
+
+static void fill_reactor(KParams &p, const sf_reactor_params *rp)
+{
+  if (!rp) throw sf_error(SF_ERR_INVALID_ARGUMENT, "null reactor params");
+  if (rp->configuration != 0 && rp->configuration != 1) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad configuration");
+  if (rp->heat_transfer < 0 || rp->heat_transfer > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad heat_transfer");
+  if (rp->open) throw sf_error(SF_ERR_UNSUPPORTED, "open (mass-exchange) reactors are not on the GPU path");
+  p.configuration = rp->configuration;
+  p.heat = rp->heat_transfer;
+  p.pressure = rp->pressure;
+  p.Tc = rp->fluid_temperature;
+  p.Tr = rp->surface_temperature;
+  p.hc = rp->h_convection;
+  p.eps = rp->eps_radiation;
+  p.SoV = rp->surface_area_to_volume;
+}
+
+int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *rp, int n, const double *q,
+                         const double *pressures, double *out_rhs, void *stream)
+{
+  return guard([&] {
+    if (!mech || n < 0 || (n > 0 && (!q || !out_rhs))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    KParams p{};
+    fill_reactor(p, rp);
+    p.n = n;
+    p.q = q;
+    p.pressures = pressures;
+    p.out_rhs = out_rhs;
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RHS, p, (cudaStream_t)stream, group_override());
+  });
+}
+
+int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n, const double *q,
+                         const double *pressures, double *out_rhs, double *out_jac, void *stream)
+{
+  return guard([&] {
+    if (!mech || n < 0 || (n > 0 && (!q || !out_rhs || !out_jac))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    if (rates_option < 0 || rates_option > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "rates option must be 0, 1 or 2");
+    KParams p{};
+    fill_reactor(p, rp);
+    p.n = n;
+    p.q = q;
+    p.pressures = pressures;
+    p.option = rates_option;
+    p.out_rhs = out_rhs;
+    p.out_J = out_jac;
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_JAC, p, (cudaStream_t)stream, group_override());
+  });
+}
+
+int sf_device_status(const sf_mech *mech, int clear)
+{
+  if (!mech || !mech->m.d_status) return -1;
+  int v = 0;
+  if (cudaMemcpy(&v, mech->m.d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (clear && v) cudaMemset(mech->m.d_status, 0, sizeof(int));
+  return v;
+}
+
+}  // extern "C"

@@ -529,6 +529,34 @@ class ChemicalMechanismSpec:
             else:
                 raise ValueError(f'unknown reaction kind {kind}')
 
+    # --- JSON form of mech_data (bundled mechanisms, spitfire_gb300/data) ---
+    def mech_data_json(self):
+        md = dict(self._mech_data)
+        md['species_order'] = list(self._species_names)
+        md['element_mw_map'] = {k: float(v) for k, v in md['element_mw_map'].items()}
+        md['species'] = {s: {'atom_map': v['atom_map'], 'cp': [float(c) if not isinstance(c, (str, list)) else c
+                                                                 for c in v['cp']]}
+                         for s, v in md['species'].items()}
+        md['reactions'] = [list(r) for r in md['reactions']]
+        return md
+
+    @classmethod
+    def from_json(cls, path):
+        import json
+        with open(path) as f:
+            md = json.load(f)
+        order = md.pop('species_order')
+        md['species'] = {s: {'atom_map': md['species'][s]['atom_map'], 'cp': tuple(md['species'][s]['cp'])}
+                         for s in order}
+        md['reactions'] = [tuple(r) for r in md['reactions']]
+        return cls(mech_data=md)
+
+    @classmethod
+    def bundled(cls, name):
+        """A mechanism shipped in spitfire_gb300/data (h2-burke, methane-gri30, reaction-test, unit-*)."""
+        import os
+        return cls.from_json(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'data', name + '.json'))
+
     # --- pickling as in mechanism.py:108-115 ---
     def __getstate__(self):
         return dict({'mech_data': self._mech_data, 'element_stoichiometry': self._element_stoichiometry})
