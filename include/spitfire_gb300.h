@@ -290,6 +290,12 @@ int sf_btddod_scale_and_add_diagonal_batch(int n_flamelets, int ns, const int *o
                                            double matrix_scale, const double *diagonal, double diag_scale,
                                            void *stream);
 
+/* ------------------------------------------------------------------------------------------- measurement */
+/* Measured FP64 FMA throughput of the current device (TFLOP/s): independent register FMA chains on every SM,
+ * timed with CUDA events; synchronizes the stream. sink: DEVICE pointer to one double. No reference counterpart:
+ * it gives the FP64 roofline denominator of the benchmark. */
+int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,7 @@ def _declare(L):
     L.sf_btddod_factor_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_btddod_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_btddod_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.sf_fp64_peak_probe.argtypes = [_ip, C.POINTER(C.c_double), _vp, _vp]
     L.sf_btddod_scale_and_add_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                                          C.c_double, _vp]
 
@@ -63,7 +64,7 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_newton_lu_batch', 'sf_newton_solve_batch', 'sf_integrate_workspace_size', 'sf_integrate_batch',
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',
-            'sf_btddod_scale_and_add_diagonal_batch']
+            'sf_btddod_scale_and_add_diagonal_batch', 'sf_fp64_peak_probe']
 
 
 def load(path=None):

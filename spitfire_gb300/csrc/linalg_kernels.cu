@@ -288,3 +288,59 @@ int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const i
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------ FP64 pipe peak probe
+// Independent FP64 FMA chains in registers (8 per thread, no memory traffic), for the FP64 roofline denominator:
+// the measured-peaks file of this machine has HBM and bf16 figures only.
+namespace sfgb {
+namespace {
+__global__ void fp64_probe_kernel(int iters, double seed, double *sink)
+{
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + k * 1e-3 + threadIdx.x * 1e-7;
+  const double b = 0.999999999, c = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == 12345.678) sink[0] = s;  // keeps the chains live
+}
+}  // namespace
+}  // namespace sfgb
+
+extern "C" int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream)
+{
+  if (!out_tflops || !sink || iters < 1) {
+    set_error("sf_fp64_peak_probe: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  int dev, nsm;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = nsm * 8, threads = 256;
+  fp64_probe_kernel<<<blocks, threads, 0, st>>>(16, 1.0, sink);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, st);
+  fp64_probe_kernel<<<blocks, threads, 0, st>>>(iters, 1.0, sink);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return SF_ERR_CUDA;
+  }
+  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  *out_tflops = flops / (ms * 1e-3) / 1e12;
+  return SF_OK;
+}
