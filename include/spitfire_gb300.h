@@ -180,6 +180,24 @@ int sf_reactor_jac_plain_batch(const sf_mech *mech, const sf_reactor_params *par
                                const double *pressures, double *out_rhs, double *out_jac, void *workspace,
                                size_t workspace_bytes, void *stream);
 
+/* Size of the fixed device scratch used by sf_reactor_jac_plain_batch_static: 32 MiB on each device. */
+#define SF_PLAIN_STATIC_SCRATCH_BYTES (32u << 20)
+
+/* sf_reactor_jac_plain_batch without any allocation. No counterpart in the reference: it is for callers that
+ * cannot allocate device memory where they evaluate Jacobians (a host code whose memory manager owns every
+ * device allocation and forbids raw cudaMalloc, or a caller that must not allocate while it records work on its
+ * streams). Instead of a caller-provided workspace, the per-state scratch comes from a fixed array of
+ * SF_PLAIN_STATIC_SCRATCH_BYTES in device global memory that the library holds on every device that loads it,
+ * until the process exits; inputs and outputs are still the caller's. The first call on a device looks up that
+ * array's device address (a runtime query, no allocation), so make the first call on each device before any
+ * stream capture. Batches whose scratch does not fit (n * per-state scratch > 32 MiB; about 600 GRI-3.0 states or
+ * 8000 h2-burke states) are rejected with SF_ERR_WORKSPACE and a message giving the limit. All calls on a device
+ * share the array: two calls that run at the same time on the GPU (e.g. on different streams) overwrite each
+ * other's scratch and give wrong results; serialize them. Each call rewrites all scratch it reads, so contents
+ * left by an earlier call do no harm. */
+int sf_reactor_jac_plain_batch_static(const sf_mech *mech, const sf_reactor_params *params, int n, const double *q,
+                                      const double *pressures, double *out_rhs, double *out_jac, void *stream);
+
 /* ------------------------------------------------------------------------------------------- Newton algebra */
 /* Factor the Newton iteration matrices A_k = gamma_h[k] * J_k - I (m x m column-major, n of them).
  * precision: 0 FP64 LU with partial pivoting (as LAPACK dgetrf, reactors.py:340-344); 1 FP32 LU of the same

@@ -38,6 +38,7 @@ def _declare(L):
     L.sf_reactor_jac_plain_workspace_size.restype = C.c_size_t
     L.sf_reactor_jac_plain_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp, _vp,
                                              C.c_size_t, _vp]
+    L.sf_reactor_jac_plain_batch_static.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp, _vp]
     L.sf_newton_lu_batch.argtypes = [_ip, _ip, _vp, _vp, _ip, _vp, _vp, _vp, _vp, _vp]
     L.sf_newton_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _ip, _ip, _vp, _vp, _vp]
     L.sf_integrate_workspace_size.argtypes = [_vp, C.POINTER(SfReactorParams), _ip]
@@ -61,6 +62,7 @@ def _declare(L):
 EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 'sf_mech_info', 'sf_device_status',
             'sf_thermo_batch', 'sf_production_rates_batch', 'sf_rates_sens_batch', 'sf_reactor_rhs_batch',
             'sf_reactor_jac_batch', 'sf_reactor_jac_plain_workspace_size', 'sf_reactor_jac_plain_batch',
+            'sf_reactor_jac_plain_batch_static',
             'sf_newton_lu_batch', 'sf_newton_solve_batch', 'sf_integrate_workspace_size', 'sf_integrate_batch',
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',

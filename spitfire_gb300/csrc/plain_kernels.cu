@@ -8,6 +8,8 @@
 #include "chem_device.cuh"
 #include "sf_internal.h"
 
+#include <mutex>
+
 namespace sfgb {
 
 namespace {
@@ -267,3 +269,101 @@ int sf_thermo_batch(const sf_mech *mech, int what, int n, const double *T, const
 }
 
 }  // extern "C"
+
+// ======================================================================= plain Jacobian without any allocation
+// Some callers cannot allocate device memory at the point where they evaluate Jacobians: a host code that hands
+// all device memory to its own pool allocator and forbids raw cudaMalloc, or a caller that must not allocate
+// while other work is being recorded on its streams. sf_reactor_jac_plain_batch_static gives them the plain
+// Jacobian evaluation with its per-state scratch taken from a fixed array in device global memory that this
+// library owns for the lifetime of the process (on every device that loads the library), instead of a
+// caller-provided workspace.
+namespace sfgb {
+namespace {
+
+// Fixed scratch: SF_PLAIN_STATIC_SCRATCH_BYTES (32 MiB) per device, shared by every call of
+// sf_reactor_jac_plain_batch_static on that device.
+static __device__ __align__(256) double g_plain_static_scratch[SF_PLAIN_STATIC_SCRATCH_BYTES / sizeof(double)];
+
+constexpr int kMaxStaticDevices = 64;
+double *g_static_scratch_ptr[kMaxStaticDevices] = {nullptr};
+std::mutex g_static_scratch_mutex;
+
+// Device address of the fixed scratch on the current device. The host-side symbol is only a stand-in for the
+// device array, so the address is obtained once per device (with that device current) and cached.
+int static_scratch_address(double **out)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return SF_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxStaticDevices) {
+    set_error("sf_reactor_jac_plain_batch_static: device index out of range");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lock(g_static_scratch_mutex);
+  if (!g_static_scratch_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_plain_static_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error(std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+      return SF_ERR_CUDA;
+    }
+    g_static_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_static_scratch_ptr[dev];
+  return SF_OK;
+}
+
+}  // namespace
+}  // namespace sfgb
+
+extern "C" int sf_reactor_jac_plain_batch_static(const sf_mech *mech, const sf_reactor_params *rp, int n,
+                                                 const double *q, const double *pressures, double *out_rhs,
+                                                 double *out_jac, void *stream)
+{
+  if (!mech || !rp || n < 0 || (n > 0 && (!q || !out_rhs || !out_jac))) {
+    set_error("sf_reactor_jac_plain_batch_static: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  if (rp->open || rp->heat_transfer != 0) {
+    set_error("sf_reactor_jac_plain_batch_static: only closed adiabatic reactors");
+    return SF_ERR_UNSUPPORTED;
+  }
+  const int ns = mech->m.dm.ns;
+  const size_t per_state = (size_t)mech->m.sl.total + (size_t)(ns + 1) * (ns + 1) + ns + 2;
+  const size_t capacity = SF_PLAIN_STATIC_SCRATCH_BYTES / sizeof(double) / per_state;
+  if ((size_t)n > capacity) {
+    set_error("sf_reactor_jac_plain_batch_static: " + std::to_string(n) + " states exceed the fixed scratch (" +
+              std::to_string(capacity) + " states of this mechanism fit in " +
+              std::to_string(SF_PLAIN_STATIC_SCRATCH_BYTES >> 20) + " MiB); split the batch");
+    return SF_ERR_WORKSPACE;
+  }
+  if (n == 0) return SF_OK;
+  double *scratch = nullptr;
+  const int rc = static_scratch_address(&scratch);
+  if (rc != SF_OK) return rc;
+  // every value a state reads from its scratch slice is written earlier in the same launch (the S block and
+  // the species sums are zeroed per state), so leftover contents of earlier calls need no clearing
+  PlainParams p{};
+  p.m = mech->m.dm;
+  p.blob = mech->m.d_blob;
+  p.L = mech->m.sl;
+  p.n = n;
+  p.configuration = rp->configuration;
+  p.pressure = rp->pressure;
+  p.q = q;
+  p.pressures = pressures;
+  p.out_rhs = out_rhs;
+  p.out_J = out_jac;
+  p.ws = scratch;
+  p.per_state = per_state;
+  plain_jac_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    return SF_ERR_CUDA;
+  }
+  return SF_OK;
+}
