@@ -1,0 +1,190 @@
+"""ORACLE -- test infrastructure, not the product.
+
+CPU restatement of Spitfire's reactor time integration, as HomogeneousReactor.integrate runs it with its
+defaults: odesolve (src/spitfire/time/integrator.py:229-713) driving KennedyCarpenterS6P4Q3 (ESDIRK64,
+time/methods.py:441-612) with SimpleNewtonSolver (time/nonlinear.py:143-268, frozen Jacobian) and PIController
+(time/stepcontrol.py:50-117); the right-hand side and Jacobian come from the oracle's Griffon restatement and the
+linear algebra from LAPACK dgetrf/dgetrs through scipy, as in chemistry/reactors.py:340-356.
+Used by tests (ignition delays, step counts) and by the CPU baseline of the ignition benchmark.
+"""
+
+import numpy as np
+from scipy.linalg.lapack import dgetrf, dgetrs
+
+# ESDIRK64 tableau (methods.py:464-500)
+GAMMA = 0.25
+A = np.array([[0., 0., 0., 0., 0., 0.],
+              [0.25, GAMMA, 0., 0., 0., 0.],
+              [8611. / 62500., -1743. / 31250., GAMMA, 0., 0., 0.],
+              [5012029. / 34652500., -654441. / 2922500., 174375. / 388108., GAMMA, 0., 0.],
+              [15267082809. / 155376265600., -71443401. / 120774400., 730878875. / 902184768.,
+               2285395. / 8070912., GAMMA, 0.],
+              [82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., GAMMA]])
+B = A[5].copy()
+BH = np.array([4586570599. / 29645900160., 0., 178811875. / 945068544., 814220225. / 1159782912.,
+               -3700637. / 11593932., 61727. / 225920.])
+
+STATUS = {'done': 1, 'ignited': 2, 'steady': 3, 'max_steps': 4, 'nan': 5, 'no_ignition': 6}
+
+
+class ReactorProblem:
+    """Closed reactor RHS/Jacobian closures (reactors.py:538-592) over the oracle Griffon."""
+
+    def __init__(self, og, configuration, pressure=101325., heat='adiabatic'):
+        import oracle as orc
+        from spitfire_gb300._desc import reactor_params
+        self.og = og
+        self.configuration = configuration
+        self.pressure = pressure
+        self.P = reactor_params(configuration, heat, pressure=pressure)
+        self._yin = np.zeros(og.n_species)
+        self.P.inflow_Y = orc._p(self._yin)
+        self.Tidx = 0 if configuration == 'isobaric' else 1
+        self.pres = np.array([pressure]) if configuration == 'isobaric' else None
+
+    def rhs(self, q):
+        return self.og.reactor_rhs_batch(self.P, q[None, :], pressures=self.pres)[0]
+
+    def jac(self, q):
+        n = q.size
+        _, J = self.og.reactor_jac_batch(self.P, q[None, :], 0, pressures=self.pres)
+        return J[0].reshape((n, n), order='F')
+
+
+def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tolerance=1.e-10,
+              nonlinear_tolerance=1.e-12, minimum_time_step_count=40, maximum_time_step_count=np.inf,
+              max_nonlinear_iter=20, maximum_steps_per_jacobian=1, stop_at_time=None, delta_temperature_ignition=None,
+              minimum_allowable_residual=1.e-12, stop_at_steady=None, max_attempts=1000000, save_each_step=False):
+    """Returns dict(state, t, steps, newton_iters, jac_setups, failed_steps, status[, times, states])."""
+    neq = q0.size
+    w = np.ones(neq)
+    w[prob.Tidx] = 1. / 1.e3  # 1 / variable_scales (reactors.py:321-322)
+    T0 = q0[prob.Tidx]
+    state = q0.astype(np.float64).copy()
+    t = 0.
+    dt = first_time_step
+    eval_setup = True
+    setup_count = 0
+    nsteps = 0
+    nnewton = 0
+    njac = 0
+    nfail = 0
+    lu = piv = None
+    status = 0
+    coerce = stop_at_time is not None
+    times = [0.] if save_each_step else None
+    states = [state.copy()] if save_each_step else None
+    attempts = 0
+    while True:
+        attempts += 1
+        if attempts > max_attempts:
+            status = STATUS['max_steps']
+            break
+        if coerce and t + dt > stop_at_time:
+            dt = stop_at_time - t
+        if eval_setup:
+            Jm = prob.jac(state) * (dt * GAMMA)
+            Jm[np.diag_indices(neq)] -= 1.
+            lu, piv, _ = dgetrf(Jm)
+            njac += 1
+        setup_count += 1
+        # ---- ESDIRK64 single step (methods.py:502-612)
+        k = np.zeros((6, neq))
+        k[0] = prob.rhs(state)
+        Y = state.copy()
+        nl_ok = True
+        nl_slow = False
+        for s in range(1, 6):
+            prior = A[s, :s] @ k[:s]
+            resid = dt * (GAMMA * k[s - 1] + prior) - (Y - state)
+            conv = False
+            f = k[s - 1]
+            for it in range(1, max_nonlinear_iter + 1):
+                dx = dgetrs(lu, piv, resid)[0]
+                Y = Y - dx
+                f = prob.rhs(Y)
+                resid = dt * (GAMMA * f + prior) - (Y - state)
+                nnewton += 1
+                if np.max(np.abs(resid * w)) < nonlinear_tolerance:
+                    conv = True
+                    break
+            k[s] = f
+            if not conv:
+                nl_ok = False
+                nl_slow = True
+        dstate = dt * (B @ k)
+        dstate_h = dt * (BH @ k)
+        err = np.max(np.abs((dstate - dstate_h) * w))
+        residual = np.max(np.abs(dstate * w)) / dt
+        # ---- governor (integrator.py:540-640)
+        recent = dt
+        if np.all(np.isfinite(dstate)):
+            state = state + dstate
+            t = t + dt
+            nsteps += 1
+            state[state < 0.] = 0.  # post_step_callback (reactors.py:506-508)
+            if save_each_step:
+                times.append(t)
+                states.append(state.copy())
+            # PI controller (stepcontrol.py:84-101): after a step the P factor is exactly 1
+            if err < 1.e-16:
+                dt = min(dt * 1.1, max_time_step)
+            else:
+                dt = min(dt * min(1.1, (transient_tolerance / err) ** 0.1333333333), max_time_step)
+            # _check_linear_setup (integrator.py:100-130)
+            if setup_count == maximum_steps_per_jacobian:
+                setup_count = 0
+                eval_setup = True
+            elif nl_slow:
+                dt *= 0.8
+                eval_setup = True
+            elif not nl_ok:
+                dt *= 0.8
+                eval_setup = True
+            elif dt > recent * 1.05:
+                eval_setup = True
+            elif dt < recent * 0.9:
+                eval_setup = True
+            else:
+                eval_setup = False
+        else:
+            dt *= 0.8
+            eval_setup = True
+            nfail += 1
+        cont = True
+        if delta_temperature_ignition is not None:
+            ignited = state[prob.Tidx] > T0 + delta_temperature_ignition
+            if residual > minimum_allowable_residual:
+                cont = not ignited
+                if ignited:
+                    status = STATUS['ignited']
+            else:
+                status = STATUS['no_ignition']
+                break
+        if nsteps < minimum_time_step_count:
+            cont = True
+            if status == STATUS['ignited']:
+                status = 0
+        if nsteps > maximum_time_step_count:
+            cont = False
+            status = STATUS['max_steps']
+        elif coerce and t >= stop_at_time:
+            cont = False
+            if status == 0:
+                status = STATUS['done']
+        elif stop_at_steady is not None and residual < stop_at_steady:
+            cont = False
+            status = STATUS['steady']
+        if not cont:
+            break
+    out = dict(state=state, t=t, steps=nsteps, newton_iters=nnewton, jac_setups=njac, failed_steps=nfail,
+               status=status)
+    if save_each_step:
+        out['times'] = np.array(times)
+        out['states'] = np.array(states)
+    return out
+
+
+def ignition_delay(prob, q0, delta=400., **kw):
+    r = integrate(prob, q0, delta_temperature_ignition=delta, **kw)
+    return r['t'], r

@@ -1,0 +1,106 @@
+"""The oracle (CPU restatement) pinned against golden vectors produced by the reference Spitfire itself
+(tests/golden/make_golden.py): loader, Griffon kernels, and ESDIRK64 reactor integration."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import colmajor, pair, rownorm_err
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+
+
+def test_loader_matches_cantera_converted_mech_data():
+    """The project YAML loader reproduces the mech_data Cantera produced for h2-burke (embedded in the
+    reference's tests/tabulation/adiabatic_slfm/gold.pkl)."""
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    gold = json.load(open(os.path.join(GOLD, 'h2_mech_data.json')))
+    spec = ChemicalMechanismSpec.bundled('h2-burke')
+    md = json.loads(json.dumps(spec.mech_data, default=float))
+    for k in ('ref_pressure', 'ref_temperature', 'elements', 'gas_constant', 'element_mw_map'):
+        assert md[k] == gold[k], k
+    assert list(md['species']) == list(gold['species'])
+    for s in gold['species']:
+        assert md['species'][s]['atom_map'] == gold['species'][s]['atom_map']
+        assert list(md['species'][s]['cp']) == list(gold['species'][s]['cp'])
+    assert len(md['reactions']) == len(gold['reactions'])
+    for a, b in zip(md['reactions'], gold['reactions']):
+        assert list(a) == list(b)
+
+
+@pytest.mark.parametrize('name', ['h2-burke', 'methane-gri30', 'reaction-test'])
+def test_oracle_kernels_match_reference(name):
+    import oracle as orc
+    from spitfire_gb300._desc import reactor_params
+    g = np.load(os.path.join(GOLD, f'kernels_{name}.npz'))
+    spec, og = pair(name)
+    ns = spec.n_species
+    w = og.production_rates_batch(g['T'], g['rho'], g['Y'])
+    assert rownorm_err(w, g['w']) <= 1e-13
+    for opt in range(3):
+        _, S = og.rates_sens_batch(g['rho'], g['T'], g['Y'], opt)
+        assert rownorm_err(colmajor(S, ns + 1)[:, :ns], colmajor(g['S'][opt], ns + 1)[:, :ns]) <= 1e-13, opt
+    yin = np.zeros(ns)
+    Piv = reactor_params('isochoric')
+    Piv.inflow_Y = orc._p(yin)
+    Pib = reactor_params('isobaric')
+    Pib.inflow_Y = orc._p(yin)
+    assert rownorm_err(og.reactor_rhs_batch(Piv, g['qiv']), g['rhs_iv']) <= 1e-13
+    assert rownorm_err(og.reactor_rhs_batch(Pib, g['qib'], pressures=g['p']), g['rhs_ib']) <= 1e-13
+    r, J = og.reactor_jac_batch(Piv, g['qiv'], 0)
+    rb, Jb = og.reactor_jac_batch(Pib, g['qib'], 0, pressures=g['p'])
+    assert rownorm_err(r, g['jac_rhs_iv']) <= 1e-13
+    assert rownorm_err(rb, g['jac_rhs_ib']) <= 1e-13
+    # temperature rows of the artificial reaction-test mechanism are pure cancellation (terms ~1e21, value ~1e-2)
+    riv = slice(2, None) if name == 'reaction-test' else slice(0, None)
+    rib = slice(1, None) if name == 'reaction-test' else slice(0, None)
+    assert rownorm_err(colmajor(J, ns + 1)[:, riv], colmajor(g['Jiv'], ns + 1)[:, riv]) <= 1e-13
+    assert rownorm_err(colmajor(Jb, ns)[:, rib], colmajor(g['Jib'], ns)[:, rib]) <= 1e-13
+
+
+def _case_problem(case):
+    import integrate as I
+    name = case['mechanism']
+    spec, og = pair(name)
+    prob = I.ReactorProblem(og, case['configuration'], pressure=case['p'])
+    Y = np.array(case['Y0'])
+    T0 = case['T0']
+    if case['configuration'] == 'isobaric':
+        q0 = np.hstack([[T0], Y[:-1]])
+    else:
+        rho = case['p'] * (1. / (Y / spec.molecular_weights).sum()) / (8314.46261815324 * T0)
+        q0 = np.hstack([[rho, T0], Y[:-1]])
+    return prob, q0
+
+
+CASES = json.load(open(os.path.join(GOLD, 'ignition_ref.json')))
+
+
+@pytest.mark.parametrize('case', CASES, ids=[f"{c['mechanism']}-{c['configuration']}-{c['T0']:.0f}K-{c['phi']}"
+                                             for c in CASES])
+def test_oracle_ignition_matches_reference(case):
+    import integrate as I
+    prob, q0 = _case_problem(case)
+    tau, r = I.ignition_delay(prob, q0)
+    assert r['status'] == I.STATUS['ignited']
+    assert r['steps'] == case['steps']
+    assert abs(tau - case['tau']) / case['tau'] <= 1e-9
+
+
+def test_oracle_closed_reactor_trajectory_matches_gold():
+    """tests/reactor/closed_reactors/gold.pkl ('cp, adiabatic'): h2-burke, X = 2:1:3.74 H2:O2:N2, 1200 K, 1 atm,
+    integrate_to_steady (steady tolerance 1e-6); the reference stored 517 steps. The reference's own test compares
+    with rtol 1e-4 (tests/reactor/closed_reactors/test.py:26-28): the accepted-step sequence of adaptive ESDIRK
+    moves by ~1e-5 when a Newton solve lands next to its 1e-12 tolerance and its iteration count flips under
+    rounding-level differences (the reference run here differs from its own gold file by 1.9e-5 in time)."""
+    import integrate as I
+    g = np.load(os.path.join(GOLD, 'closed_reactor_gold.npz'))
+    t, T, Y = g['cp_adiabatic_t'], g['cp_adiabatic_T'], g['cp_adiabatic_Y']
+    spec, og = pair('h2-burke')
+    prob = I.ReactorProblem(og, 'isobaric', pressure=101325.)
+    q0 = np.hstack([[T[0]], Y[:-1, 0]])
+    r = I.integrate(prob, q0, stop_at_steady=1e-6, save_each_step=True)
+    assert r['steps'] == t.size - 1
+    assert np.max(np.abs(r['times'] - t) / np.maximum(t, 1e-300)) <= 1e-4
+    assert np.max(np.abs(r['states'][:, 0] - T) / T) <= 1e-4
