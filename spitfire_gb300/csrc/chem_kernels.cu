@@ -11,7 +11,7 @@
 //   P6  T row of the Jacobian                                              (lanes over columns)
 // Reference: isochoric_reactor_kernels.cpp:18-333, isobaric_reactor_kernels.cpp:19-343,
 //            chemistry_kernels.cpp:35-483, rates_sensitivities_exact.cpp:33-1028.
-#include "chem_device.cuh"
+#include "reactor_eval.cuh"
 #include "sf_internal.h"
 
 namespace sfgb {
@@ -50,6 +50,13 @@ struct JWriter {
   }
 };
 
+// Column-major neq x neq block in global memory.
+struct GlobalJ {
+  double *J;
+  int neq;
+  __device__ __forceinline__ void operator()(int row, int col, double v) const { J[(size_t)col * neq + row] = v; }
+};
+
 template <int G, int MODE>
 __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
 {
@@ -64,45 +71,39 @@ __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
   double *scr = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)gid * scr_doubles;
   const Group<G> grp;
   const int lane = grp.lane;
-  const int ns = m.ns, nr = m.nr;
+  const int ns = m.ns;
   constexpr bool JAC = (MODE == MODE_JAC || MODE == MODE_SENS);
-  const bool isochoric = p.configuration == 1;
-  const int neq = isochoric ? ns + 1 : ns;
+  Progs pg;
+  pg.w = p.prog_w;
+  pg.full = p.prog_full;
+  pg.j = p.prog_j;
+  ReactorCfg cfg;
+  cfg.configuration = p.configuration;
+  cfg.heat = p.heat;
+  cfg.option = p.option;
+  cfg.Tc = p.Tc;
+  cfg.Tr = p.Tr;
+  cfg.hc = p.hc;
+  cfg.eps = p.eps;
+  cfg.SoV = p.SoV;
+  const int neq = p.configuration == 1 ? ns + 1 : ns;
 
   for (int st = blockIdx.x * p.groups_per_cta + gid; st < p.n; st += gridDim.x * p.groups_per_cta) {
-    // ---------------- P0: state
-    double T, rho = 0., pres = 0.;
-    const double *qs = nullptr;
-    if (MODE == MODE_RATES || MODE == MODE_SENS) {
-      T = p.T[st];
-      rho = p.rho[st];
-    } else {
-      qs = p.q + (size_t)st * neq;
-      if (isochoric) {
-        rho = qs[0];
-        T = qs[1];
-      } else {
-        T = qs[0];
-        pres = p.pressures ? p.pressures[st] : p.pressure;
-      }
+    if (MODE == MODE_RHS || MODE == MODE_JAC) {
+      const double *qs = p.q + (size_t)st * neq;
+      const double pres = p.configuration == 1 ? 0. : (p.pressures ? p.pressures[st] : p.pressure);
+      GlobalJ gj{JAC ? p.out_J + (size_t)st * neq * neq : nullptr, neq};
+      reactor_eval<G, JAC>(m, b, L, scr, grp, qs, pres, cfg, pg, p.out_rhs + (size_t)st * neq, gj);
+      continue;
     }
-    double sy = 0., sim = 0.;
-    if (MODE == MODE_RATES || MODE == MODE_SENS) {
-      for (int i = lane; i < ns; i += G) scr[L.y + i] = p.Y[(size_t)st * ns + i];
-    } else {
-      for (int i = lane; i < ns - 1; i += G) {
-        const double yi = qs[(isochoric ? 2 : 1) + i];
-        scr[L.y + i] = yi;
-        sy += yi;
-      }
-      sy = grp.sum(sy);
-      if (lane == 0) scr[L.y + ns - 1] = 1. - sy;  // extract_y (combustion_kernels.h:526-535)
-    }
+    // ---------------- production rates / sensitivities at (T, rho, Y)
+    const double T = p.T[st], rho = p.rho[st];
+    for (int i = lane; i < ns; i += G) scr[L.y + i] = p.Y[(size_t)st * ns + i];
     grp.sync();
+    double sim = 0.;
     for (int i = lane; i < ns; i += G) sim += scr[L.y + i] * b.d[m.d_invmw + i];
     sim = grp.sum(sim);
     const double mmw = 1. / sim;
-    if (!(MODE == MODE_RATES || MODE == MODE_SENS) && !isochoric) rho = pres * mmw / (T * m.Ru);
     StateCtx s;
     s.T = T;
     s.logT = log(T);
@@ -114,185 +115,25 @@ __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
     s.ct = rho / mmw;
     s.log_port = log(m.pref * s.invT * m.invRu);
     s.option = p.option;
-
-    // ---------------- P1: species
-    double cpmix = 0., cpsens = 0.;
-    for (int i = lane; i < ns; i += G) {
-      const double yi = scr[L.y + i];
-      const double invmw = b.d[m.d_invmw + i];
-      scr[L.C + i] = yi * rho * invmw;
-      const SpeciesThermo th = species_thermo(m, b, i, T, s.logT, s.invT, JAC);
-      scr[L.gRT + i] = th.g * s.invT * m.invRu;
-      if (MODE != MODE_RATES) {
-        scr[L.eh + i] = isochoric ? th.h - m.Ru * T * invmw : th.h;
-        scr[L.cpv + i] = isochoric ? th.cp - m.Ru * invmw : th.cp;
-        cpmix += yi * th.cp;
-      } else {
-        scr[L.eh + i] = 0.;
-      }
-      // gather destinations start at zero: an entry with no contributions (e.g. an inert species) is never
-      // written by the gather program
-      scr[L.w + i] = 0.;
-      if (JAC) {
-        scr[L.dB + i] = th.dB;
-        scr[L.dcp + i] = th.dcp;
-        cpsens += yi * th.dcp;
-        scr[L.Srho + i] = 0.;
-        scr[L.ST + i] = 0.;
-        scr[L.P + i] = 0.;
-        scr[L.Q + i] = 0.;
-      }
-    }
-    cpmix = grp.sum(cpmix);
-    if (JAC) cpsens = grp.sum(cpsens);
-    const double cmix = isochoric ? cpmix - m.Ru / mmw : cpmix;  // cv or cp
-    grp.sync();
-
-    // ---------------- P2: reactions
-    double EA = 0., EB = 0.;
-    for (int r = lane; r < nr; r += G) eval_reaction<JAC>(m, b, L, scr, s, r, &EA, &EB);
-    if (JAC) {
-      EA = grp.sum(EA);
-      EB = grp.sum(EB);
-    }
-    grp.sync();
-
-    // ---------------- P3: species gathers
-    NoJ noj;
-    run_program<G>(JAC ? p.prog_full : p.prog_w, lane, b.d, scr, noj);
-    grp.sync();
-
+    prep_species<G, JAC>(m, b, L, scr, grp, s, false, MODE == MODE_SENS);
+    reactions_and_gathers<G, JAC>(m, b, L, scr, grp, s, pg);
     if (MODE == MODE_RATES) {
       for (int i = lane; i < ns; i += G) p.out_w[(size_t)st * ns + i] = scr[L.w + i];
       grp.sync();
       continue;
     }
-
-    if (MODE == MODE_SENS) {
-      // Griffon's (ns+1)^2 column-major sensitivity block (rates_sensitivities_exact.cpp:1001-1026)
-      const int n1 = ns + 1;
-      double *S = p.out_S + (size_t)st * n1 * n1;
-      for (int i = lane; i < ns; i += G) {
-        p.out_w[(size_t)st * ns + i] = scr[L.w + i];
-        S[i] = scr[L.Srho + i];
-        S[n1 + i] = scr[L.ST + i];
-      }
-      for (int k = lane; k < n1; k += G) S[k * n1 + ns] = 0.;
-      // last-species row: dense part + sparse contributions, computed directly
-      grp.sync();
-      JWriter<G> jw{S, n1, 0, 2, rho};
-      run_program<G>(p.prog_j, lane, b.d, scr, jw);
-      grp.sync();
-      continue;
-    }
-
-    // ---------------- P4: right-hand side and rho/T columns
-    double swe = 0., sre = 0., ste = 0., swc = 0.;
+    // Griffon's (ns+1)^2 column-major sensitivity block (rates_sensitivities_exact.cpp:1001-1026)
+    const int n1 = ns + 1;
+    double *S = p.out_S + (size_t)st * n1 * n1;
     for (int i = lane; i < ns; i += G) {
-      const double e = scr[L.eh + i];
-      swe += scr[L.w + i] * e;
-      if (JAC) {
-        sre += scr[L.Srho + i] * e;
-        ste += scr[L.ST + i] * e;
-        swc += scr[L.w + i] * scr[L.cpv + i];
-      }
+      p.out_w[(size_t)st * ns + i] = scr[L.w + i];
+      S[i] = scr[L.Srho + i];
+      S[n1 + i] = scr[L.ST + i];
     }
-    swe = grp.sum(swe);
-    if (JAC) {
-      sre = grp.sum(sre);
-      ste = grp.sum(ste);
-      swc = grp.sum(swc);
-    }
-    const double invRho = s.invRho;
-    const double iC = 1. / cmix, iRC = 1. / (rho * cmix);
-    double rhsT = -swe / (rho * cmix);
-    double qheat = 0.;
-    if (p.heat == 2)
-      qheat = p.SoV / (rho * cmix) *
-              (p.hc * (p.Tc - T) + p.eps * 5.67e-8 * (p.Tr * p.Tr * p.Tr * p.Tr - T * T * T * T));
-    double *rhs = p.out_rhs + (size_t)st * neq;
-    const int tix = isochoric ? 1 : 0;  // index of T in the state
-    for (int i = lane; i < ns - 1; i += G) rhs[tix + 1 + i] = scr[L.w + i] * invRho;
-    if (lane == 0) {
-      if (isochoric) rhs[0] = 0.;
-      rhs[tix] = p.heat == 1 ? 0. : rhsT + qheat;
-    }
-    if (MODE == MODE_RHS) {
-      grp.sync();
-      continue;
-    }
-
-    double *J = p.out_J + (size_t)st * neq * neq;
-    // primitive rho and T columns of the T row (chem_jac_isochoric / chem_jac_isobaric)
-    const double JTrho = -iRC * sre - invRho * rhsT;
-    const double JTT = -iC * (invRho * (ste + swc) + rhsT * cpsens);
-    const double cpv_last = scr[L.cpv + ns - 1];
-    if (isochoric) {
-      // rows 2+i: rho column invRho*(S_rho - invRho*w), T column invRho*S_T; P, Q unchanged
-      for (int i = lane; i < ns - 1; i += G) {
-        J[2 + i] = invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]);
-        J[neq + 2 + i] = invRho * scr[L.ST + i];
-      }
-    } else {
-      // isobaric transform (isobaric_reactor_kernels.cpp:319-343): T column = PJ_T - rho/T * PJ_rho,
-      // Y columns get (-rho*mmw) * u_k * PJ_rho -> folded into P
-      const double roT = rho / T, nrm = -rho * mmw;
-      for (int i = lane; i < ns - 1; i += G) {
-        const double pjr = invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]);
-        const double pjt = invRho * scr[L.ST + i];
-        J[1 + i] = pjt - roT * pjr;
-        scr[L.P + i] += nrm * pjr;
-      }
-    }
-    for (int k = lane; k < ns; k += G) scr[L.trow + k] = 0.;
+    for (int k = lane; k < n1; k += G) S[k * n1 + ns] = 0.;
     grp.sync();
-
-    // ---------------- P5: Y block and T-row sums
-    if (isochoric) {
-      JWriter<G> jw{J, neq, 2, 2, 1.};
-      run_program<G>(p.prog_j, lane, b.d, scr, jw);
-    } else {
-      JWriter<G> jw{J, neq, 1, 1, 1.};
-      run_program<G>(p.prog_j, lane, b.d, scr, jw);
-    }
-    grp.sync();
-
-    // ---------------- P6: T row (and the zero rho row of the isochoric Jacobian)
-    const double iso_heat = (p.heat == 1) ? 0. : 1.;
-    if (isochoric) {
-      for (int k = lane; k < ns - 1; k += G) {
-        const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
-        double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
-        if (p.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
-        J[(2 + k) * neq + 1] = v * iso_heat;
-      }
-      for (int k = lane; k < neq; k += G) J[k * neq] = 0.;
-      if (lane == 0) {
-        double j10 = JTrho, j11 = JTT;
-        if (p.heat == 2) {
-          j10 += -qheat / rho;
-          j11 += -iC * cpsens * qheat - p.SoV * iRC * (p.hc + 4. * p.eps * 5.67e-8 * T * T * T);
-        }
-        J[1] = j10 * iso_heat;
-        J[neq + 1] = j11 * iso_heat;
-      }
-    } else {
-      const double roT = rho / T, nrm = -rho * mmw;
-      double pjr = JTrho, pjt = JTT;
-      if (p.heat == 2) {
-        pjr += -qheat / rho;
-        pjt += -iC * cpsens * qheat - p.SoV * iRC * (p.hc + 4. * p.eps * 5.67e-8 * T * T * T);
-      }
-      pjr *= iso_heat;
-      pjt *= iso_heat;
-      for (int k = lane; k < ns - 1; k += G) {
-        const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
-        double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
-        if (p.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
-        J[(1 + k) * ns] = v * iso_heat + nrm * b.d[m.d_u + k] * pjr;
-      }
-      if (lane == 0) J[0] = pjt - roT * pjr;
-    }
+    JWriter<G> jw{S, n1, 0, 2, rho};
+    run_program<G>(p.prog_j, lane, b.d, scr, jw);
     grp.sync();
   }
 }

@@ -1,0 +1,380 @@
+// Batched adaptive ESDIRK64 integration of closed homogeneous reactors in one persistent launch.
+//
+// One warp integrates one reactor at a time and takes the next unfinished reactor from an atomic work queue when
+// it is done, so reactors with ten times more steps than others do not hold the rest back. Everything a reactor
+// needs between steps lives in the warp's shared memory: the state, the six stage derivatives, the Newton
+// iteration matrix A = dt*gamma*J - I and its LU factors, and the Griffon scratch of the right-hand side and
+// Jacobian evaluations.
+//
+// The step logic restates the reference's default reactor integration exactly, so that the accepted-step sequence
+// (and therefore the ignition delay, the end time of the first accepted step with T > T0 + delta) is the same:
+//   odesolve governor        src/spitfire/time/integrator.py:520-640 (Jacobian setup policy :100-130, failed
+//                            steps :82-97, stop rules :629-640)
+//   KennedyCarpenterS6P4Q3   src/spitfire/time/methods.py:441-612 (tableau :464-500)
+//   SimpleNewtonSolver       src/spitfire/time/nonlinear.py:185-268 (frozen Jacobian, inf-norm test, 20 iterations)
+//   PIController             src/spitfire/time/stepcontrol.py:84-101 (after the first step the P factor is 1)
+//   HomogeneousReactor       src/spitfire/chemistry/reactors.py:429-611 (weights 1/[1e3 on T], clamp of negative
+//                            entries after each step)
+#include "reactor_eval.cuh"
+#include "sf_internal.h"
+#include "warp_lu.cuh"
+
+namespace sfgb {
+namespace {
+
+constexpr double kGamma = 0.25;
+// ESDIRK64 stage coefficients a_sj (methods.py:464-500)
+__constant__ double c_a[6][6] = {
+    {0., 0., 0., 0., 0., 0.},
+    {0.25, 0.25, 0., 0., 0., 0.},
+    {8611. / 62500., -1743. / 31250., 0.25, 0., 0., 0.},
+    {5012029. / 34652500., -654441. / 2922500., 174375. / 388108., 0.25, 0., 0.},
+    {15267082809. / 155376265600., -71443401. / 120774400., 730878875. / 902184768., 2285395. / 8070912., 0.25, 0.},
+    {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25}};
+__constant__ double c_b[6] = {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25};
+__constant__ double c_bh[6] = {4586570599. / 29645900160., 0., 178811875. / 945068544., 814220225. / 1159782912.,
+                               -3700637. / 11593932., 61727. / 225920.};
+
+struct IntParams {
+  DevMech m;
+  const void *blob;
+  int *status;
+  ScratchLayout L;
+  Progs pg;
+  ReactorCfg cfg;
+  sf_integrate_params ip;
+  int n, neq, prec;
+  double pressure;
+  const double *pressures, *q0;
+  double *out_q, *out_t;
+  int *out_counts, *out_status;
+  unsigned int *queue;
+  size_t per_warp;  // doubles of shared memory per warp
+};
+
+// Writes A = pref * J - I straight from the Jacobian evaluation.
+struct IterMatrix {
+  double *A;
+  int neq;
+  double pref;
+  __device__ __forceinline__ void operator()(int row, int col, double v) const
+  {
+    A[col * neq + row] = pref * v - (row == col ? 1. : 0.);
+  }
+};
+
+__device__ __forceinline__ double warp_max(double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar;
+  const DevMech &m = p.m;
+  if (!stage_to_smem(smem, p.blob, m.blob_bytes, &bar, p.status)) return;
+  const Blob b = blob_at(m, smem);
+  const ScratchLayout &L = p.L;
+  const Group<32> grp;
+  const int lane = grp.lane;
+  const int warp = threadIdx.x >> 5;
+  const int neq = p.neq;
+  const sf_integrate_params &ip = p.ip;
+  double *base = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)warp * p.per_warp;
+  double *A = base;                                       // neq*neq
+  double *y = A + neq * neq;                              // current state
+  double *Y = y + neq;                                    // stage iterate
+  double *res = Y + neq;                                  // Newton residual / step update
+  double *f = res + neq;                                  // RHS at the iterate
+  double *prior = f + neq;                                // sum_j a_sj k_j
+  double *x = prior + neq;                                // linear-solve work vector
+  double *k = x + neq;                                    // 6 stage derivatives
+  double *scr = k + 6 * neq;                              // Griffon scratch
+  double *after = scr + L.total;
+  float *LU32 = reinterpret_cast<float *>(after);         // FP32 factors (precision 1)
+  float *xf = reinterpret_cast<float *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 : 0));  // 2*neq floats
+  int *piv = reinterpret_cast<int *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 + neq : 0));
+  float *rf = xf + neq;
+  const int Tidx = p.cfg.configuration == 1 ? 1 : 0;
+  NoJ noj;
+
+  for (;;) {
+    unsigned int r = 0;
+    if (lane == 0) r = atomicAdd(p.queue, 1u);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    if (r >= (unsigned)p.n) break;
+    const double pres = p.cfg.configuration == 1 ? 0. : (p.pressures ? p.pressures[r] : p.pressure);
+    for (int i = lane; i < neq; i += 32) y[i] = p.q0[(size_t)r * neq + i];
+    __syncwarp();
+    const double T0 = y[Tidx];
+    double t = 0., dt = ip.first_time_step;
+    bool setup = true;
+    int count = 0, nsteps = 0, nnewton = 0, njac = 0, nfail = 0, status = 0, attempts = 0;
+    const bool coerce = ip.stop_at_time > 0.;
+    for (;;) {
+      if (++attempts > ip.max_attempts) {
+        status = SF_INT_MAX_STEPS;
+        break;
+      }
+      if (coerce && t + dt > ip.stop_at_time) dt = ip.stop_at_time - t;
+      if (setup) {
+        IterMatrix im{A, neq, dt * kGamma};
+        reactor_eval<32, true>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, f, im);
+        __syncwarp();
+        if (p.prec == 1) {
+          for (int e = lane; e < neq * neq; e += 32) LU32[e] = (float)A[e];
+          __syncwarp();
+          warp_lu(LU32, neq, piv);
+        } else {
+          warp_lu(A, neq, piv);
+        }
+        __syncwarp();
+        ++njac;
+      }
+      ++count;
+      // ---------------- one ESDIRK64 step (methods.py:502-612)
+      reactor_eval<32, false>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, k, noj);
+      for (int i = lane; i < neq; i += 32) Y[i] = y[i];
+      __syncwarp();
+      bool nl_ok = true;
+      for (int s = 1; s < 6; ++s) {
+        const double *kprev = k + (s - 1) * neq;
+        for (int i = lane; i < neq; i += 32) {
+          double pr = 0.;
+          for (int j = s - 1; j >= 0; --j) pr += c_a[s][j] * k[j * neq + i];  // a_s,s-1 k_s-1 + ... + a_s1 k_1
+          prior[i] = pr;
+          res[i] = dt * (kGamma * kprev[i] + pr) - (Y[i] - y[i]);
+        }
+        __syncwarp();
+        bool conv = false;
+        for (int it = 1; it <= ip.max_nonlinear_iter; ++it) {
+          // dx = A^-1 res
+          if (p.prec == 1) {
+            // FP32 triangular solves of the FP32 factors, FP64 residual refinement r = res - A x
+            for (int i = lane; i < neq; i += 32) xf[i] = (float)res[i];
+            __syncwarp();
+            warp_lu_solve(LU32, neq, piv, xf);
+            for (int i = lane; i < neq; i += 32) x[i] = (double)xf[i];
+            __syncwarp();
+            for (int sweep = 0; sweep < ip.refine_sweeps; ++sweep) {
+              for (int i = lane; i < neq; i += 32) {
+                double rr = res[i];
+                for (int j = 0; j < neq; ++j) rr = fma(-A[j * neq + i], x[j], rr);
+                rf[i] = (float)rr;
+              }
+              __syncwarp();
+              warp_lu_solve(LU32, neq, piv, rf);
+              for (int i = lane; i < neq; i += 32) x[i] += (double)rf[i];
+              __syncwarp();
+            }
+          } else {
+            for (int i = lane; i < neq; i += 32) x[i] = res[i];
+            __syncwarp();
+            warp_lu_solve(A, neq, piv, x);
+          }
+          for (int i = lane; i < neq; i += 32) Y[i] -= x[i];
+          __syncwarp();
+          reactor_eval<32, false>(m, b, L, scr, grp, Y, pres, p.cfg, p.pg, f, noj);
+          double nrm = 0.;
+          for (int i = lane; i < neq; i += 32) {
+            res[i] = dt * (kGamma * f[i] + prior[i]) - (Y[i] - y[i]);
+            nrm = fmax(nrm, fabs(res[i]) * (i == Tidx ? 1.e-3 : 1.));
+          }
+          nrm = warp_max(nrm);
+          ++nnewton;
+          __syncwarp();
+          if (nrm < ip.nonlinear_tolerance) {
+            conv = true;
+            break;
+          }
+        }
+        for (int i = lane; i < neq; i += 32) k[s * neq + i] = f[i];
+        __syncwarp();
+        if (!conv) nl_ok = false;
+      }
+      // ---------------- update, error estimate, residual
+      double err = 0., rsd = 0.;
+      bool finite = true;
+      for (int i = lane; i < neq; i += 32) {
+        double ds = 0., dh = 0.;
+        for (int j = 0; j < 6; ++j) {
+          ds += c_b[j] * k[j * neq + i];
+          dh += c_bh[j] * k[j * neq + i];
+        }
+        ds *= dt;
+        dh *= dt;
+        res[i] = ds;
+        const double wi = (i == Tidx) ? 1.e-3 : 1.;
+        err = fmax(err, fabs((ds - dh) * wi));
+        rsd = fmax(rsd, fabs(ds * wi));
+        finite = finite && isfinite(ds);
+      }
+      err = warp_max(err);
+      rsd = warp_max(rsd) / dt;
+      finite = __all_sync(0xffffffffu, finite);
+      __syncwarp();
+      const double recent = dt;
+      if (finite) {
+        for (int i = lane; i < neq; i += 32) {
+          const double v = y[i] + res[i];
+          y[i] = v < 0. ? 0. : v;  // post_step_callback (reactors.py:506-508)
+        }
+        __syncwarp();
+        t += dt;
+        ++nsteps;
+        if (err < 1.e-16)
+          dt = fmin(dt * 1.1, ip.max_time_step);
+        else
+          dt = fmin(dt * fmin(1.1, pow(ip.transient_tolerance / err, 0.1333333333)), ip.max_time_step);
+        if (count == ip.maximum_steps_per_jacobian) {
+          count = 0;
+          setup = true;
+        } else if (!nl_ok) {
+          dt *= 0.8;
+          setup = true;
+        } else if (dt > recent * 1.05 || dt < recent * 0.9) {
+          setup = true;
+        } else {
+          setup = false;
+        }
+      } else {
+        dt *= 0.8;
+        setup = true;
+        ++nfail;
+      }
+      // ---------------- stop rules (integrator.py:629-640, reactors.py:774-787)
+      bool cont = true;
+      if (ip.delta_temperature_ignition > 0.) {
+        const bool ignited = y[Tidx] > T0 + ip.delta_temperature_ignition;
+        if (rsd > ip.minimum_allowable_residual) {
+          cont = !ignited;
+          status = ignited ? SF_INT_IGNITED : 0;
+        } else {
+          status = SF_INT_NO_IGNITION;
+          break;
+        }
+      }
+      if (nsteps < ip.minimum_time_step_count) {
+        cont = true;
+        if (status == SF_INT_IGNITED) status = 0;
+      }
+      if (nsteps > ip.maximum_time_step_count) {
+        cont = false;
+        status = SF_INT_MAX_STEPS;
+      } else if (coerce && t >= ip.stop_at_time) {
+        cont = false;
+        if (status == 0) status = SF_INT_DONE;
+      } else if (ip.stop_at_steady > 0. && rsd < ip.stop_at_steady) {
+        cont = false;
+        status = SF_INT_STEADY;
+      }
+      if (!cont) break;
+    }
+    for (int i = lane; i < neq; i += 32) p.out_q[(size_t)r * neq + i] = y[i];
+    if (lane == 0) {
+      p.out_t[r] = t;
+      p.out_counts[4 * (size_t)r + 0] = nsteps;
+      p.out_counts[4 * (size_t)r + 1] = nnewton;
+      p.out_counts[4 * (size_t)r + 2] = njac;
+      p.out_counts[4 * (size_t)r + 3] = nfail;
+      p.out_status[r] = status;
+    }
+    __syncwarp();
+  }
+}
+
+size_t per_warp_doubles(const HostMech &hm, int neq, int prec)
+{
+  return (size_t)neq * neq + 12 * (size_t)neq + hm.sl.total +
+         (prec == 1 ? ((size_t)neq * neq + 1) / 2 + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2;
+}
+
+}  // namespace
+}  // namespace sfgb
+
+using namespace sfgb;
+
+extern "C" {
+
+size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n)
+{
+  (void)mech;
+  (void)params;
+  (void)n;
+  return 256;
+}
+
+int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
+                       const double *q0, const double *pressures, double *out_q, double *out_t, int *out_counts,
+                       int *out_status, void *workspace, size_t workspace_bytes, void *stream)
+{
+  try {
+    if (!mech || !rp || !ip || n < 0 || (n > 0 && (!q0 || !out_q || !out_t || !out_counts || !out_status)))
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "sf_integrate_batch: bad argument");
+    if (rp->open) throw sf_error(SF_ERR_UNSUPPORTED, "open reactors are not on the GPU path");
+    if (rp->configuration != 0 && rp->configuration != 1) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad configuration");
+    if (ip->linear_precision != 0 && ip->linear_precision != 1)
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "linear_precision must be 0 or 1");
+    if (ip->rates_option < 0 || ip->rates_option > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad rates option");
+    if (ip->max_nonlinear_iter < 1 || ip->maximum_steps_per_jacobian < 1 || ip->max_attempts < 1 ||
+        !(ip->first_time_step > 0.))
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad integration controls");
+    if (!workspace || workspace_bytes < 256) throw sf_error(SF_ERR_WORKSPACE, "workspace of 256 bytes required");
+    if (mech->m.dm.ns + 1 > 128) throw sf_error(SF_ERR_UNSUPPORTED, "the integrator supports up to 127 species");
+    if (n == 0) return SF_OK;
+    HostMech &hm = const_cast<HostMech &>(mech->m);
+    const auto &progs = hm.programs_for(32);
+    IntParams p{};
+    p.m = hm.dm;
+    p.blob = hm.d_blob;
+    p.status = hm.d_status;
+    p.L = hm.sl;
+    p.pg.w = progs.progs[0];
+    p.pg.full = progs.progs[1];
+    p.pg.j = progs.progs[2];
+    p.cfg.configuration = rp->configuration;
+    p.cfg.heat = rp->heat_transfer;
+    p.cfg.option = ip->rates_option;
+    p.cfg.Tc = rp->fluid_temperature;
+    p.cfg.Tr = rp->surface_temperature;
+    p.cfg.hc = rp->h_convection;
+    p.cfg.eps = rp->eps_radiation;
+    p.cfg.SoV = rp->surface_area_to_volume;
+    p.ip = *ip;
+    if (p.ip.maximum_time_step_count <= 0) p.ip.maximum_time_step_count = 2147483647;
+    p.n = n;
+    p.neq = rp->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
+    p.prec = ip->linear_precision;
+    p.pressure = rp->pressure;
+    p.pressures = pressures;
+    p.q0 = q0;
+    p.out_q = out_q;
+    p.out_t = out_t;
+    p.out_counts = out_counts;
+    p.out_status = out_status;
+    p.queue = static_cast<unsigned int *>(workspace);
+    p.per_warp = per_warp_doubles(hm, p.neq, p.prec);
+    int dev, smem_max, nsm;
+    CUDA_THROW(cudaGetDevice(&dev));
+    CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
+    const int warps = (int)std::min<size_t>(8, avail / (p.per_warp * 8));
+    if (warps < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory integrator");
+    const size_t smem = hm.dm.blob_bytes + (size_t)warps * p.per_warp * 8;
+    CUDA_THROW(cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_THROW(cudaMemsetAsync(workspace, 0, 256, st));
+    const int grid = (int)std::min<long long>((long long)nsm, ((long long)n + warps - 1) / warps);
+    integrate_kernel<<<grid, 32 * warps, smem, st>>>(p);
+    CUDA_THROW(cudaGetLastError());
+    return SF_OK;
+  } catch (sf_error &e) {
+    set_error(e.what());
+    return e.code;
+  }
+}
+
+}  // extern "C"

@@ -3,9 +3,6 @@
 using namespace sfgb;
 extern "C" {
 static int nyi(const char *f) { set_error(std::string(f) + ": not available in this build"); return SF_ERR_UNSUPPORTED; }
-size_t sf_integrate_workspace_size(const sf_mech *, const sf_reactor_params *, int) { return 0; }
-int sf_integrate_batch(const sf_mech *, const sf_reactor_params *, const sf_integrate_params *, int, const double *,
-                       const double *, double *, double *, int *, int *, void *, size_t, void *) { return nyi("sf_integrate_batch"); }
 int sf_flamelet_stencils(const sf_mech *, const double *, int, const double *, const double *, double *, double *,
                          double *, double *, double *) { return nyi("sf_flamelet_stencils"); }
 int sf_flamelet_jac_indices(const sf_mech *, int, int *, int *) { return nyi("sf_flamelet_jac_indices"); }

@@ -1,0 +1,83 @@
+// Warp-level dense LU with partial pivoting and triangular solves on column-major matrices in shared memory
+// (the factorization LAPACK dgetrf computes, with 0-based pivots), used by the batched Newton algebra and by the
+// persistent integrator.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace sfgb {
+
+// Right-looking LU with partial pivoting of an m x m column-major matrix in shared memory, one warp.
+// Pivot rows are 0-based. Returns info (0, or k+1 for an exactly zero pivot at step k).
+template <typename F>
+__device__ __forceinline__ int warp_lu(F *A, int m, int *piv)
+{
+  const int lane = threadIdx.x & 31;
+  int info = 0;
+  for (int k = 0; k < m; ++k) {
+    // pivot: first index of the largest |A[i,k]|, i >= k (as idamax)
+    F best = -1;
+    int bi = k;
+    for (int i = k + lane; i < m; i += 32) {
+      const F v = fabs(A[i + k * m]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const F ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) piv[k] = bi;
+    if (bi != k)
+      for (int j = lane; j < m; j += 32) {
+        const F t = A[k + j * m];
+        A[k + j * m] = A[bi + j * m];
+        A[bi + j * m] = t;
+      }
+    __syncwarp();
+    const F pv = A[k + k * m];
+    if (pv == (F)0) {
+      if (!info) info = k + 1;
+      continue;
+    }
+    const F inv = (F)1 / pv;
+    for (int i = k + 1 + lane; i < m; i += 32) A[i + k * m] *= inv;
+    __syncwarp();
+    // trailing update, flattened over (i, j) so every lane has work
+    const int r = m - k - 1;
+    const int tot = r * r;
+    for (int t = lane; t < tot; t += 32) {
+      const int jj = t / r, ii = t - jj * r;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      A[i + j * m] -= A[i + k * m] * A[k + j * m];
+    }
+    __syncwarp();
+  }
+  return info;
+}
+
+// Solve (LU) x = b in place on x (shared memory), one warp.
+template <typename F>
+__device__ __forceinline__ void warp_lu_solve(const F *LU, int m, const int *piv, F *x)
+{
+  const int lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int k = 0; k < m; ++k) {
+      const int p = piv[k];
+      if (p != k) { const F t = x[k]; x[k] = x[p]; x[p] = t; }
+    }
+  __syncwarp();
+  for (int j = 0; j < m; ++j) {
+    const F xj = x[j];
+    for (int i = j + 1 + lane; i < m; i += 32) x[i] -= LU[i + j * m] * xj;
+    __syncwarp();
+  }
+  for (int j = m - 1; j >= 0; --j) {
+    if (lane == 0) x[j] /= LU[j + j * m];
+    __syncwarp();
+    const F xj = x[j];
+    for (int i = lane; i < j; i += 32) x[i] -= LU[i + j * m] * xj;
+    __syncwarp();
+  }
+}
+
+}  // namespace sfgb

@@ -1,0 +1,107 @@
+"""GPU batched ESDIRK64 integration against the reference's own ignition delays (tests/golden/ignition_ref.json,
+made by the reference HomogeneousReactor) and against the oracle integrator.
+
+Bars: ignition delay within 1e-6 relative of the reference and of the oracle; accepted-step counts equal. The
+FP32-LU + FP64-refinement variant is compared with the all-FP64 result (its error is reported, bound 1e-4).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import pair
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+CASES = json.load(open(os.path.join(GOLD, 'ignition_ref.json')))
+
+
+def _q0(spec, case):
+    Y = np.array(case['Y0'])
+    if case['configuration'] == 'isobaric':
+        return np.hstack([[case['T0']], Y[:-1]])
+    rho = case['p'] / (Y / spec.molecular_weights).sum() / (8314.46261815324 * case['T0'])
+    return np.hstack([[rho, case['T0']], Y[:-1]])
+
+
+@pytest.mark.parametrize('group', sorted({(c['mechanism'], c['configuration']) for c in CASES}))
+def test_ignition_delays_match_reference(cuda, group):
+    from spitfire_gb300.reactors import BatchIntegrator
+    mech, conf = group
+    cases = [c for c in CASES if (c['mechanism'], c['configuration']) == group]
+    spec, og = pair(mech)
+    q0 = np.array([_q0(spec, c) for c in cases])
+    pres = np.array([c['p'] for c in cases])
+    bi = BatchIntegrator(spec, conf, pressure=pres[0])
+    kw = dict(pressures=pres) if conf == 'isobaric' else {}
+    if conf == 'isochoric':
+        assert np.allclose(pres, pres[0])
+    out = bi.run(q0, delta_temperature_ignition=400., **kw)
+    tau = out['t'].cpu().numpy()
+    counts = out['counts'].cpu().numpy()
+    status = out['status'].cpu().numpy()
+    for i, c in enumerate(cases):
+        assert status[i] == 2, (c, status[i])
+        assert abs(tau[i] - c['tau']) / c['tau'] <= 1e-6, (c, tau[i])
+        assert counts[i, 0] == c['steps'], (c, counts[i])
+    assert spec.griffon.device_status() == 0
+
+
+def test_batched_ignition_matches_oracle(cuda):
+    """16 isobaric GRI-3.0 reactors from the batched-ignition distribution (T0 900-1500 K, phi 0.5-2, p 1-20 atm)
+    against the oracle integrator, reactor by reactor."""
+    import integrate as I
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec, og = pair('methane-gri30')
+    d = W.ignition_batch(spec, 16, seed=77, T_range=(1050., 1500.))
+    bi = BatchIntegrator(spec, 'isobaric')
+    out = bi.run(d['q0'], pressures=d['p'], delta_temperature_ignition=400., stop_at_time=0.1)
+    tau = out['t'].cpu().numpy()
+    st = out['status'].cpu().numpy()
+    cnt = out['counts'].cpu().numpy()
+    for i in range(16):
+        prob = I.ReactorProblem(og, 'isobaric', pressure=d['p'][i])
+        r = I.integrate(prob, d['q0'][i], delta_temperature_ignition=400., stop_at_time=0.1)
+        assert st[i] == r['status'], i
+        assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
+        assert abs(tau[i] - r['t']) / r['t'] <= 1e-6, (i, tau[i], r['t'])
+
+
+def test_fp32_lu_variant_error_is_small(cuda):
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec, og = pair('methane-gri30')
+    d = W.ignition_batch(spec, 32, seed=78, T_range=(1100., 1500.))
+    o64 = BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                                stop_at_time=0.1)
+    o32 = BatchIntegrator(spec, 'isobaric', linear_precision=1, refine_sweeps=2).run(
+        d['q0'], pressures=d['p'], delta_temperature_ignition=400., stop_at_time=0.1)
+    t64, t32 = o64['t'].cpu().numpy(), o32['t'].cpu().numpy()
+    rel = np.abs(t32 - t64) / t64
+    print('FP32-LU + 2 FP64 refinement sweeps: max rel. ignition-delay error vs FP64 LU %.2e' % rel.max())
+    assert rel.max() <= 1e-4
+
+
+def test_graph_replay_and_drop_in_reactor(cuda):
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.mechanism import Stream
+    from spitfire_gb300.reactors import BatchIntegrator, HomogeneousReactor
+    spec, og = pair('h2-burke')
+    c = [c for c in CASES if c['mechanism'] == 'h2-burke' and c['configuration'] == 'isobaric'][0]
+    mix = Stream(spec, c['T0'], c['p'], np.array(c['Y0']))
+    r = HomogeneousReactor(spec, mix, 'isobaric', 'adiabatic', 'closed')
+    tau = r.compute_ignition_delay()
+    assert abs(tau - c['tau']) / c['tau'] <= 1e-6
+    assert r.last_counts['steps'] == c['steps']
+    q0 = np.repeat(_q0(spec, c)[None, :], 64, axis=0)
+    bi = BatchIntegrator(spec, 'isobaric', pressure=c['p'])
+    out = bi.run(q0, graph=True, delta_temperature_ignition=400.)
+    torch.cuda.synchronize()
+    t1 = out['t'].clone()
+    bi.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(t1, bi._graph[3]['t'])
+    assert abs(float(t1[0]) - c['tau']) / c['tau'] <= 1e-6
