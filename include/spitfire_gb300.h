@@ -282,10 +282,12 @@ typedef struct sf_flamelet_batch {
 /* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218, adiabatic path). */
 int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, double *out_rhs,
                           void *stream);
-/* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, adiabatic path, rates option 0/2, exact transform).
+/* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, adiabatic path, rates options 0/1/2, exact transform).
  * If scale_and_offset, J <- prefactor*J - I on the diagonal blocks (flamelet_kernels.cpp:1395-1408). If
- * out_expeig is non-NULL it receives, per point, an upper bound of max(Re(lambda) - diffterm, 0) of the block
- * (replacing the dgeev call at flamelet_kernels.cpp:1329-1341; see DESIGN for the bound). */
+ * out_expeig is non-NULL it receives, for every row of a point, max(max Re(lambda) - diffterm, 0) over the
+ * eigenvalues lambda of that point's diagonal block without the diffusion diagonal (block - diag(cmajor)),
+ * computed by Householder-Hessenberg reduction and Francis double-shift QR on one warp; this replaces the dgeev
+ * call at flamelet_kernels.cpp:1329-1341. scale_and_offset must be 0 when out_expeig is requested. */
 int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, int rates_option,
                           int scale_and_offset, double prefactor, double diffterm, double *out_expeig,
                           double *out_values, void *stream);

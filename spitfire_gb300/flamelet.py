@@ -1,0 +1,630 @@
+"""Steady flamelets on the GPU: Spitfire's ``FlameletSpec``/``Flamelet`` for the adiabatic path, batched.
+
+``FlameletBatch`` holds any number of adiabatic flamelets of one mechanism, each with its own mixture-fraction grid
+and dissipation-rate profile, and evaluates all of them with one launch per operation: the flamelet residual
+(``sf_flamelet_rhs_batch``), the block-tridiagonal Jacobian (``sf_flamelet_jac_batch``), the block-Thomas
+factorization and solve (``sf_btddod_*``). The steady solvers restate the reference's control flow per flamelet
+(spitfire/chemistry/flamelet.py): ``steady_solve_newton`` (:1352-1485; chord Newton on -J with a refresh after
+line-search cuts, max 38 iterations in compute_steady_state), ``steady_solve_psitc`` (:1487-1703; pseudo-transient
+continuation with ds = min(0.1/(lambda+ + 1e-16), 1.1 ds, 1e4), a global ds on the first iteration, Jacobian
+refresh every 8 iterations or while the residual exceeds 1e-2, restart with ds_init/4 on failure) and
+``compute_steady_state`` (:1705-1778, Newton then psitc). All flamelets advance together; each has its own
+iteration counters, Jacobian-refresh flags, line-search state and convergence status.
+"""
+
+import ctypes as C
+
+import numpy as np
+from scipy.special import erfinv
+
+from . import _native as N
+from ._desc import SfFlameletBatch
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def clustered_grid(grid_points, grid_cluster_point, grid_cluster_intensity=6.):
+    """Anderson's stretched grid clustered around grid_cluster_point (flamelet.py:300-341)."""
+    if grid_cluster_intensity < 1.e-16:
+        raise ValueError('cluster_coeff must be strictly positive')
+    if grid_cluster_point < 0. or grid_cluster_point > 1.:
+        raise ValueError('z_cluster must be between 0 and 1')
+    z = np.linspace(0., 1., grid_points)
+    a_ = grid_cluster_intensity
+    zo = 1.0 / (2.0 * a_) * np.log((1. + (np.exp(a_) - 1.) * grid_cluster_point) /
+                                  (1. + (np.exp(-a_) - 1.) * grid_cluster_point))
+    a = np.sinh(a_ * zo)
+    for i in range(grid_points):
+        z[i] = grid_cluster_point / a * (np.sinh(a_ * (z[i] - zo)) + a)
+    z[-1] = 1.
+    return z, z[1:] - z[:-1]
+
+
+def uniform_grid(grid_points):
+    z = np.linspace(0., 1., grid_points)
+    return z, z[1:] - z[:-1]
+
+
+def compute_dissipation_rate(mixture_fraction, max_dissipation_rate, form='Peters'):
+    """Peters' form chi = chi_max exp(-2 erfinv(2Z-1)^2), else constant (flamelet.py:240-266)."""
+    if form in ('Peters', 'peters'):
+        return max_dissipation_rate * np.exp(-2. * (erfinv(2. * mixture_fraction - 1.)) ** 2)
+    return np.full_like(mixture_fraction, max_dissipation_rate)
+
+
+class FlameletSpec:
+    """The specification arguments of spitfire's FlameletSpec used on the adiabatic path (flamelet.py:35-237)."""
+
+    def __init__(self, mech_spec=None, initial_condition=None, oxy_stream=None, fuel_stream=None, grid=None,
+                 grid_points=None, grid_type='clustered', grid_cluster_intensity=4.,
+                 grid_cluster_point='stoichiometric', max_dissipation_rate=None, stoich_dissipation_rate=None,
+                 dissipation_rate=None, dissipation_rate_form='Peters', heat_transfer='adiabatic',
+                 rates_sensitivity_type='dense', sensitivity_transform_type='exact', include_enthalpy_flux=True,
+                 include_variable_cp=True, **ignored):
+        if heat_transfer != 'adiabatic':
+            raise NotImplementedError('the GPU flamelet path covers adiabatic flamelets')
+        self.mech_spec = mech_spec
+        self.initial_condition = initial_condition
+        self.oxy_stream = oxy_stream
+        self.fuel_stream = fuel_stream
+        self.grid = grid
+        self.grid_points = grid_points
+        self.grid_type = grid_type
+        self.grid_cluster_intensity = grid_cluster_intensity
+        self.grid_cluster_point = grid_cluster_point
+        self.max_dissipation_rate = max_dissipation_rate
+        self.stoich_dissipation_rate = stoich_dissipation_rate
+        self.dissipation_rate = dissipation_rate
+        self.dissipation_rate_form = dissipation_rate_form
+        self.heat_transfer = heat_transfer
+        self.rates_sensitivity_type = rates_sensitivity_type
+        self.sensitivity_transform_type = sensitivity_transform_type
+        self.include_enthalpy_flux = include_enthalpy_flux
+        self.include_variable_cp = include_variable_cp
+
+
+class FlameletSetup:
+    """Grid, dissipation rate, boundary states and initial state of one flamelet (flamelet.py:366-637)."""
+
+    def __init__(self, fs: FlameletSpec):
+        m = fs.mech_spec
+        self.mech = m
+        self.pressure = float(fs.oxy_stream.P)
+        if abs(fs.fuel_stream.P - fs.oxy_stream.P) / fs.oxy_stream.P > 1.e-6:
+            raise ValueError('fuel and oxidizer streams must have the same pressure')
+        self.state_fuel = np.hstack([fs.fuel_stream.T, fs.fuel_stream.Y[:-1]])
+        self.state_oxy = np.hstack([fs.oxy_stream.T, fs.oxy_stream.Y[:-1]])
+        self.z_st = m.stoich_mixture_fraction(fs.fuel_stream, fs.oxy_stream)
+        if fs.grid is not None:
+            self.z = np.array(fs.grid, dtype=np.float64)
+            self.dz = self.z[1:] - self.z[:-1]
+        elif fs.grid_type == 'uniform':
+            self.z, self.dz = uniform_grid(fs.grid_points)
+        else:
+            cp = self.z_st if fs.grid_cluster_point == 'stoichiometric' else fs.grid_cluster_point
+            self.z, self.dz = clustered_grid(fs.grid_points, cp, fs.grid_cluster_intensity)
+        self.nzi = self.z.size - 2
+        ns = m.n_species
+        if fs.dissipation_rate is not None:
+            self.x = np.array(fs.dissipation_rate, dtype=np.float64)
+            self.max_dissipation_rate = float(np.max(self.x))
+            self.form = 'custom'
+        elif fs.max_dissipation_rate is not None:
+            self.max_dissipation_rate = fs.max_dissipation_rate
+            self.form = fs.dissipation_rate_form
+            self.x = compute_dissipation_rate(self.z, self.max_dissipation_rate, self.form)
+        elif fs.stoich_dissipation_rate is not None:
+            if fs.dissipation_rate_form in ('peters', 'Peters'):
+                self.max_dissipation_rate = fs.stoich_dissipation_rate / np.exp(-2. * erfinv(2. * self.z_st - 1.) ** 2)
+            else:
+                self.max_dissipation_rate = fs.stoich_dissipation_rate
+            self.form = fs.dissipation_rate_form
+            self.x = compute_dissipation_rate(self.z, self.max_dissipation_rate, self.form)
+        else:
+            self.x = np.zeros_like(self.z)
+            self.max_dissipation_rate = 0.
+            self.form = 'unspecified-set-to-0'
+        self.include_enthalpy_flux = fs.include_enthalpy_flux
+        self.include_variable_cp = fs.include_variable_cp
+        self.rates_option = {'dense': 0, 'no-TBAF': 1, 'sparse': 2}[fs.rates_sensitivity_type]
+        ic = fs.initial_condition
+        if isinstance(ic, np.ndarray):
+            if ic.size != self.nzi * ns:
+                raise ValueError('size of initial condition is incorrect!')
+            self.initial_state = ic.astype(np.float64).copy()
+        elif ic == 'linear-TY':
+            zz = self.z[1:-1]
+            st = np.empty((self.nzi, ns))
+            for i in range(ns):
+                st[:, i] = self.state_oxy[i] + (self.state_fuel[i] - self.state_oxy[i]) * zz
+            self.initial_state = st.ravel()
+        elif ic == 'unreacted':
+            st = np.empty((self.nzi, ns))
+            for i in range(self.nzi):
+                zi = self.z[1 + i]
+                mix = m.mix_streams([(m.copy_stream(fs.oxy_stream), 1 - zi), (m.copy_stream(fs.fuel_stream), zi)],
+                                    basis='mass', constant='HP')
+                st[i] = np.hstack([mix.T, mix.Y[:-1]])
+            self.initial_state = st.ravel()
+        elif ic == 'Burke-Schumann':
+            self.initial_state = burke_schumann_state(m, fs.oxy_stream, fs.fuel_stream, self.z, self.pressure)
+        else:
+            raise ValueError(f'initial_condition {ic!r} is not available on the GPU path (Cantera equilibrium is '
+                             f'not available); use linear-TY, unreacted, Burke-Schumann or an array')
+
+    @property
+    def linear_temperature(self):
+        return self.state_oxy[0] + self.z[1:-1] * (self.state_fuel[0] - self.state_oxy[0])
+
+
+def burke_schumann_state(m, oxy, fuel, z, pressure):
+    """Burke-Schumann (infinitely fast, complete combustion) interior state (flamelet.py:554-586), with HP mixing on
+    the project's own NASA7 thermodynamics."""
+    zst = m.stoich_mixture_fraction(fuel, oxy)
+    stmix = m.mix_streams([(m.copy_stream(oxy), 1 - zst), (m.copy_stream(fuel), zst)], 'mass', 'HP')
+    atoms = m._get_atoms_in_stream(stmix, ['H', 'C', 'O', 'N'])
+    X = np.zeros(m.n_species)
+    X[m.species_index('N2')] = atoms['N'] / 2
+    X[m.species_index('H2O')] = 0.5 * atoms['H']
+    if 'CO2' in m.species_names:
+        X[m.species_index('CO2')] = atoms['C']
+    Yst = X * m.molecular_weights
+    Yst /= Yst.sum()
+    Yo, Yf = oxy.Y, fuel.Y
+    ns = m.n_species
+    out = np.empty((z.size - 2, ns))
+    for i in range(z.size - 2):
+        zi = z[1 + i]
+        h = m.mix_streams([(m.copy_stream(oxy), 1 - zi), (m.copy_stream(fuel), zi)], 'mass', 'HP').enthalpy_mass
+        Y = Yo + zi / zst * (Yst - Yo) if zi <= zst else Yst + (zi - zst) / (1. - zst) * (Yf - Yst)
+        T = m.temperature_from_enthalpy(h, Y, 1500.)
+        out[i] = np.hstack([T, Y[:-1]])
+    return out.ravel()
+
+
+class FlameletBatch:
+    """GPU evaluation of a batch of adiabatic flamelets (one mechanism, common pressure)."""
+
+    def __init__(self, setups):
+        torch = _torch()
+        self.setups = list(setups)
+        m = self.setups[0].mech
+        self.mech = m
+        self.g = m.griffon
+        ns = m.n_species
+        self.ns = ns
+        self.pressure = self.setups[0].pressure
+        for s in self.setups:
+            if abs(s.pressure - self.pressure) > 1e-9 * self.pressure:
+                raise ValueError('all flamelets of a batch share one pressure')
+            if s.include_enthalpy_flux != self.setups[0].include_enthalpy_flux or \
+                    s.include_variable_cp != self.setups[0].include_variable_cp:
+                raise ValueError('all flamelets of a batch share the enthalpy-flux / variable-cp options')
+        nz = [s.nzi for s in self.setups]
+        self.nf = len(nz)
+        offz = np.zeros(self.nf + 1, dtype=np.int32)
+        offz[1:] = np.cumsum(nz)
+        offv = np.zeros(self.nf + 1, dtype=np.int64)
+        offv[1:] = np.cumsum([ns * (n * ns + 2 * (n - 1)) for n in nz])
+        self.offz_host = offz
+        self.offv_host = offv
+        self.npts = int(offz[-1])
+        L = N.load()
+        h = self.g.handle
+        cma, csb, csp, mc, nc, chi = [], [], [], [], [], []
+        invle = np.ones(ns)
+        for s in self.setups:
+            a = np.zeros(s.nzi * ns)
+            b = np.zeros(s.nzi * ns)
+            c = np.zeros(s.nzi * ns)
+            mm = np.zeros(s.nzi)
+            nn = np.zeros(s.nzi)
+            p = lambda v: v.ctypes.data_as(C.POINTER(C.c_double))
+            N.check(L.sf_flamelet_stencils(h, p(np.ascontiguousarray(s.dz)), s.nzi, p(np.ascontiguousarray(s.x)),
+                                           p(invle), p(a), p(b), p(c), p(mm), p(nn)))
+            cma.append(a)
+            csb.append(b)
+            csp.append(c)
+            mc.append(mm)
+            nc.append(nn)
+            # the reference passes the full-grid dissipation rate to flamelet_rhs/flamelet_jacobian and indexes it
+            # with the interior index (flamelet.py:654, flamelet_kernels.cpp:1174,1360), so interior point i reads
+            # the value at grid index i
+            chi.append(s.x[:-2])
+        dev = torch.device('cuda', torch.cuda.current_device())
+        T = lambda v, dt=torch.float64: torch.tensor(np.concatenate(v) if isinstance(v, list) else v, dtype=dt,
+                                                     device=dev)
+        self.t_offz = T(offz, torch.int32)
+        self.t_offv = T(offv, torch.int64)
+        self.t_cmajor, self.t_csub, self.t_csup = T(cma), T(csb), T(csp)
+        self.t_mc, self.t_nc, self.t_chi = T(mc), T(nc), T(chi)
+        self.t_oxy = T(np.stack([s.state_oxy for s in self.setups]).ravel())
+        self.t_fuel = T(np.stack([s.state_fuel for s in self.setups]).ravel())
+        fb = SfFlameletBatch()
+        fb.n_flamelets = self.nf
+        fb.offsets_z = C.cast(self.t_offz.data_ptr(), C.POINTER(C.c_int))
+        fb.offsets_v = C.cast(self.t_offv.data_ptr(), C.POINTER(C.c_longlong))
+        fb.offsets_z_host = self.offz_host.ctypes.data_as(C.POINTER(C.c_int))
+        fb.pressure = self.pressure
+        for name, t in (('oxy_state', self.t_oxy), ('fuel_state', self.t_fuel), ('cmajor', self.t_cmajor),
+                        ('csub', self.t_csub), ('csup', self.t_csup), ('mcoeff', self.t_mc), ('ncoeff', self.t_nc),
+                        ('chi', self.t_chi)):
+            setattr(fb, name, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
+        fb.include_enthalpy_flux = int(self.setups[0].include_enthalpy_flux)
+        fb.include_variable_cp = int(self.setups[0].include_variable_cp)
+        self.fb = fb
+        self.nvals = int(offv[-1])
+        self.values = torch.empty(self.nvals, dtype=torch.float64, device=dev)
+        self.lvalues = torch.empty(self.npts * ns * ns, dtype=torch.float64, device=dev)
+        self.pivots = torch.empty(self.npts * ns, dtype=torch.int32, device=dev)
+        self.point_flamelet = torch.repeat_interleave(torch.arange(self.nf, device=dev),
+                                                      torch.tensor(nz, device=dev))
+        self.dof_flamelet = self.point_flamelet.repeat_interleave(ns)
+        scales = torch.ones(self.npts * ns, dtype=torch.float64, device=dev)
+        scales[::ns] = 1.e3
+        self.inv_scales = 1. / scales
+        self.rates_option = self.setups[0].rates_option
+        self._cnt_v = torch.tensor(np.diff(offv), device=dev)
+        self._cnt_l = torch.tensor(np.diff(offz).astype(np.int64) * ns * ns, device=dev)
+        self._cnt_p = torch.tensor(np.diff(offz).astype(np.int64) * ns, device=dev)
+        self.diffterm = 4. * np.array([s.max_dissipation_rate for s in self.setups])
+
+    # ------------------------------------------------------------------------------------------ operations
+    def initial_state(self):
+        torch = _torch()
+        return torch.tensor(np.concatenate([s.initial_state for s in self.setups]), dtype=torch.float64,
+                            device=self.values.device)
+
+    def rhs(self, state, out=None):
+        torch = _torch()
+        out = torch.empty_like(state) if out is None else out
+        N.check(N.load().sf_flamelet_rhs_batch(self.g.handle, C.byref(self.fb), N.ptr(state), N.ptr(out),
+                                               N.stream_handle()))
+        return out
+
+    def jacobian(self, state, scale_and_offset=False, prefactor=0., eig=False, diffterm=0.):
+        torch = _torch()
+        expeig = torch.empty(self.npts * self.ns, dtype=torch.float64, device=state.device) if eig else None
+        N.check(N.load().sf_flamelet_jac_batch(self.g.handle, C.byref(self.fb), N.ptr(state), self.rates_option,
+                                               int(scale_and_offset), float(prefactor), float(diffterm),
+                                               N.ptr(expeig), N.ptr(self.values), N.stream_handle()))
+        return (self.values, expeig) if eig else self.values
+
+    def expeig_per_flamelet_diffterm(self, state):
+        """Eigenvalue bounds with each flamelet's own diffterm = 4 max(chi) (flamelet.py:1587)."""
+        torch = _torch()
+        _, e = self.jacobian(state, eig=True, diffterm=0.)
+        dt = torch.tensor(self.diffterm, dtype=torch.float64, device=state.device)[self.dof_flamelet]
+        return torch.clamp(e - dt, min=0.)
+
+    def factor(self):
+        N.check(N.load().sf_btddod_factor_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
+                                                N.ptr(self.offz_host), N.ptr(self.values), N.ptr(self.lvalues),
+                                                N.ptr(self.pivots), N.stream_handle()))
+
+    def solve(self, rhs, out=None):
+        torch = _torch()
+        out = torch.empty_like(rhs) if out is None else out
+        N.check(N.load().sf_btddod_solve_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
+                                               N.ptr(self.offz_host), N.ptr(self.values), N.ptr(self.lvalues),
+                                               N.ptr(self.pivots), N.ptr(rhs), N.ptr(out), N.stream_handle()))
+        return out
+
+    def matvec(self, x, out=None):
+        torch = _torch()
+        out = torch.empty_like(x) if out is None else out
+        N.check(N.load().sf_btddod_matvec_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
+                                                N.ptr(self.values), N.ptr(x), N.ptr(out), N.stream_handle()))
+        return out
+
+    def scale_and_add_diagonal(self, matrix_scale, diagonal, diag_scale):
+        N.check(N.load().sf_btddod_scale_and_add_diagonal_batch(self.nf, self.ns, N.ptr(self.t_offz),
+                                                                N.ptr(self.t_offv), N.ptr(self.offz_host),
+                                                                N.ptr(self.values), float(matrix_scale),
+                                                                N.ptr(diagonal), float(diag_scale),
+                                                                N.stream_handle()))
+
+    def norms(self, v):
+        """Weighted inf-norm per flamelet (scales 1e3 on T)."""
+        torch = _torch()
+        out = torch.zeros(self.nf, dtype=torch.float64, device=v.device)
+        return out.scatter_reduce(0, self.dof_flamelet, (v * self.inv_scales).abs(), reduce='amax',
+                                  include_self=True)
+
+    def mins(self, v):
+        torch = _torch()
+        out = torch.full((self.nf,), float('inf'), dtype=torch.float64, device=v.device)
+        return out.scatter_reduce(0, self.dof_flamelet, v, reduce='amin', include_self=True)
+
+    def finite(self, v):
+        torch = _torch()
+        bad = torch.zeros(self.nf, dtype=torch.float64, device=v.device)
+        bad = bad.scatter_reduce(0, self.dof_flamelet, (~torch.isfinite(v)).double(), reduce='amax',
+                                 include_self=True)
+        return bad == 0
+
+    def expand(self, per_flamelet):
+        return per_flamelet[self.dof_flamelet]
+
+    # ------------------------------------------------------------------------------------------ solvers
+    def steady_solve_newton(self, state, active=None, tolerance=1.e-6, max_iterations=10,
+                            max_factor_line_search=1.5, max_allowed_residual=1.e6, min_allowable_state_var=-1.e-6):
+        """Batched restatement of Flamelet.steady_solve_newton (flamelet.py:1352-1485). Returns (state,
+        converged[nf] bool, iterations[nf])."""
+        torch = _torch()
+        dev = state.device
+        nf = self.nf
+        state = state.clone()
+        run = torch.ones(nf, dtype=torch.bool, device=dev) if active is None else active.clone()
+        failed = torch.zeros(nf, dtype=torch.bool, device=dev)
+        it = torch.zeros(nf, dtype=torch.int64, device=dev)
+        res = torch.full((nf,), tolerance + 1., dtype=torch.float64, device=dev)
+        rhs = self.rhs(state)
+        eval_j = torch.ones(nf, dtype=torch.bool, device=dev)
+        store = (torch.zeros_like(self.values), torch.zeros_like(self.lvalues), torch.zeros_like(self.pivots))
+        for _ in range(max_iterations + 1):
+            go = run & ~failed & (res > tolerance) & (it < max_iterations)
+            if not bool(go.any()):
+                break
+            it = it + go.long()
+            need = go & eval_j
+            if bool(need.any()):
+                self.jacobian(state)
+                self.values.neg_()
+                self.factor()
+                store = self._keep_factors(need, store)
+                eval_j = eval_j & ~need
+            self._use_factors(store)
+            dstate = self.solve(rhs)
+            ok = self.finite(dstate)
+            failed = failed | (go & ~ok)
+            go = go & ok
+            dstate = torch.where(self.expand(go), dstate, torch.zeros_like(dstate))
+            norm_old = self.norms(rhs)
+            rhs_new = self.rhs(state + dstate)
+            ok = self.finite(rhs_new)
+            failed = failed | (go & ~ok)
+            go = go & ok
+            alpha = torch.ones(nf, dtype=torch.float64, device=dev)
+            for _ls in range(12):
+                n_new = self.norms(rhs_new)
+                cut = go & (n_new > max_factor_line_search * norm_old) & (alpha > 0.001)
+                if not bool(cut.any()):
+                    break
+                alpha = torch.where(cut, alpha * 0.5, alpha)
+                dstate = torch.where(self.expand(cut), dstate * self.expand(alpha), dstate)
+                trial = self.rhs(state + dstate)
+                rhs_new = torch.where(self.expand(cut), trial, rhs_new)
+                eval_j = eval_j | cut
+            state = torch.where(self.expand(go), state + dstate, state)
+            rhs = torch.where(self.expand(go), rhs_new, rhs)
+            res = torch.where(go, self.norms(rhs), res)
+            failed = failed | (go & (res > max_allowed_residual))
+            failed = failed | (go & (self.mins(state) < min_allowable_state_var))
+        state = torch.clamp(state, min=0.)
+        conv = run & ~failed & (res <= tolerance) & (it <= max_iterations)
+        return state, conv, it
+
+    def _values_mask(self, per_flamelet):
+        return per_flamelet.repeat_interleave(self._cnt_v)
+
+    def _lval_mask(self, per_flamelet):
+        return per_flamelet.repeat_interleave(self._cnt_l)
+
+    def _piv_mask(self, per_flamelet):
+        return per_flamelet.repeat_interleave(self._cnt_p)
+
+    def _keep_factors(self, need, store):
+        """Copy the freshly factorized BTDDOD arrays of the flamelets in `need` into `store` (vals, lvals, pivots)."""
+        torch = _torch()
+        v, l, p = store
+        v = torch.where(self._values_mask(need), self.values, v)
+        l = torch.where(self._lval_mask(need), self.lvalues, l)
+        p = torch.where(self._piv_mask(need), self.pivots, p)
+        return v, l, p
+
+    def _use_factors(self, store):
+        self.values.copy_(store[0])
+        self.lvalues.copy_(store[1])
+        self.pivots.copy_(store[2])
+
+    def steady_solve_psitc(self, initial, active=None, tolerance=1.e-6, max_iterations=400,
+                           min_allowable_state_var=-1.e-6, ds_init=1., ds_init_decrease=4., diffusion_factor=4.,
+                           global_ds=False, ds_safety=0.1, ds_ramp=1.1, ds_max=1.e4, max_factor_line_search=1.5,
+                           max_allowed_residual=1.e6, max_recursion_depth=20, adaptive_restart=True):
+        """Batched restatement of Flamelet.steady_solve_psitc (flamelet.py:1487-1703), including its restart from the
+        initial guess with ds_init / ds_init_decrease after a failure (a flamelet gives up once a failure happens
+        at restart depth > max_recursion_depth, or at once without adaptive_restart)."""
+        torch = _torch()
+        dev = initial.device
+        nf, ns = self.nf, self.ns
+        run = torch.ones(nf, dtype=torch.bool, device=dev) if active is None else active.clone()
+        diffterm = torch.tensor(diffusion_factor / 4. * self.diffterm, dtype=torch.float64, device=dev)
+        state = initial.clone()
+        depth = torch.zeros(nf, dtype=torch.int64, device=dev)
+        dsi = torch.full((nf,), float(ds_init), dtype=torch.float64, device=dev)
+        ds = self.expand(dsi).clone()
+        it = torch.zeros(nf, dtype=torch.int64, device=dev)
+        jac_age = torch.zeros(nf, dtype=torch.int64, device=dev)
+        res = torch.full((nf,), tolerance + 1., dtype=torch.float64, device=dev)
+        dead = torch.zeros(nf, dtype=torch.bool, device=dev)
+        rhs = self.rhs(state)
+        eval_j = torch.ones(nf, dtype=torch.bool, device=dev)
+        store = (torch.zeros_like(self.values), torch.zeros_like(self.lvalues), torch.zeros_like(self.pivots))
+        total_cap = (max_iterations + 1) * (max_recursion_depth + 3)
+        for _ in range(total_cap):
+            go = run & ~dead & (res > tolerance) & (it < max_iterations)
+            if not bool(go.any()):
+                break
+            it = it + go.long()
+            need = go & eval_j
+            if bool(need.any()):
+                _, expeig = self.jacobian(state, eig=True, diffterm=0.)
+                expeig = torch.clamp(expeig - self.expand(diffterm), min=0.)
+                new_ds = torch.minimum(torch.minimum(ds_safety / (expeig + 1.e-16), ds_ramp * ds),
+                                       torch.full_like(ds, ds_max))
+                first = need & ((it == 1) | global_ds)
+                mn = torch.full((nf,), float('inf'), dtype=torch.float64, device=dev).scatter_reduce(
+                    0, self.dof_flamelet, new_ds, reduce='amin', include_self=True)
+                new_ds = torch.where(self.expand(first), self.expand(mn), new_ds)
+                ds = torch.where(self.expand(need), new_ds, ds)
+                self.scale_and_add_diagonal(-1., 1. / ds, 1.)
+                self.factor()
+                store = self._keep_factors(need, store)
+                jac_age = torch.where(need, torch.zeros_like(jac_age), jac_age)
+            jac_age = torch.where(go & ~need, jac_age + 1, jac_age)
+            eval_j = torch.where(go, (jac_age == 8) | (res > 1.e-2), eval_j)
+            self._use_factors(store)
+            dstate = self.solve(rhs)
+            bad = go & ~self.finite(dstate)
+            dstate = torch.where(self.expand(go), torch.nan_to_num(dstate), torch.zeros_like(dstate))
+            norm_old = self.norms(rhs)
+            rhs_new = self.rhs(state + dstate)
+            bad = bad | (go & ~self.finite(rhs_new))
+            rhs_new = torch.nan_to_num(rhs_new, nan=1e300, posinf=1e300, neginf=-1e300)
+            alpha = torch.ones(nf, dtype=torch.float64, device=dev)
+            ok_go = go & ~bad
+            for _ls in range(12):
+                cut = ok_go & (self.norms(rhs_new) > max_factor_line_search * norm_old) & (alpha > 0.001)
+                if not bool(cut.any()):
+                    break
+                alpha = torch.where(cut, alpha * 0.5, alpha)
+                dstate = torch.where(self.expand(cut), dstate * self.expand(alpha), dstate)
+                trial = self.rhs(state + dstate)
+                rhs_new = torch.where(self.expand(cut), trial, rhs_new)
+                eval_j = eval_j | cut
+            state = torch.where(self.expand(ok_go), state + dstate, state)
+            rhs = torch.where(self.expand(ok_go), rhs_new, rhs)
+            res = torch.where(ok_go, self.norms(rhs), res)
+            bad = bad | (ok_go & (res > max_allowed_residual)) | (ok_go & (self.mins(state) < min_allowable_state_var))
+            # restart failed flamelets from the initial guess with a smaller initial pseudo-time step
+            if bool(bad.any()):
+                give_up = bad & ((depth > max_recursion_depth) | (not adaptive_restart))
+                dead = dead | give_up
+                rst = bad & ~give_up
+                if bool(rst.any()):
+                    depth = torch.where(rst, depth + 1, depth)
+                    dsi = torch.where(rst, dsi / ds_init_decrease, dsi)
+                    e = self.expand(rst)
+                    state = torch.where(e, initial, state)
+                    ds = torch.where(e, self.expand(dsi), ds)
+                    it = torch.where(rst, torch.zeros_like(it), it)
+                    jac_age = torch.where(rst, torch.zeros_like(jac_age), jac_age)
+                    res = torch.where(rst, torch.full_like(res, tolerance + 1.), res)
+                    eval_j = eval_j | rst
+                    rhs = torch.where(e, self.rhs(state), rhs)
+        state = torch.clamp(state, min=0.)
+        conv = run & ~dead & (res <= tolerance)
+        return state, conv, it
+
+    def compute_steady_state(self, state=None, tolerance=1.e-6, newton_iterations=38, psitc_iterations=400):
+        """Newton (38 iterations), then psitc (400) for the flamelets Newton did not converge
+        (flamelet.py:1705-1778; the ESDIRK fallback is not on the GPU path)."""
+        torch = _torch()
+        init = self.initial_state() if state is None else state
+        s1, c1, i1 = self.steady_solve_newton(init, tolerance=tolerance, max_iterations=newton_iterations)
+        if bool(c1.all()):
+            return s1, c1, {'newton': c1, 'psitc': torch.zeros_like(c1)}
+        s2, c2, i2 = self.steady_solve_psitc(init, active=~c1, tolerance=tolerance, max_iterations=psitc_iterations)
+        out = torch.where(self.expand(c1), s1, s2)
+        return out, c1 | c2, {'newton': c1, 'psitc': c2 & ~c1}
+
+
+class Flamelet:
+    """Drop-in for spitfire.chemistry.flamelet.Flamelet on the adiabatic path (one flamelet, GPU kernels)."""
+
+    def __init__(self, flamelet_specs=None, **kwargs):
+        fs = FlameletSpec(**flamelet_specs) if isinstance(flamelet_specs, dict) else \
+            (flamelet_specs if flamelet_specs is not None else FlameletSpec(**kwargs))
+        self._setup = FlameletSetup(fs)
+        self._batch = None
+        self._current_state = self._setup.initial_state.copy()
+
+    def _b(self):
+        if self._batch is None:
+            self._batch = FlameletBatch([self._setup])
+        return self._batch
+
+    @property
+    def mechanism(self):
+        return self._setup.mech
+
+    @property
+    def mixfrac_grid(self):
+        return self._setup.z
+
+    @property
+    def dissipation_rate(self):
+        return self._setup.x
+
+    @property
+    def initial_interior_state(self):
+        return self._setup.initial_state.copy()
+
+    @property
+    def current_interior_state(self):
+        return self._current_state.copy()
+
+    @property
+    def current_temperature(self):
+        return self._current_state[::self._setup.mech.n_species]
+
+    @property
+    def linear_temperature(self):
+        return self._setup.linear_temperature
+
+    def _run(self, fn, **kw):
+        torch = _torch()
+        b = self._b()
+        st = torch.tensor(self._current_state, dtype=torch.float64, device='cuda')
+        out, conv, it = fn(st, **kw)
+        return out, bool(conv[0]), int(it[0])
+
+    def steady_solve_newton(self, initial_guess=None, tolerance=1.e-6, max_iterations=10, **kw):
+        if initial_guess is not None:
+            self._current_state = np.array(initial_guess, dtype=np.float64)
+        out, conv, it = self._run(self._b().steady_solve_newton, tolerance=tolerance, max_iterations=max_iterations)
+        if not conv:
+            return None, None, False
+        self._current_state = out.cpu().numpy()
+        return self.make_library_from_interior_state(self._current_state), it, True
+
+    def steady_solve_psitc(self, initial_guess=None, tolerance=1.e-6, max_iterations=400, **kw):
+        if initial_guess is not None:
+            self._current_state = np.array(initial_guess, dtype=np.float64)
+        out, conv, it = self._run(self._b().steady_solve_psitc, tolerance=tolerance, max_iterations=max_iterations,
+                                  **kw)
+        if not conv:
+            return None, None, False, None
+        self._current_state = out.cpu().numpy()
+        return self.make_library_from_interior_state(self._current_state), it, True, None
+
+    def compute_steady_state(self, tolerance=1.e-6, verbose=False, use_psitc=True, **kw):
+        torch = _torch()
+        b = self._b()
+        st = torch.tensor(self._current_state, dtype=torch.float64, device='cuda')
+        out, conv, _ = b.compute_steady_state(st, tolerance=tolerance)
+        if not bool(conv[0]):
+            raise RuntimeError('steady flamelet solve failed (Newton and psitc)')
+        self._current_state = out.cpu().numpy()
+        return self.make_library_from_interior_state(self._current_state)
+
+    def make_library_from_interior_state(self, state):
+        from .library import Dimension, Library
+        s = self._setup
+        ns = s.mech.n_species
+        st = np.array(state).reshape(s.nzi, ns)
+        full = np.vstack([s.state_oxy, st, s.state_fuel])
+        lib = Library(Dimension('mixture_fraction', s.z))
+        lib['temperature'] = full[:, 0]
+        lib['pressure'] = np.full(s.z.size, s.pressure)
+        names = s.mech.species_names
+        last = np.ones(s.z.size)
+        for i, sp in enumerate(names[:-1]):
+            lib['mass fraction ' + sp] = full[:, 1 + i]
+            last -= full[:, 1 + i]
+        lib['mass fraction ' + names[-1]] = last
+        return lib

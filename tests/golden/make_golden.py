@@ -9,8 +9,12 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
                        HomogeneousReactor.compute_ignition_delay (reference odesolve + ESDIRK64 + Newton + PI)
   h2_mech_data.json    the Cantera-converted mech_data embedded in tests/tabulation/adiabatic_slfm/gold.pkl
   closed_reactor_gold.npz  the reference's stored closed-reactor trajectories (tests/reactor/closed_reactors/gold.pkl)
+  flamelet_ref.npz     reference Flamelet (flamelet.py) residuals, BTDDOD Jacobians (plain, scaled, with eigenvalue
+                       bounds), block-Thomas solves and matvecs, and steady Newton / psitc solutions with iteration
+                       counts, for an H2 and a GRI-3.0 flamelet started from a Burke-Schumann profile
+  adiabatic_slfm_gold.npz  temperature and mass fractions of tests/tabulation/adiabatic_slfm/gold.pkl
 
-Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold]
+Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets]
 """
 import json
 import os
@@ -23,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+sys.path.insert(0, os.path.join(ROOT, 'tests'))
 REF = os.environ.get('SPITFIRE_REFERENCE', '/root/reference')
 MECHS = os.path.join(REF, 'tests', 'test_mechanisms')
 
@@ -148,8 +153,115 @@ def gold():
     print('gold', list(g.keys()))
 
 
+def flamelets():
+    import ref_harness as rh
+    from flamelet_cases import FLAMELET_CASES, flamelet_case_setup
+    from spitfire_gb300.flamelet import burke_schumann_state, clustered_grid
+    ns_ref = rh.load_reference()
+    G = ns_ref.griffon
+    out = {}
+    for case in FLAMELET_CASES:
+        name, fname, phase = case[:3]
+        ref = rh.ReferenceMechanism(os.path.join(MECHS, fname), phase)
+        spec = ref.spec
+        oxy, fuel, kw = flamelet_case_setup(spec, case)
+        zst = spec.stoich_mixture_fraction(fuel, oxy)
+        z, _ = clustered_grid(kw['grid_points'], zst, 4.)
+        ic = burke_schumann_state(spec, oxy, fuel, z, 101325.)
+        F = ns_ref.flamelet.Flamelet(ns_ref.flamelet.FlameletSpec(mech_spec=ref, initial_condition=ic, **kw))
+        nzi, ns = F._nz_interior, F._n_equations
+        rng = np.random.default_rng(case[-1])
+        st = ic * (1. + 0.02 * rng.standard_normal(ic.size))
+        st = np.abs(st)
+        pre = name + '_'
+        out[pre + 'z'] = F._z
+        out[pre + 'chi'] = F._x
+        out[pre + 'oxy'] = F._state_oxy
+        out[pre + 'fuel'] = F._state_fuel
+        out[pre + 'ic'] = ic
+        out[pre + 'state'] = st
+        for ef in (0, 1):
+            for vc in (0, 1):
+                F._include_enthalpy_flux, F._include_variable_cp = bool(ef), bool(vc)
+                out[pre + f'rhs_e{ef}v{vc}'] = F._adiabatic_rhs(0., st)
+            F._include_enthalpy_flux, F._include_variable_cp = bool(ef), True
+            out[pre + f'jac_e{ef}'] = F._adiabatic_jac(st)
+        F._include_enthalpy_flux, F._include_variable_cp = True, True
+        out[pre + 'jac_scaled'] = F._adiabatic_jac_offset_scaled(st, 1.e-3)
+        diffterm = 4. * F._max_dissipation_rate
+        vals, expeig = F._adiabatic_jac_and_eig(st, diffterm)
+        out[pre + 'jac_eig'] = vals
+        out[pre + 'expeig'] = expeig
+        out[pre + 'diffterm'] = np.array(diffterm)
+        # block-Thomas algebra on -J, and on -J + diag(1/ds)
+        J = -out[pre + 'jac_e1']
+        b = rng.standard_normal(nzi * ns)
+        y = np.zeros(nzi * ns)
+        G.py_btddod_full_matvec(J, b, nzi, ns, y)
+        out[pre + 'matvec_b'] = b
+        out[pre + 'matvec_y'] = y
+        Jf = J.copy()
+        lv = np.zeros(nzi * ns * ns)
+        pv = np.zeros(J.size, dtype=np.int32)
+        G.py_btddod_full_factorize(Jf, nzi, ns, lv, pv)
+        x = np.zeros(nzi * ns)
+        G.py_btddod_full_solve(Jf, lv, pv, b, nzi, ns, x)
+        out[pre + 'solve_x'] = x
+        ds = np.exp(rng.uniform(np.log(1e-6), np.log(1e-2), nzi * ns))
+        Js = out[pre + 'jac_e1'].copy()
+        G.py_btddod_scale_and_add_diagonal(Js, -1., 1. / ds, 1., nzi, ns)
+        out[pre + 'scaled_ds'] = ds
+        out[pre + 'scaled_values'] = Js
+        # steady solvers from the Burke-Schumann profile
+        F._include_enthalpy_flux, F._include_variable_cp = True, True
+        lib, it, conv = F.steady_solve_newton(initial_guess=ic, tolerance=1.e-6, max_iterations=38, verbose=False)
+        out[pre + 'newton_conv'] = np.array(bool(conv))
+        out[pre + 'newton_iters'] = np.array(it if conv else -1)
+        out[pre + 'newton_state'] = F._current_state.copy() if conv else np.zeros(0)
+        F2 = ns_ref.flamelet.Flamelet(ns_ref.flamelet.FlameletSpec(mech_spec=ref, initial_condition=ic, **kw))
+        lib, it, conv, mds = F2.steady_solve_psitc(initial_guess=ic, tolerance=1.e-6, max_iterations=400,
+                                                   verbose=False)
+        out[pre + 'psitc_conv'] = np.array(bool(conv))
+        out[pre + 'psitc_iters'] = np.array(it if conv else -1)
+        out[pre + 'psitc_state'] = F2._current_state.copy() if conv else np.zeros(0)
+        out[pre + 'psitc_min_ds'] = np.array(mds)
+        # continuation step like the SLFM builder: Newton at 1.5 chi_st from the converged psitc profile
+        kw3 = dict(kw, stoich_dissipation_rate=1.5 * kw['stoich_dissipation_rate'])
+        F3 = ns_ref.flamelet.Flamelet(ns_ref.flamelet.FlameletSpec(mech_spec=ref,
+                                                                   initial_condition=F2._current_state.copy(), **kw3))
+        lib, it, conv = F3.steady_solve_newton(tolerance=1.e-6, max_iterations=38, verbose=False)
+        out[pre + 'cont_conv'] = np.array(bool(conv))
+        out[pre + 'cont_iters'] = np.array(it if conv else -1)
+        out[pre + 'cont_state'] = F3._current_state.copy() if conv else np.zeros(0)
+        print(name, 'nzi', nzi, 'newton', out[pre + 'newton_conv'], out[pre + 'newton_iters'], 'psitc',
+              out[pre + 'psitc_conv'], out[pre + 'psitc_iters'], 'continuation newton', out[pre + 'cont_conv'],
+              out[pre + 'cont_iters'])
+    np.savez_compressed(os.path.join(HERE, 'flamelet_ref.npz'), **out)
+
+
+def slfm_gold():
+    d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'adiabatic_slfm', 'gold.pkl'), 'rb')).load()
+    st = d._st
+    dims = st['dimensions']
+    order = [st['dim_ordering'][i] for i in range(len(st['dim_ordering']))]
+    arrs = {}
+    for i, n in enumerate(order):
+        dd = dims[n]
+        dd = dd._st if hasattr(dd, '_st') else dd
+        arrs['dim%d_name' % i] = np.array(n)
+        arrs['dim%d_values' % i] = np.asarray(dd['_values'] if '_values' in dd else dd['values'])
+    for k, v in st['properties'].items():
+        if k == 'temperature' or k.startswith('mass fraction') or k == 'pressure':
+            arrs['prop:' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'adiabatic_slfm_gold.npz'), **arrs)
+    print('slfm gold', order, [a.shape for a in arrs.values()][:4])
+
+
 if __name__ == '__main__':
-    what = sys.argv[1:] or ['kernels', 'ignition', 'gold']
+    what = sys.argv[1:] or ['kernels', 'ignition', 'gold', 'flamelets']
+    if 'flamelets' in what:
+        slfm_gold()
+        flamelets()
     if 'gold' in what:
         gold()
     if 'kernels' in what:

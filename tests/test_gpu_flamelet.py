@@ -1,0 +1,242 @@
+"""GPU flamelet path against the reference Flamelet (tests/golden/flamelet_ref.npz) and the oracle.
+
+A batch holds the reference's golden flamelet plus two more flamelets of the same mechanism with other grids and
+dissipation rates, so every launch covers ragged batches. Bars: residuals and Jacobian rows 1e-10 (row-normwise,
+FP64); eigenvalue bounds 1e-13 ||A||_F + 1e-8 max(|lambda|, 1) (two backward-stable eigenvalue algorithms agree
+to a multiple of eps ||A||, and chemistry blocks reach ||A||_F ~ 1e11); block-Thomas solutions 1e-9 normwise; steady solvers:
+same convergence and iteration counts as the reference solvers, temperatures within 1e-6 relative (the solvers'
+own tolerance), mass fractions within 1e-6 per species of the species' maximum.
+"""
+import numpy as np
+import pytest
+
+import flamelet_cases as FC
+from helpers import pair
+
+pytestmark = pytest.mark.gpu
+CASES = [c[0] for c in FC.FLAMELET_CASES]
+
+
+def _setups(name, extra=True):
+    from spitfire_gb300.flamelet import FlameletSetup, FlameletSpec
+    d = FC.golden()
+    spec, og = pair(FC.BUNDLED[name])
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case(name))
+    setups = [FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition=d[name + '_state'], **kw))]
+    if extra:
+        rng = np.random.default_rng(5)
+        for npts, chi in ((9, 0.3), (21, 5.)):
+            s = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition='Burke-Schumann',
+                                           **dict(kw, grid_points=npts, stoich_dissipation_rate=chi)))
+            s.initial_state = np.abs(s.initial_state * (1. + 0.02 * rng.standard_normal(s.initial_state.size)))
+            setups.append(s)
+    return d, spec, og, setups
+
+
+def _ops(og, setups):
+    import flamelet_steady as FS
+    return [FS.FlameletOperator(og, s.z, s.x, s.state_oxy, s.state_fuel) for s in setups]
+
+
+def _split(b, v, per='z'):
+    v = v.cpu().numpy()
+    out = []
+    for f in range(b.nf):
+        if per == 'z':
+            out.append(v[b.offz_host[f] * b.ns:b.offz_host[f + 1] * b.ns])
+        else:
+            out.append(v[b.offv_host[f]:b.offv_host[f + 1]])
+    return out
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_flamelet_rhs_and_jacobian(cuda, name):
+    from spitfire_gb300.flamelet import FlameletBatch
+    d, spec, og, setups = _setups(name)
+    b = FlameletBatch(setups)
+    ops = _ops(og, setups)
+    ns = b.ns
+    st = b.initial_state()
+    states = [s.initial_state for s in setups]
+    for ef in (0, 1):
+        for vc in (0, 1):
+            b.fb.include_enthalpy_flux, b.fb.include_variable_cp = ef, vc
+            r = _split(b, b.rhs(st))
+            assert FC.vec_err(r[0], d[name + f'_rhs_e{ef}v{vc}'], ns) < 1e-10, (ef, vc)
+            for f in range(b.nf):
+                assert FC.vec_err(r[f], ops[f].rhs(states[f], eflux=ef, vcp=vc), ns) < 1e-10, (f, ef, vc)
+        b.fb.include_variable_cp = 1
+        J = _split(b, b.jacobian(st).clone(), 'v')
+        assert FC.btddod_row_err(J[0], d[name + f'_jac_e{ef}'], setups[0].nzi, ns) < 1e-10, ef
+        for f in range(b.nf):
+            assert FC.btddod_row_err(J[f], ops[f].jac(states[f], eflux=ef), setups[f].nzi, ns) < 1e-10, (f, ef)
+    b.fb.include_enthalpy_flux, b.fb.include_variable_cp = 1, 1
+    J = _split(b, b.jacobian(st, scale_and_offset=True, prefactor=1.e-3).clone(), 'v')
+    assert FC.btddod_row_err(J[0], d[name + '_jac_scaled'], setups[0].nzi, ns) < 1e-10
+    for f in range(b.nf):
+        ref = ops[f].jac(states[f], scale_and_offset=True, prefactor=1.e-3)
+        assert FC.btddod_row_err(J[f], ref, setups[f].nzi, ns) < 1e-10, f
+    assert spec.griffon.device_status() == 0
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_flamelet_eigenvalue_bounds(cuda, name):
+    from spitfire_gb300.flamelet import FlameletBatch
+    d, spec, og, setups = _setups(name)
+    b = FlameletBatch(setups)
+    ops = _ops(og, setups)
+    st = b.initial_state()
+    dt = float(d[name + '_diffterm'])
+    vals, e = b.jacobian(st, eig=True, diffterm=dt)
+    J = _split(b, vals.clone(), 'v')
+    e = _split(b, e)
+    # values are the plain Jacobian (eigenvalues do not change them)
+    assert FC.btddod_row_err(J[0], d[name + '_jac_eig'], setups[0].nzi, b.ns) < 1e-10
+    ref = d[name + '_expeig']
+    assert FC.eig_err(e[0], ref, ops[0], setups[0].initial_state) < 1.
+    for f in range(b.nf):
+        o = ops[f].expeig(setups[f].initial_state, dt)
+        assert FC.eig_err(e[f], o, ops[f], setups[f].initial_state) < 1., f
+    # per-flamelet diffusion term, as steady_solve_psitc uses it
+    e2 = _split(b, b.expeig_per_flamelet_diffterm(st))
+    for f in range(b.nf):
+        o = ops[f].expeig(setups[f].initial_state, 4. * setups[f].max_dissipation_rate)
+        assert FC.eig_err(e2[f], o, ops[f], setups[f].initial_state) < 1., f
+    assert spec.griffon.device_status() == 0
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_block_thomas_factor_solve_matvec_scale(cuda, name):
+    import torch
+    import oracle as orc
+    from spitfire_gb300.flamelet import FlameletBatch
+    d, spec, og, setups = _setups(name)
+    b = FlameletBatch(setups)
+    ops = _ops(og, setups)
+    ns = b.ns
+    st = b.initial_state()
+    rng = np.random.default_rng(9)
+    x = torch.tensor(rng.standard_normal(b.npts * ns), dtype=torch.float64, device='cuda')
+    J0 = [ops[f].jac(setups[f].initial_state) for f in range(b.nf)]
+    # matvec with -J
+    b.jacobian(st)
+    b.values.neg_()
+    y = _split(b, b.matvec(x))
+    xs = _split(b, x)
+    for f in range(b.nf):
+        ref = orc.btddod_full_matvec(-J0[f], xs[f], setups[f].nzi, ns)
+        assert FC.vec_err(y[f], ref, ns) < 1e-10, f
+    # golden flamelet: the reference's matvec / solve on -J at its own vector
+    g = torch.zeros(b.npts * ns, dtype=torch.float64, device='cuda')
+    g[:setups[0].nzi * ns] = torch.tensor(d[name + '_matvec_b'], device='cuda')
+    assert FC.vec_err(_split(b, b.matvec(g))[0], d[name + '_matvec_y'], ns) < 1e-10
+    b.factor()
+    sol = _split(b, b.solve(g))[0]
+    ref = d[name + '_solve_x']
+    assert np.max(np.abs(sol - ref)) / np.max(np.abs(ref)) < 1e-9
+    xsol = _split(b, b.solve(x))
+    for f in range(b.nf):
+        dd, l, piv = orc.btddod_full_factorize(-J0[f], setups[f].nzi, ns)
+        ref = orc.btddod_full_solve(dd, l, piv, xs[f], setups[f].nzi, ns)
+        assert np.max(np.abs(xsol[f] - ref)) / np.max(np.abs(ref)) < 1e-9, f
+    # -J + diag(1/ds) against the reference's scale_and_add_diagonal
+    b.jacobian(st)
+    ds = torch.tensor(np.exp(rng.uniform(np.log(1e-6), np.log(1e-2), b.npts * ns)), device='cuda')
+    ds[:setups[0].nzi * ns] = torch.tensor(d[name + '_scaled_ds'], device='cuda')
+    b.scale_and_add_diagonal(-1., 1. / ds, 1.)
+    S = _split(b, b.values.clone(), 'v')
+    assert FC.btddod_row_err(S[0], d[name + '_scaled_values'], setups[0].nzi, ns) < 1e-10
+    assert spec.griffon.device_status() == 0
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_batched_steady_solvers_match_reference(cuda, name):
+    """psitc from the Burke-Schumann profile (Newton fails there, as in the reference) and a Newton continuation
+    step at 1.5 chi_st, in one batch with two other flamelets; the golden flamelet must follow the reference
+    solvers' iteration counts and converge to their profiles, the others must match the oracle solvers."""
+    import torch
+    import flamelet_steady as FS
+    from spitfire_gb300.flamelet import FlameletBatch, FlameletSetup, FlameletSpec
+    d, spec, og, setups = _setups(name)
+    setups[0].initial_state = d[name + '_ic'].copy()
+    b = FlameletBatch(setups)
+    ops = _ops(og, setups)
+    ns = b.ns
+    init = b.initial_state()
+    s, conv, it = b.steady_solve_newton(init, tolerance=1.e-6, max_iterations=38)
+    assert bool(conv[0]) == bool(d[name + '_newton_conv'])
+    s, conv, it = b.steady_solve_psitc(init, tolerance=1.e-6, max_iterations=400)
+    conv, it = conv.cpu().numpy(), it.cpu().numpy()
+    st = _split(b, s)
+    assert conv[0] and it[0] == int(d[name + '_psitc_iters']), (conv, it)
+    ref = d[name + '_psitc_state']
+    assert np.max(np.abs(st[0][::ns] - ref[::ns]) / ref[::ns]) < 1e-6
+    assert FC.vec_err(st[0], ref, ns) < 1e-6
+    for f in range(1, b.nf):
+        o, oit, oconv, _ = FS.steady_solve_psitc(ops[f], setups[f].initial_state)
+        assert bool(conv[f]) == oconv, f
+        if oconv:
+            assert it[f] == oit, (f, it[f], oit)
+            assert FC.vec_err(st[f], o, ns) < 1e-6
+    # continuation Newton step
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case(name))
+    kw['stoich_dissipation_rate'] *= 1.5
+    s3 = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition=ref.copy(), **kw))
+    b3 = FlameletBatch([s3])
+    out, conv, it = b3.steady_solve_newton(b3.initial_state(), tolerance=1.e-6, max_iterations=38)
+    assert bool(conv[0]) and int(it[0]) == int(d[name + '_cont_iters'])
+    r3 = d[name + '_cont_state']
+    o3 = out.cpu().numpy()
+    assert np.max(np.abs(o3[::ns] - r3[::ns]) / r3[::ns]) < 1e-6
+    assert FC.vec_err(o3, r3, ns) < 1e-6
+    assert spec.griffon.device_status() == 0
+
+
+def test_flamelet_drop_in_compute_steady_state(cuda):
+    from spitfire_gb300.flamelet import Flamelet
+    d = FC.golden()
+    spec, og = pair('h2-burke')
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case('h2'))
+    f = Flamelet(dict(mech_spec=spec, initial_condition='Burke-Schumann', **kw))
+    lib = f.compute_steady_state(tolerance=1.e-6)
+    ref = d['h2_psitc_state']
+    T = lib['temperature'][1:-1]
+    assert np.max(np.abs(T - ref[::spec.n_species]) / ref[::spec.n_species]) < 1e-6
+    assert abs(lib['temperature'][0] - oxy.T) < 1e-12 and abs(lib['temperature'][-1] - fuel.T) < 1e-12
+    ysum = sum(lib['mass fraction ' + n] for n in spec.species_names)
+    assert np.allclose(ysum, 1., atol=1e-12)
+
+
+def test_adiabatic_slfm_library_matches_reference_gold(cuda):
+    """tests/tabulation/adiabatic_slfm of the reference (h2-burke, air 1200 K / H2 300 K, 34 points,
+    chi_st = logspace(0, 1, 8)) through the drop-in build_adiabatic_slfm_library; the reference test's bars
+    (rtol = atol = 1e-6) on temperature, pressure and every mass fraction, and the library dimensions."""
+    import os
+    from spitfire_gb300.library import Library
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    from spitfire_gb300.tabulation import build_adiabatic_slfm_library
+    g = np.load(os.path.join(FC.GOLD, 'adiabatic_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    lib = build_adiabatic_slfm_library(dict(mech_spec=m, oxy_stream=air, fuel_stream=fuel, grid_points=34),
+                                       verbose=False, diss_rate_values=np.logspace(0, 1, 8),
+                                       diss_rate_log_scaled=True)
+    assert lib.dim_names == ['mixture_fraction', 'dissipation_rate_stoich']
+    np.testing.assert_allclose(lib.dims[0].values, g['dim0_values'], rtol=1e-14)
+    np.testing.assert_allclose(lib.dims[1].values, g['dim1_values'], rtol=1e-12)
+    assert lib.dims[1].log_scaled
+    keys = [k for k in g.files if k.startswith('prop:')]
+    assert len(keys) == 2 + m.n_species
+    for k in keys:
+        np.testing.assert_allclose(lib[k[5:]], g[k], rtol=1e-6, atol=1e-6, err_msg=k)
+    # the pickle round trip keeps everything
+    import tempfile
+    with tempfile.TemporaryDirectory() as t:
+        p = os.path.join(t, 'slfm.pkl')
+        lib.extra_attributes.pop('mech_spec')
+        lib.save_to_file(p)
+        l2 = Library.load_from_file(p)
+        for k in keys:
+            assert np.array_equal(l2[k[5:]], lib[k[5:]])
