@@ -1,6 +1,6 @@
 """Benchmark of the GB300 Griffon hot path; prints one JSON line.
 
-Workload (one "step"): the analytical isochoric reactor right-hand side + Jacobian of GRI-3.0 (53 species,
+Headline workload (one "step"): the analytical isochoric reactor right-hand side + Jacobian of GRI-3.0 (53 species,
 325 reactions) on 65536 seeded states (T ~ U(600, 2800) K, p log-uniform 1-40 atm, Y = 0.7 Dir + 0.3
 complete-combustion profile; spitfire_gb300.workloads.gri_states). One step = one batched evaluation of all states.
 
@@ -13,7 +13,19 @@ complete-combustion profile; spitfire_gb300.workloads.gri_states). One step = on
   cpu_baseline / --impl reference: the oracle (C++ restatement of Griffon, OpenMP over all host cores) on the
              same states
 
-Multi-GPU: states are independent, so each rank evaluates its own 65536-state batch (weak scaling, no collective).
+Further blocks of the same line (each measured once after warm-up, inputs resident):
+  newton     batched factor + solve of gamma*h*J - I (54 x 54) for the 65536 states: FP64 LU vs FP32 LU + 2 FP64
+             refinement sweeps, with the FP32 variant's error against the FP64 solution
+  ignition   8192 isobaric adiabatic GRI-3.0 reactors (T0 ~ U(900, 1500) K, phi ~ U(0.5, 2), p log-uniform 1-20
+             atm) integrated to T0 + 400 K or t = 0.1 s in one persistent launch replayed from a CUDA graph;
+             ignitions/s, ignition-delay error against the oracle integrator on a sample, the oracle's rate on the
+             host cores
+  flamelet   64 steady GRI-3.0 CH4/air flamelets (chi_st log-spaced 1e-2 - 1e3 1/s, grids of 64 - 256 points)
+             solved together from Burke-Schumann profiles (batched Newton, then pseudo-transient continuation);
+             flamelets/s, per-kernel times and rooflines of one batched launch, the oracle solver on a sample
+
+Multi-GPU: states, reactors and flamelets are independent, so each rank runs its own batch (weak scaling, no
+collective; the time is the max over ranks).
 """
 import argparse
 import json
@@ -28,8 +40,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 
+from spitfire_gb300.sharding import dist_env, max_over_ranks, sum_over_ranks  # noqa: E402
+
 METRIC = 'batched ignitions/s at 1e-6 rel τ_ign err; RHS+Jac states/s vs plain & CPU'
 N_STATES = 65536
+N_REACTORS = 8192
+N_FLAMELETS = 64
 # executed FP64 flops per GRI state of the batched Jacobian kernel (thread-level DADD + DMUL + 2*DFMA counted by
 # ncu, profiles/chem_kernel_jac_gri30_8192.md)
 FP64_FLOPS_PER_STATE = float(os.environ.get('SF_FP64_FLOPS_PER_STATE', '104960'))
@@ -99,13 +115,6 @@ class ClockSampler:
                 'reasons': reasons, 'samples': len(self.samples)}
 
 
-def dist_env():
-    rank = int(os.environ.get('RANK', '0'))
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    return rank, world, local
-
-
 def cpu_baseline(spec, q, seconds=10.0, threads=None):
     """Oracle RHS+Jacobian on the host cores over repeated passes of a sample of the states."""
     import numpy as np
@@ -129,6 +138,285 @@ def cpu_baseline(spec, q, seconds=10.0, threads=None):
     return {'value': done / dt, 'unit': 'states/s', 'cores': cores, 'kind': 'port',
             'sample': f'{done} GRI-3.0 isochoric RHS+Jacobian evaluations ({sample.shape[0]}-state passes of the '
                       f'benchmark states) in {dt:.1f} s'}
+
+
+def _ignite_one(args):
+    """Oracle integration of one isobaric GRI-3.0 reactor (runs in a spawned worker)."""
+    q0, p = args
+    import oracle as orc
+    import integrate as I
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    g = _ignite_one.__dict__.get('og')
+    if g is None:
+        orc.set_threads(1)
+        spec = ChemicalMechanismSpec.bundled('methane-gri30')
+        g = orc.OracleGriffon()
+        spec._populate_griffon(g)
+        _ignite_one.og = g
+    r = I.integrate(I.ReactorProblem(g, 'isobaric', pressure=p), q0, delta_temperature_ignition=400.,
+                    stop_at_time=0.1)
+    return r['t'], r['status'], r['steps']
+
+
+def _worker_init(root):
+    sys.path[:0] = [root, os.path.join(root, 'oracle')]
+
+
+def cpu_ignitions(q0, p, n_sample, seconds=30.0):
+    """Oracle ignitions of the first n_sample reactors on all host cores (spawned pool). Returns (ignitions/s,
+    cores, tau[list], status[list], wall seconds)."""
+    import multiprocessing as mp
+    cores = os.cpu_count()
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(ROOT,)) as pool:
+        pool.map(_ignite_one, [(q0[0], p[0])] * cores)  # worker start-up outside the timing
+        t0 = time.perf_counter()
+        res = []
+        it = pool.imap(_ignite_one, [(q0[i], p[i]) for i in range(n_sample)])
+        for r in it:
+            res.append(r)
+            if time.perf_counter() - t0 > seconds:
+                break
+        dt = time.perf_counter() - t0
+        pool.terminate()
+    return len(res) / dt, cores, [r[0] for r in res], [r[1] for r in res], dt
+
+
+def _flamelet_one(args):
+    z, x, oxy, fuel, ic = args
+    import oracle as orc
+    import flamelet_steady as FS
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    g = _flamelet_one.__dict__.get('og')
+    if g is None:
+        orc.set_threads(1)
+        spec = ChemicalMechanismSpec.bundled('methane-gri30')
+        g = orc.OracleGriffon()
+        spec._populate_griffon(g)
+        _flamelet_one.og = g
+    t0 = time.perf_counter()
+    op = FS.FlameletOperator(g, z, x, oxy, fuel)
+    st, how, it = FS.compute_steady_state(op, ic)
+    return st, how, it, time.perf_counter() - t0
+
+
+def cpu_flamelets(setups, idx, seconds=60.0):
+    """Oracle compute_steady_state of the flamelets `idx` on all host cores (spawned pool), stopped after `seconds`.
+    Returns (list of (index, state, method, cpu seconds)), cores, wall seconds."""
+    import multiprocessing as mp
+    cores = os.cpu_count()
+    ctx = mp.get_context('spawn')
+    out = []
+    with ctx.Pool(min(cores, len(idx)), initializer=_worker_init, initargs=(ROOT,)) as pool:
+        t0 = time.perf_counter()
+        args = [(setups[k].z, setups[k].x, setups[k].state_oxy, setups[k].state_fuel, setups[k].initial_state)
+                for k in idx]
+        it = pool.imap_unordered(_flamelet_job, list(zip(idx, args)))
+        try:
+            while True:
+                left = seconds - (time.perf_counter() - t0)
+                if left <= 0:
+                    break
+                out.append(it.next(timeout=left))
+        except (StopIteration, mp.TimeoutError):
+            pass
+        dt = time.perf_counter() - t0
+        pool.terminate()
+    return out, min(cores, len(idx)), dt
+
+
+def _flamelet_job(a):
+    k, args = a
+    st, how, it, sec = _flamelet_one(args)
+    return k, st, how, sec
+
+
+def _timed(fn, stream, reps=1):
+    """Average milliseconds of fn() on `stream` with CUDA events (one untimed call first)."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'MEASURED_PEAKS.json hbm_gbs (of measured)'
+    except Exception:
+        return 6800., 'fallback 6.8 TB/s (of fallback)'
+
+
+def bench_newton(q, rhs, J, gamma_h, stream):
+    """Batched Newton algebra on the benchmark states: FP64 LU vs FP32 LU + 2 FP64 refinement sweeps."""
+    import numpy as np
+    import torch
+    from spitfire_gb300.linalg import NewtonSystems, backward_error
+    n, m = q.shape
+    out = {'systems': n, 'm': m, 'gamma_h': 'log-uniform 1e-9 - 1e-5 s'}
+    xs = {}
+    for prec, name in ((0, 'fp64'), (1, 'fp32_lu_fp64_refine2')):
+        ns = NewtonSystems(n, m, prec, refine=2)
+        f_ms = _timed(lambda: ns.factor(J, gamma_h), stream)
+        x = torch.empty_like(rhs)
+        s_ms = _timed(lambda: ns.solve(rhs, out=x), stream)
+        xs[name] = x
+        A = ns.A[:512].cpu().numpy().reshape(-1, m, m).transpose(0, 2, 1)
+        be = backward_error(A, x[:512].cpu().numpy(), rhs[:512].cpu().numpy())
+        out[name] = {'factor_ms': f_ms, 'solve_ms': s_ms, 'systems_per_s': n / ((f_ms + s_ms) * 1e-3),
+                     'lu_tflops': (2. / 3. * m ** 3) * n / (f_ms * 1e-3) / 1e12,
+                     'max_backward_error_sample512': float(be.max()),
+                     'info_nonzero': int((ns.info != 0).sum().item())}
+        del ns
+    d = (xs['fp32_lu_fp64_refine2'] - xs['fp64']).abs().amax(1) / xs['fp64'].abs().amax(1)
+    q = torch.quantile(d, torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=d.device))
+    out['fp32_variant_rel_err_vs_fp64'] = {
+        'median': float(q[0]), 'p99': float(q[1]), 'p999': float(q[2]), 'max': float(d.max()),
+        'note': 'normwise forward difference of the two solutions per system; gamma*h*J - I reaches condition '
+                'numbers near 1/eps for the largest gamma*h, where any FP64 solver has O(1) forward error, so the '
+                'backward errors above are the accuracy statement'}
+    return out
+
+
+def bench_ignition(spec, rank, stream, cpu):
+    import numpy as np
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    d = W.ignition_batch(spec, N_REACTORS, seed=1003 + rank)
+    bi = BatchIntegrator(spec, 'isobaric')
+    kw = dict(delta_temperature_ignition=400., stop_at_time=0.1)
+    bi.run(d['q0'][:256], pressures=d['p'][:256], **kw)
+    out = bi.run(d['q0'], pressures=d['p'], graph=True, **kw)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    bi.replay()
+    e1.record(stream)
+    e1.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    tau = out['t'].cpu().numpy()
+    status = out['status'].cpu().numpy()
+    steps = out['counts'][:, 0].cpu().numpy()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    res = {'reactors': N_REACTORS, 'value': world * N_REACTORS / (ms * 1e-3), 'unit': 'ignitions/s',
+           'ms': ms, 'graph': 'one persistent launch captured in a CUDA graph, replay timed',
+           'status_counts': {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
+           'steps': {'min': int(steps.min()), 'median': float(np.median(steps)), 'max': int(steps.max())},
+           'device_status': spec.griffon.device_status()}
+    # FP32-LU + FP64-refinement integrator on the first 512 reactors against the FP64 run
+    o32 = BatchIntegrator(spec, 'isobaric', linear_precision=1, refine_sweeps=2).run(
+        d['q0'][:512], pressures=d['p'][:512], **kw)
+    t32 = o32['t'].cpu().numpy()
+    s32 = o32['status'].cpu().numpy()
+    ok = (s32 == status[:512])
+    rel32 = np.abs(t32[ok] - tau[:512][ok]) / tau[:512][ok]
+    res['fp32_lu_variant'] = {'reactors': 512, 'status_mismatches': int((~ok).sum()),
+                              'tau_rel_err_vs_fp64_max': float(rel32.max()),
+                              'tau_rel_err_vs_fp64_median': float(np.median(rel32))}
+    if cpu:
+        n_s = 256
+        rate, cores, t_cpu, st_cpu, dt = cpu_ignitions(d['q0'], d['p'], n_s, seconds=30.)
+        k = len(t_cpu)
+        both = [i for i in range(k) if st_cpu[i] == 2 and status[i] == 2]
+        rel = [abs(tau[i] - t_cpu[i]) / t_cpu[i] for i in both]
+        res['cpu_baseline'] = {'value': rate, 'unit': 'ignitions/s', 'cores': cores, 'kind': 'port',
+                               'sample': f'oracle integrator (ESDIRK64 + Newton + PI restated, C++ kernels) on the '
+                                         f'first {k} reactors, spawned pool, {dt:.1f} s'}
+        res['tau_rel_err_vs_oracle'] = {'reactors_compared': len(both), 'max': max(rel) if rel else None,
+                                        'status_mismatches': int(sum(st_cpu[i] != status[i] for i in range(k)))}
+    return res
+
+
+def bench_flamelet(spec, rank, stream, cpu):
+    import numpy as np
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.flamelet import FlameletBatch
+    setups = W.slfm_flamelet_setups(spec, N_FLAMELETS, seed=1004 + rank)
+    FlameletBatch(setups[:2]).compute_steady_state()
+    b = FlameletBatch(setups)
+    ns = b.ns
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out, conv, how = b.compute_steady_state()
+    torch.cuda.synchronize()
+    wall = max_over_ranks(time.perf_counter() - t0)
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    st = out.cpu().numpy()
+    conv_h = conv.cpu().numpy()
+    ext = []
+    for f, s in enumerate(setups):
+        T = st[b.offz_host[f] * ns:b.offz_host[f + 1] * ns:ns]
+        ext.append(bool(np.max(T - s.linear_temperature) < 10.))
+    pts = b.npts
+    res = {'flamelets': N_FLAMELETS, 'points': pts, 'value': world * N_FLAMELETS / wall, 'unit': 'flamelets/s',
+           'seconds': wall, 'points_per_s': world * pts / wall,
+           'converged': int(conv_h.sum()), 'by_newton': int(how['newton'].sum().item()),
+           'by_psitc': int(how['psitc'].sum().item()), 'extinguished': int(sum(ext)),
+           'device_status': spec.griffon.device_status()}
+    # one batched launch of each operation on the converged profiles
+    x = out.clone()
+    y = torch.empty_like(x)
+    k = {}
+    k['rhs_ms'] = _timed(lambda: b.rhs(x, out=y), stream, 3)
+    k['jacobian_ms'] = _timed(lambda: b.jacobian(x), stream, 3)
+    k['jacobian_eig_ms'] = _timed(lambda: b.jacobian(x, eig=True), stream, 3)
+    b.jacobian(x)
+    vals = b.values.clone()
+    k['matvec_ms'] = _timed(lambda: b.matvec(x, out=y), stream, 3)
+
+    def fac():
+        b.values.copy_(vals)
+        b.factor()
+    copy_ms = _timed(lambda: b.values.copy_(vals), stream, 3)
+    k['factor_ms'] = _timed(fac, stream, 3) - copy_ms
+    k['solve_ms'] = _timed(lambda: b.solve(x, out=y), stream, 3)
+    hbm, hbm_src = measured_peaks()
+    nvals = b.nvals
+    mv_bytes = (nvals + 2 * pts * ns) * 8
+    rhs_bytes = pts * 4 * ns * 8
+    fac_flops = pts * (2. / 3. * ns ** 3 + 2. * ns ** 3)
+    k['roofline'] = {
+        'matvec': {'bound': 'hbm', 'algorithmic_bytes': mv_bytes, 'achieved': mv_bytes / (k['matvec_ms'] * 1e-3)
+                   / 1e9, 'peak': hbm, 'unit': 'GB/s', 'frac': mv_bytes / (k['matvec_ms'] * 1e-3) / 1e9 / hbm,
+                   'peak_source': hbm_src},
+        'rhs_sweep': {'bound': 'fp64 (rates per point); HBM bytes reported', 'algorithmic_bytes': rhs_bytes,
+                      'achieved_gbs': rhs_bytes / (k['rhs_ms'] * 1e-3) / 1e9,
+                      'points_per_s': pts / (k['rhs_ms'] * 1e-3)},
+        'jacobian': {'points_per_s': pts / (k['jacobian_ms'] * 1e-3),
+                     'fp64_tflops_executed_est': FP64_FLOPS_PER_STATE * pts / (k['jacobian_ms'] * 1e-3) / 1e12},
+        'factor': {'bound': 'fp64', 'flops_per_point': 2. / 3. * ns ** 3 + 2. * ns ** 3,
+                   'achieved_tflops': fac_flops / (k['factor_ms'] * 1e-3) / 1e12}}
+    res['kernels'] = k
+    if cpu:
+        idx = list(range(0, N_FLAMELETS, 4))
+        done, cores, dt = cpu_flamelets(setups, idx, seconds=60.)
+        errs, mism = [], 0
+        for kf, s_cpu, how_cpu, sec in done:
+            g = st[b.offz_host[kf] * ns:b.offz_host[kf + 1] * ns]
+            if s_cpu is None or not conv_h[kf]:
+                mism += int((s_cpu is None) != (not conv_h[kf]))
+                continue
+            errs.append(float(np.max(np.abs(g[::ns] - s_cpu[::ns]) / s_cpu[::ns])))
+        npts_done = sum(setups[kf].nzi for kf, *_ in done)
+        res['cpu_baseline'] = {'value': len(done) / dt, 'unit': 'flamelets/s', 'cores': cores, 'kind': 'port',
+                               'points_per_s': npts_done / dt,
+                               'sample': f'oracle compute_steady_state (restated Newton + psitc, C++ kernels, numpy '
+                                         f'eigvals) of {len(done)} of the {len(idx)} flamelets k = 0, 4, 8, ... '
+                                         f'finished in {dt:.1f} s, one per core'}
+        res['T_rel_err_vs_oracle'] = {'flamelets_compared': len(errs), 'max': max(errs) if errs else None,
+                                      'convergence_mismatches': mism}
+    return res
 
 
 def run_reference(args, rank, world):
@@ -225,11 +513,7 @@ def main():
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
     barrier()
-    ms = statistics.mean(times)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(times), dev)
     value = world * N_STATES / (ms * 1e-3)
 
     # ---------------- end to end through the public API (host buffers)
@@ -253,11 +537,7 @@ def main():
         e2e_step()
     e1.record(stream)
     e1.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
     e2e = {'value': world * N_STATES / (e2e_ms * 1e-3), 'unit': 'states/s', 'ms_per_step': e2e_ms,
            'h2d_bytes_per_step': qpin.numel() * 8, 'd2h_bytes_per_step': (rhs_h.numel() + J_h.numel()) * 8}
 
@@ -299,6 +579,15 @@ def main():
     hbm_bytes = N_STATES * (neq + neq + neq * neq) * 8
     roof['hbm'] = {'algorithmic_bytes': hbm_bytes, 'achieved_gbs': hbm_bytes / (ms * 1e-3) / 1e9}
 
+    # ---------------- further workloads
+    gh = torch.tensor(d['gamma_h'], dtype=torch.float64, device=dev)
+    newton = bench_newton(q, rhs, J, gh, stream)
+    del J, J_h
+    torch.cuda.empty_cache()
+    cpu = rank == 0 and world == 1 and not args.no_cpu
+    ignition = bench_ignition(spec, rank, stream, cpu)
+    flamelet = bench_flamelet(spec, rank, stream, cpu)
+
     line = {'metric': METRIC, 'value': value, 'unit': 'states/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded GRI-3.0 states, config 2 distribution)',
@@ -308,7 +597,8 @@ def main():
                        'l2': 'flushed between steps (256 MB write outside the timed events)'},
             'e2e': e2e, 'roofline': roof, 'clocks': clk.summary(), 'gpu_launches': args.steps,
             'plain_gpu_form': {'value': N_STATES / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
-                               'speedup_batched_over_plain': plain_ms / ms}}
+                               'speedup_batched_over_plain': plain_ms / ms},
+            'newton': newton, 'ignition': ignition, 'flamelet': flamelet}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(spec, qh)
     if rank == 0:

@@ -162,7 +162,8 @@ class FlameletSetup:
 
 def burke_schumann_state(m, oxy, fuel, z, pressure):
     """Burke-Schumann (infinitely fast, complete combustion) interior state (flamelet.py:554-586), with HP mixing on
-    the project's own NASA7 thermodynamics."""
+    the project's own NASA7 thermodynamics: the stoichiometric products N2, H2O (and CO2) at the stoichiometric
+    mixture's atoms, mass fractions piecewise linear in Z through them, temperature from the mixed enthalpy."""
     zst = m.stoich_mixture_fraction(fuel, oxy)
     stmix = m.mix_streams([(m.copy_stream(oxy), 1 - zst), (m.copy_stream(fuel), zst)], 'mass', 'HP')
     atoms = m._get_atoms_in_stream(stmix, ['H', 'C', 'O', 'N'])
@@ -174,14 +175,14 @@ def burke_schumann_state(m, oxy, fuel, z, pressure):
     Yst = X * m.molecular_weights
     Yst /= Yst.sum()
     Yo, Yf = oxy.Y, fuel.Y
-    ns = m.n_species
-    out = np.empty((z.size - 2, ns))
-    for i in range(z.size - 2):
-        zi = z[1 + i]
-        h = m.mix_streams([(m.copy_stream(oxy), 1 - zi), (m.copy_stream(fuel), zi)], 'mass', 'HP').enthalpy_mass
-        Y = Yo + zi / zst * (Yst - Yo) if zi <= zst else Yst + (zi - zst) / (1. - zst) * (Yf - Yst)
-        T = m.temperature_from_enthalpy(h, Y, 1500.)
-        out[i] = np.hstack([T, Y[:-1]])
+    zi = z[1:-1]
+    # adiabatic mass-basis mixing: the mixture enthalpy is linear in Z between the stream enthalpies
+    h = (1. - zi) * oxy.enthalpy_mass + zi * fuel.enthalpy_mass
+    lean = (zi <= zst)[:, None]
+    Y = np.where(lean, Yo[None, :] + (zi / zst)[:, None] * (Yst - Yo)[None, :],
+                 Yst[None, :] + ((zi - zst) / (1. - zst))[:, None] * (Yf - Yst)[None, :])
+    T = m.temperature_from_enthalpy_vec(h, Y, 1500.)
+    out = np.hstack([T[:, None], Y[:, :-1]])
     return out.ravel()
 
 

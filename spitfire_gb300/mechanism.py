@@ -649,6 +649,34 @@ class ChemicalMechanismSpec:
             h[i] = hh / self._mw[i]
         return h
 
+    def species_h_cp_host_vec(self, T):
+        """Species enthalpies and heat capacities (J/kg, J/kg/K) at an array of temperatures: [n, ns] each, the
+        same clipped-range NASA7 evaluation as species_enthalpies_host / species_cp_host."""
+        T = np.asarray(T, dtype=np.float64)[:, None]
+        tmin, tmid, tmax = self._nasa[:, 0], self._nasa[:, 1], self._nasa[:, 2]
+        t = np.minimum(np.maximum(T, tmin[None, :]), tmax[None, :])
+        a = np.where((t <= tmid[None, :])[:, :, None], self._nasa[None, :, 3:10], self._nasa[None, :, 10:17])
+        cpr = a[..., 0] + t * (a[..., 1] + t * (a[..., 2] + t * (a[..., 3] + t * a[..., 4])))
+        hh = GAS_CONSTANT * t * (a[..., 0] + t * (a[..., 1] / 2 + t * (a[..., 2] / 3 + t * (a[..., 3] / 4 + t *
+                                                                                            a[..., 4] / 5))) +
+                                 a[..., 5] / t)
+        hh = hh + np.where(T != t, GAS_CONSTANT * cpr * (T - t), 0.)
+        return hh / self._mw[None, :], GAS_CONSTANT * cpr / self._mw[None, :]
+
+    def temperature_from_enthalpy_vec(self, h, Y, T_guess=1000.):
+        """temperature_from_enthalpy for arrays of enthalpies h[n] and mass fractions Y[n, ns]."""
+        h = np.asarray(h, dtype=np.float64)
+        T = np.full(h.shape, float(T_guess))
+        done = np.zeros(h.shape, dtype=bool)
+        for _ in range(100):
+            hs, cps = self.species_h_cp_host_vec(T)
+            dT = -((hs * Y).sum(1) - h) / (cps * Y).sum(1)
+            T = np.where(done, T, T + dT)
+            done |= np.abs(dT) < 1e-10 * T
+            if done.all():
+                break
+        return T
+
     def temperature_from_enthalpy(self, h, Y, T_guess=1000.):
         T = float(T_guess)
         for _ in range(100):

@@ -8,6 +8,10 @@ There is no public benchmark for this path; states are drawn as follows.
   CH4/air at phi (lean: CO2, H2O, N2, O2 excess; rich: CO2, CO, H2O, H2, N2 with the carbon and hydrogen deficit
   split 1:1 between CO and H2); Newton factor gamma*h = exp(U(ln 1e-9, ln 1e-5)) s.
 * Ignition (config 3): isobaric CH4/air, T0 ~ U(900, 1500) K, phi ~ U(0.5, 2), p = 101325 exp(U(0, ln 20)).
+* Steady flamelets (config 4): GRI-3.0, oxidizer air 300 K (O2:N2 = 1:3.76 molar), fuel CH4 300 K, 1 atm;
+  64 stoichiometric dissipation rates log-spaced 1e-2 - 1e3 1/s (Peters profile); flamelet k has a grid of
+  nz_k = 64 + floor(192 k / 63) points clustered at the stoichiometric mixture fraction (intensity 4), the grid
+  sizes assigned to the dissipation rates by a seeded permutation; Burke-Schumann initial profiles.
 """
 
 import numpy as np
@@ -97,3 +101,22 @@ def ignition_batch(mech: ChemicalMechanismSpec, n, seed=1003, T_range=(900., 150
     Y = np.array([ch4_air_mixture(mech, f) for f in phi])
     q0 = np.hstack([T0[:, None], Y[:, :-1]])
     return dict(T0=T0, phi=phi, p=p, Y=Y, q0=q0)
+
+
+def slfm_flamelet_setups(mech: ChemicalMechanismSpec, n=64, seed=1004, chi_range=(1e-2, 1e3), nz_range=(64, 256)):
+    """FlameletSetup objects of the steady-flamelet workload (see the module docstring)."""
+    from .flamelet import FlameletSetup, FlameletSpec
+    rng = np.random.default_rng(seed)
+    air = mech.stream('TPX', (300., 101325., 'O2:1 N2:3.76'))
+    fuel = mech.stream('TPX', (300., 101325., 'CH4:1'))
+    chis = np.logspace(np.log10(chi_range[0]), np.log10(chi_range[1]), n)
+    span = nz_range[1] - nz_range[0]
+    nz = np.array([nz_range[0] + (span * k) // max(n - 1, 1) for k in range(n)])
+    nz = nz[rng.permutation(n)]
+    out = []
+    for k in range(n):
+        fs = FlameletSpec(mech_spec=mech, oxy_stream=air, fuel_stream=fuel, grid_points=int(nz[k]),
+                          grid_type='clustered', grid_cluster_intensity=4., grid_cluster_point='stoichiometric',
+                          stoich_dissipation_rate=float(chis[k]), initial_condition='Burke-Schumann')
+        out.append(FlameletSetup(fs))
+    return out
