@@ -277,6 +277,9 @@ typedef struct sf_flamelet_batch {
   const double *mcoeff, *ncoeff, *chi; /* DEVICE [points] */
   int include_enthalpy_flux;
   int include_variable_cp;
+  const double *diffterm;   /* DEVICE [n_flamelets] diffusion term of each flamelet for the eigenvalue bound of
+                               sf_flamelet_jac_batch, or NULL to use its scalar diffterm argument for all */
+  const int *active;        /* DEVICE [n_flamelets] or NULL: flamelets with active[f] == 0 are left untouched */
 } sf_flamelet_batch;
 
 /* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218, adiabatic path). */
@@ -284,31 +287,40 @@ int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
                           void *stream);
 /* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, adiabatic path, rates options 0/1/2, exact transform).
  * If scale_and_offset, J <- prefactor*J - I on the diagonal blocks (flamelet_kernels.cpp:1395-1408). If
- * out_expeig is non-NULL it receives, for every row of a point, max(max Re(lambda) - diffterm, 0) over the
- * eigenvalues lambda of that point's diagonal block without the diffusion diagonal (block - diag(cmajor)),
- * computed by Householder-Hessenberg reduction and Francis double-shift QR on one warp; this replaces the dgeev
- * call at flamelet_kernels.cpp:1329-1341. scale_and_offset must be 0 when out_expeig is requested. */
+ * out_expeig is non-NULL it receives, for every row of a point, max(max Re(lambda) - d, 0) over the eigenvalues
+ * lambda of that point's diagonal block without the diffusion diagonal (block - diag(cmajor)), d = fb->diffterm[f]
+ * or the scalar diffterm, computed by balancing, Householder-Hessenberg reduction and Francis double-shift QR on
+ * one warp (exactly 0 without QR when the balanced block's Gershgorin bound is <= d); this replaces the dgeev call
+ * at flamelet_kernels.cpp:1329-1341. scale_and_offset must be 0 when out_expeig is requested. */
 int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, int rates_option,
                           int scale_and_offset, double prefactor, double diffterm, double *out_expeig,
                           double *out_values, void *stream);
 
-/* Block-Thomas factorization of a batch of BTDDOD matrices, in place (btddod_matrix_kernels.cpp:19-80).
- * values: DEVICE, layout per flamelet as above; l_values: DEVICE scratch-like output of nzi*ns*ns per flamelet at
- * point offset offsets_z[f]*ns*ns; pivots: DEVICE int [points][ns]. */
+/* The four block-Thomas functions take `active`: DEVICE int [n_flamelets] or NULL; flamelets with active[f] == 0
+ * are left untouched (their values, factors and outputs keep what they held).
+ * Block-Thomas factorization of a batch of BTDDOD matrices, in place (btddod_matrix_kernels.cpp:19-80).
+ * values: DEVICE, layout per flamelet as above; l_values: DEVICE output of nzi*ns*ns per flamelet at point offset
+ * offsets_z[f]*ns*ns (the L_i = diag(sub) D_{i-1}^-1 blocks); pivots: DEVICE int [points][ns], the row
+ * permutation of each block's LU factorization (factored row k is row pivots[k] of the block; the reference stores
+ * LAPACK swap indices there, which only its own solve reads). ns <= 128 and 3*ns*ns doubles must fit in the
+ * shared memory of one block (ns <= 97 on GB300). */
 int sf_btddod_factor_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
-                           const int *offsets_z_host, double *values, double *l_values, int *pivots, void *stream);
-/* Solve with the factors (btddod_matrix_kernels.cpp:82-119). rhs and out_x are point-major [points][ns]. */
+                           const int *offsets_z_host, double *values, double *l_values, int *pivots,
+                           const int *active, void *stream);
+/* Solve with the factors (btddod_matrix_kernels.cpp:82-119). rhs and out_x are point-major [points][ns]
+ * (they must not alias). */
 int sf_btddod_solve_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
                           const int *offsets_z_host, const double *values, const double *l_values,
-                          const int *pivots, const double *rhs, double *out_x, void *stream);
+                          const int *pivots, const double *rhs, double *out_x, const int *active, void *stream);
 /* y = A x for a batch of BTDDOD matrices (btddod_matrix_kernels.cpp:121-160). */
 int sf_btddod_matvec_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
-                           const double *values, const double *x, double *out_y, void *stream);
+                           const int *offsets_z_host, const double *values, const double *x, double *out_y,
+                           const int *active, void *stream);
 /* A <- matrix_scale*A + diag_scale*diag(d) (btddod_matrix_kernels.cpp:448-465). */
 int sf_btddod_scale_and_add_diagonal_batch(int n_flamelets, int ns, const int *offsets_z,
                                            const long long *offsets_v, const int *offsets_z_host, double *values,
                                            double matrix_scale, const double *diagonal, double diag_scale,
-                                           void *stream);
+                                           const int *active, void *stream);
 
 /* ------------------------------------------------------------------------------------------- measurement */
 /* Measured FP64 FMA throughput of the current device (TFLOP/s): independent register FMA chains on every SM,

@@ -55,7 +55,8 @@ class SfFlameletBatch(C.Structure):
     _fields_ = [('n_flamelets', C.c_int), ('offsets_z', _ip), ('offsets_v', _lp), ('offsets_z_host', _ip),
                 ('pressure', C.c_double), ('oxy_state', _dp), ('fuel_state', _dp),
                 ('cmajor', _dp), ('csub', _dp), ('csup', _dp), ('mcoeff', _dp), ('ncoeff', _dp), ('chi', _dp),
-                ('include_enthalpy_flux', C.c_int), ('include_variable_cp', C.c_int)]
+                ('include_enthalpy_flux', C.c_int), ('include_variable_cp', C.c_int), ('diffterm', _dp),
+                ('active', _ip)]
 
 
 def reactor_params(configuration='isobaric', heat_transfer='adiabatic', open_=False, pressure=101325.,

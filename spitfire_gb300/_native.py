@@ -50,12 +50,12 @@ def _declare(L):
     L.sf_flamelet_rhs_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _vp, _vp]
     L.sf_flamelet_jac_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _ip, _ip, C.c_double, C.c_double,
                                         _vp, _vp, _vp]
-    L.sf_btddod_factor_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
-    L.sf_btddod_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
-    L.sf_btddod_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.sf_btddod_factor_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.sf_btddod_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.sf_btddod_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_fp64_peak_probe.argtypes = [_ip, C.POINTER(C.c_double), _vp, _vp]
     L.sf_btddod_scale_and_add_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
-                                                         C.c_double, _vp]
+                                                         C.c_double, _vp, _vp]
 
 
 # Entry points declared in include/spitfire_gb300.h (the C-ABI test checks the library exports all of them).

@@ -1,11 +1,15 @@
-// Eigenvalues of a small real nonsymmetric matrix by one warp, in shared memory: Householder reduction to upper
-// Hessenberg form followed by the implicit double-shift (Francis) QR iteration with deflation. Only eigenvalues
-// are computed (the active block is updated, not the full Schur form). This is the published algorithm of
-// Golub & Van Loan, "Matrix Computations", sections 7.4-7.5 (Householder Hessenberg reduction, Francis QR step,
-// deflation by negligible subdiagonal entries, exceptional shifts after 10 and 20 stalled iterations), written for
-// a warp: reflector applications run over lanes.
+// Largest real part of the eigenvalues of a small real nonsymmetric matrix, by one warp, in shared memory:
+// Parlett-Reinsch balancing (diagonal similarity by powers of two, exact in floating point), Householder reduction
+// to upper Hessenberg form, then the implicit double-shift (Francis) QR iteration with deflation on the active
+// window only (eigenvalues, no Schur vectors). Published algorithms: B. N. Parlett and C. Reinsch, "Balancing a
+// matrix for calculation of eigenvalues and eigenvectors", Numer. Math. 13 (1969); G. H. Golub and C. F. Van Loan,
+// "Matrix Computations", sections 7.4-7.5 (Hessenberg reduction, Francis step, deflation, exceptional shifts).
 //
-// It replaces the LAPACK dgeev call Griffon makes per flamelet Jacobian block for the pseudo-transient
+// GB300 issues FP64 at a fixed cost per warp instruction whatever the number of active lanes, so the warp
+// layout keeps lanes busy: column-parallel Hessenberg updates (no per-column reductions), reflectors in the
+// tau form (one reciprocal), and a lane-parallel deflation scan.
+//
+// Replaces the LAPACK dgeev call Griffon makes per flamelet Jacobian block for the pseudo-transient
 // continuation time step (flamelet_kernels.cpp:1329-1341).
 #pragma once
 #include <cuda_runtime.h>
@@ -19,117 +23,207 @@ __device__ __forceinline__ double warp_sum_all(double v)
   return v;
 }
 
-// Reduce the n x n column-major matrix A (leading dimension n) to upper Hessenberg form in place.
-// v: n doubles of shared work space.
-__device__ void warp_hessenberg(double *A, int n, double *v)
+__device__ __forceinline__ double warp_max_all(double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Parlett-Reinsch balancing with radix 2 (scaling only): repeat until no row/column pair changes by more than
+// 5%, at most `max_sweeps` sweeps. Column-major A, leading dimension n.
+__device__ void warp_balance(double *A, int n, int max_sweeps = 32)
 {
   const int lane = threadIdx.x & 31;
-  for (int k = 0; k + 2 < n; ++k) {
-    // Householder vector for x = A[k+1:n, k]
-    double ss = 0.;
-    for (int i = k + 2 + lane; i < n; i += 32) ss += A[i + k * n] * A[i + k * n];
-    ss = warp_sum_all(ss);
-    const double x0 = A[(k + 1) + k * n];
-    if (ss == 0.) continue;  // already in Hessenberg form below the subdiagonal
-    const double alpha = -copysign(sqrt(x0 * x0 + ss), x0);
-    // v = x - alpha e1, beta = 2 / (v^T v)
-    for (int i = k + 1 + lane; i < n; i += 32) v[i] = (i == k + 1) ? x0 - alpha : A[i + k * n];
-    __syncwarp();
-    const double vtv = (x0 - alpha) * (x0 - alpha) + ss;
-    const double beta = 2. / vtv;
-    // left: A[k+1:, j] -= beta v (v^T A[k+1:, j]) for j >= k
-    for (int j = k; j < n; ++j) {
-      double s = 0.;
-      for (int i = k + 1 + lane; i < n; i += 32) s += v[i] * A[i + j * n];
-      s = warp_sum_all(s) * beta;
-      for (int i = k + 1 + lane; i < n; i += 32) A[i + j * n] -= s * v[i];
-      __syncwarp();
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    bool changed = false;
+    for (int i = 0; i < n; ++i) {
+      double c = 0., r = 0.;
+      for (int j = lane; j < n; j += 32)
+        if (j != i) {
+          c += fabs(A[j + i * n]);
+          r += fabs(A[i + j * n]);
+        }
+      c = warp_sum_all(c);
+      r = warp_sum_all(r);
+      if (c == 0. || r == 0. || !isfinite(c) || !isfinite(r)) continue;
+      double g = r * 0.5, f = 1.;
+      const double s = c + r;
+      for (int t = 0; t < 1100 && c < g; ++t) {
+        f *= 2.;
+        c *= 4.;
+      }
+      g = r * 2.;
+      for (int t = 0; t < 1100 && c >= g; ++t) {
+        f *= 0.5;
+        c *= 0.25;
+      }
+      if ((c + r) / f < 0.95 * s) {
+        changed = true;
+        const double fi = 1. / f;  // a power of two: exact
+        for (int j = lane; j < n; j += 32) {
+          A[i + j * n] *= fi;
+          A[j + i * n] *= f;
+        }
+        __syncwarp();
+      }
     }
-    // right: A[i, k+1:] -= beta (A[i, k+1:] v) v^T for all rows i
-    for (int i = lane; i < n; i += 32) {
-      double s = 0.;
-      for (int l = k + 1; l < n; ++l) s += A[i + l * n] * v[l];
-      s *= beta;
-      for (int l = k + 1; l < n; ++l) A[i + l * n] -= s * v[l];
-    }
-    __syncwarp();
-    for (int i = k + 2 + lane; i < n; i += 32) A[i + k * n] = 0.;
-    __syncwarp();
+    if (!changed) break;
   }
 }
 
-// Apply the reflector P = I - beta v v^T (v of length nr <= 3, v[0] = 1) to rows r0..r0+nr-1 of H over columns
-// c0..c1, and to columns r0..r0+nr-1 over rows c2..c3.
-__device__ __forceinline__ void apply_reflector(double *H, int n, const double *v, int nr, double beta, int r0, int c0,
+// Upper bound of the real parts of the eigenvalues by Gershgorin's theorem applied to rows and to columns.
+__device__ double warp_gershgorin_bound(const double *A, int n)
+{
+  const int lane = threadIdx.x & 31;
+  double br = -INFINITY, bc = -INFINITY;
+  for (int i = lane; i < n; i += 32) {
+    double rs = 0., cs = 0.;
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        rs += fabs(A[i + j * n]);
+        cs += fabs(A[j + i * n]);
+      }
+    br = fmax(br, A[i + i * n] + rs);
+    bc = fmax(bc, A[i + i * n] + cs);
+  }
+  return fmin(warp_max_all(br), warp_max_all(bc));
+}
+
+// Reduce the n x n column-major A to upper Hessenberg form in place. v: n doubles, s: n doubles of shared work.
+__device__ void warp_hessenberg(double *A, int n, double *v, double *s)
+{
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k + 2 < n; ++k) {
+    double ss = 0.;
+    for (int i = k + 2 + lane; i < n; i += 32) ss += A[i + k * n] * A[i + k * n];
+    ss = warp_sum_all(ss);
+    if (ss == 0.) continue;  // already zero below the subdiagonal
+    const double x0 = A[(k + 1) + k * n];
+    const double nrm = sqrt(x0 * x0 + ss);
+    const double alpha = -copysign(nrm, x0);
+    const double tau = 1. / (nrm * (nrm + fabs(x0)));  // 2 / (u^T u) for u = x - alpha e1
+    for (int i = k + 1 + lane; i < n; i += 32) v[i] = (i == k + 1) ? x0 - alpha : A[i + k * n];
+    __syncwarp();
+    // left: A[k+1:, j] -= tau u (u^T A[k+1:, j]), lanes over columns j > k; column k becomes alpha e1
+    for (int j = k + 1 + lane; j < n; j += 32) {
+      double d = 0.;
+      for (int i = k + 1; i < n; ++i) d += v[i] * A[i + j * n];
+      d *= tau;
+      for (int i = k + 1; i < n; ++i) A[i + j * n] -= d * v[i];
+    }
+    if (lane == 0) A[(k + 1) + k * n] = alpha;
+    for (int i = k + 2 + lane; i < n; i += 32) A[i + k * n] = 0.;
+    __syncwarp();
+    // right: A[i, k+1:] -= tau (A[i, k+1:] u) u^T, lanes over rows
+    for (int i = lane; i < n; i += 32) {
+      double d = 0.;
+      for (int l = k + 1; l < n; ++l) d += A[i + l * n] * v[l];
+      d *= tau;
+      for (int l = k + 1; l < n; ++l) A[i + l * n] -= d * v[l];
+    }
+    __syncwarp();
+  }
+  (void)s;
+}
+
+// Householder reflector P = I - tau u u^T mapping (x, y[, z]) to a multiple of e1 (u0 = x - alpha).
+__device__ __forceinline__ void house3(double x, double y, double z, int nr, double *u, double *tau)
+{
+  const double nn = x * x + y * y + (nr == 3 ? z * z : 0.);
+  if (nn == 0.) {
+    *tau = 0.;
+    u[0] = 1.;
+    u[1] = 0.;
+    u[2] = 0.;
+    return;
+  }
+  const double nrm = sqrt(nn);
+  u[0] = x + copysign(nrm, x);
+  u[1] = y;
+  u[2] = nr == 3 ? z : 0.;
+  *tau = 1. / (nrm * (nrm + fabs(x)));
+}
+
+// Apply P = I - tau u u^T (u of length nr <= 3) to rows r0..r0+nr-1 of H over columns c0..c1, and to columns
+// r0..r0+nr-1 over rows c2..c3.
+__device__ __forceinline__ void apply_reflector(double *H, int n, const double *u, int nr, double tau, int r0, int c0,
                                                 int c1, int c2, int c3)
 {
   const int lane = threadIdx.x & 31;
   for (int j = c0 + lane; j <= c1; j += 32) {
-    double s = 0.;
-    for (int a = 0; a < nr; ++a) s += v[a] * H[(r0 + a) + j * n];
-    s *= beta;
-    for (int a = 0; a < nr; ++a) H[(r0 + a) + j * n] -= s * v[a];
+    double s = u[0] * H[r0 + j * n] + u[1] * H[(r0 + 1) + j * n];
+    if (nr == 3) s += u[2] * H[(r0 + 2) + j * n];
+    s *= tau;
+    H[r0 + j * n] -= s * u[0];
+    H[(r0 + 1) + j * n] -= s * u[1];
+    if (nr == 3) H[(r0 + 2) + j * n] -= s * u[2];
   }
   __syncwarp();
   for (int i = c2 + lane; i <= c3; i += 32) {
-    double s = 0.;
-    for (int a = 0; a < nr; ++a) s += H[i + (r0 + a) * n] * v[a];
-    s *= beta;
-    for (int a = 0; a < nr; ++a) H[i + (r0 + a) * n] -= s * v[a];
+    double s = H[i + r0 * n] * u[0] + H[i + (r0 + 1) * n] * u[1];
+    if (nr == 3) s += H[i + (r0 + 2) * n] * u[2];
+    s *= tau;
+    H[i + r0 * n] -= s * u[0];
+    H[i + (r0 + 1) * n] -= s * u[1];
+    if (nr == 3) H[i + (r0 + 2) * n] -= s * u[2];
   }
   __syncwarp();
 }
 
-// Householder reflector mapping (x, y[, z]) to a multiple of e1: v = [1, y/(x-a), z/(x-a)], beta.
-__device__ __forceinline__ int house3(double x, double y, double z, int nr, double *v, double *beta)
+// Start of the unreduced block ending at row hi: the largest lo <= hi with H[lo, lo-1] negligible (set to zero), or
+// 0. Lanes test the subdiagonals in parallel, 32 rows at a time from the bottom.
+__device__ __forceinline__ int warp_find_lo(double *H, int n, int hi)
 {
-  const double nrm = sqrt(x * x + y * y + (nr == 3 ? z * z : 0.));
-  if (nrm == 0.) {
-    *beta = 0.;
-    v[0] = 1.;
-    v[1] = 0.;
-    v[2] = 0.;
-    return 0;
+  const int lane = threadIdx.x & 31;
+  for (int top = hi; top > 0; top -= 32) {
+    const int r = top - lane;  // candidate row, r >= 1
+    bool neg = false;
+    if (r >= 1) {
+      const double sub = fabs(H[r + (r - 1) * n]);
+      double s = fabs(H[(r - 1) + (r - 1) * n]) + fabs(H[r + r * n]);
+      if (s == 0.) s = 1.;
+      neg = sub <= 2.220446049250313e-16 * s;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, neg);
+    if (m) {
+      const int first = __ffs(m) - 1;  // lowest lane = largest row
+      const int lo = top - first;
+      if (lane == 0) H[lo + (lo - 1) * n] = 0.;
+      __syncwarp();
+      return lo;
+    }
   }
-  const double a = -copysign(nrm, x);
-  const double d = x - a;
-  v[0] = 1.;
-  v[1] = y / d;
-  v[2] = nr == 3 ? z / d : 0.;
-  const double vv = 1. + v[1] * v[1] + v[2] * v[2];
-  *beta = 2. / vv;
-  return 1;
+  return 0;
 }
 
-// Largest real part of the eigenvalues of the n x n matrix A (destroyed). Returns false if the QR iteration did not
-// converge within its iteration budget (the largest real part of the diagonal found so far is returned then).
-__device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_max)
+// Largest real part of the eigenvalues of the n x n matrix A (destroyed; A is balanced first). work: 2n doubles
+// of shared memory. If cutoff is given and the balanced matrix's Gershgorin bound is <= cutoff, the function
+// returns that bound instead of running QR (every eigenvalue is then known to have real part <= cutoff).
+// Returns false if the QR iteration did not converge within its budget (the largest real part of the diagonal
+// found so far is returned then).
+__device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_max, double cutoff = -INFINITY)
 {
-  warp_hessenberg(A, n, work);
+  warp_balance(A, n);
+  __syncwarp();
+  const double gb = warp_gershgorin_bound(A, n);
+  if (gb <= cutoff) {
+    *out_max = gb;
+    return true;
+  }
+  warp_hessenberg(A, n, work, work + n);
   double *H = A;
   double vmax = -INFINITY;
   int hi = n - 1, iter = 0, total = 0;
   const int budget = 40 * n;
   bool ok = true;
-  double v[3];
+  double u[3];
   while (hi >= 0) {
     if (total > budget) {
       ok = false;
       for (int i = 0; i <= hi; ++i) vmax = fmax(vmax, H[i + i * n]);
       break;
     }
-    // find the start lo of the unreduced block ending at hi
-    int lo = hi;
-    while (lo > 0) {
-      const double sub = fabs(H[lo + (lo - 1) * n]);
-      double s = fabs(H[(lo - 1) + (lo - 1) * n]) + fabs(H[lo + lo * n]);
-      if (s == 0.) s = 1.;
-      if (sub <= 2.220446049250313e-16 * s) {
-        H[lo + (lo - 1) * n] = 0.;
-        break;
-      }
-      --lo;
-    }
+    const int lo = hi > 0 ? warp_find_lo(H, n, hi) : 0;
     if (lo == hi) {
       vmax = fmax(vmax, H[hi + hi * n]);
       --hi;
@@ -141,12 +235,7 @@ __device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_ma
       const double c = H[hi + (hi - 1) * n], d = H[hi + hi * n];
       const double tr = 0.5 * (a + d), det = a * d - b * c;
       const double disc = tr * tr - det;
-      if (disc >= 0.) {
-        const double r = sqrt(disc);
-        vmax = fmax(vmax, tr + r);
-      } else {
-        vmax = fmax(vmax, tr);
-      }
+      vmax = fmax(vmax, disc >= 0. ? tr + sqrt(disc) : tr);
       hi -= 2;
       iter = 0;
       continue;
@@ -168,20 +257,20 @@ __device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_ma
     double y = H[(lo + 1) + lo * n] * (H[lo + lo * n] + H[(lo + 1) + (lo + 1) * n] - s);
     double z = H[(lo + 1) + lo * n] * H[(lo + 2) + (lo + 1) * n];
     for (int k = lo - 1; k <= hi - 3; ++k) {
-      double beta;
-      house3(x, y, z, 3, v, &beta);
-      if (beta != 0.) {
+      double tau;
+      house3(x, y, z, 3, u, &tau);
+      if (tau != 0.) {
         const int c0 = k < lo ? lo : k;
         const int r1 = k + 4 < hi ? k + 4 : hi;
-        apply_reflector(H, n, v, 3, beta, k + 1, c0, hi, lo, r1);
+        apply_reflector(H, n, u, 3, tau, k + 1, c0, hi, lo, r1);
       }
       x = H[(k + 2) + (k + 1) * n];
       y = H[(k + 3) + (k + 1) * n];
       if (k < hi - 3) z = H[(k + 4) + (k + 1) * n];
     }
-    double beta;
-    house3(x, y, 0., 2, v, &beta);
-    if (beta != 0.) apply_reflector(H, n, v, 2, beta, hi - 1, hi - 2, hi, lo, hi);
+    double tau;
+    house3(x, y, 0., 2, u, &tau);
+    if (tau != 0.) apply_reflector(H, n, u, 2, tau, hi - 1, hi - 2, hi, lo, hi);
   }
   *out_max = vmax;
   return ok;

@@ -36,6 +36,7 @@ struct FlmParams {
   int rates_option;
   double prefactor;
   double *eflux_store;  // if set: the enthalpy-flux diagonal correction is stored here (per point) instead
+  const int *active;    // device [nf] or null: flamelets with active[f] == 0 are skipped
   int groups_per_cta;
 };
 
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
   NoJ noj;
   for (int pt = blockIdx.x * p.groups_per_cta + gid; pt < p.n_points; pt += gridDim.x * p.groups_per_cta) {
     const int f = find_flamelet(p.offz, p.n_flamelets, pt);
+    if (p.active && !p.active[f]) continue;
     const int z0 = p.offz[f], nzi = p.offz[f + 1] - z0;
     const int iz = pt - z0;
     const double *st = p.state + (size_t)pt * ns;
@@ -186,21 +188,25 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
   }
 }
 
-// Pseudo-time-step eigenvalue bound (flamelet_kernels.cpp:1329-1341): for each point, max(max Re(lambda) - diffterm,
-// 0) of the transformed isobaric chemistry block (the block before the diffusion diagonal and the enthalpy-flux
-// correction are added), written to all ns entries of the point; then the held-back enthalpy-flux correction is
-// applied to the block. One warp per point, the block in shared memory.
+// Pseudo-time-step eigenvalue bound (flamelet_kernels.cpp:1329-1341): for each point, max(max Re(lambda) - d, 0)
+// of the transformed isobaric chemistry block (the block before the diffusion diagonal and the enthalpy-flux
+// correction are added), d the flamelet's diffusion term, written to all ns entries of the point; then the held-back
+// enthalpy-flux correction is applied to the block. One warp per point, the block in shared memory. When the
+// balanced block's Gershgorin bound is already <= d the result is exactly 0 and the QR iteration is skipped.
 __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *offz, const long long *offv,
-                                       double *values, const double *cmajor, double diffterm, double *expeig,
-                                       int *status, int warps)
+                                       double *values, const double *cmajor, double diffterm,
+                                       const double *diffterm_f, const int *active, double *expeig, int *status,
+                                       int warps)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *A = reinterpret_cast<double *>(smem) + (size_t)w * (ns * ns + ns);
+  double *A = reinterpret_cast<double *>(smem) + (size_t)w * (ns * ns + 2 * ns);
   double *work = A + ns * ns;
   for (int pt = blockIdx.x * warps + w; pt < n_points; pt += gridDim.x * warps) {
     const int f = find_flamelet(offz, nf, pt);
+    if (active && !active[f]) continue;
     const int iz = pt - offz[f];
+    const double d = diffterm_f ? diffterm_f[f] : diffterm;
     double *blk = values + offv[f] + (size_t)iz * ns * ns;
     for (int e = lane; e < ns * ns; e += 32) {
       const int col = e / ns, row = e - col * ns;
@@ -208,11 +214,11 @@ __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *
     }
     __syncwarp();
     double mx;
-    const bool ok = warp_max_real_eig(A, ns, work, &mx);
+    const bool ok = warp_max_real_eig(A, ns, work, &mx, d);
     if (!ok && lane == 0) report_error(status, DEVERR_WAIT_TIMEOUT);
     const double corr = expeig[(size_t)pt * ns];
     __syncwarp();
-    const double e = fmax(mx - diffterm, 0.);
+    const double e = fmax(mx - d, 0.);
     for (int q = lane; q < ns; q += 32) expeig[(size_t)pt * ns + q] = e;
     if (lane == 0) blk[0] -= corr;
     __syncwarp();
@@ -220,221 +226,395 @@ __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *
 }
 
 // ------------------------------------------------------------------------------- block-Thomas (BTDDOD) algebra
-// Factorization (btddod_matrix_kernels.cpp:19-80): D_0 = LU; for i >= 1: L_i = diag(sub_{i-1}) D_{i-1}^-1,
-// D_i <- D_i - L_i diag(sup_{i-1}), LU(D_i). One CTA per flamelet, D_{i-1} factors and D_i in shared memory.
+// Factorization (btddod_matrix_kernels.cpp:19-80): LU(D_0); for i >= 1: L_i = diag(sub_{i-1}) D_{i-1}^-1 (the
+// reference solves D_{i-1} X = I with dgetrs), D_i <- D_i - L_i diag(sup_{i-1}), LU(D_i). One CTA per flamelet
+// walks its blocks in order; within a block every step is spread over the CTA's threads: the inverse is a
+// right-looking triangular solve over all ns columns at once, the LU a right-looking factorization with two
+// barriers per column. Pivots are stored as the row permutation of each factorization (factored row k is row
+// perm[k] of the block), which the solve applies as one gather.
 constexpr int kFactorThreads = 256;
 
-__device__ void cta_lu(double *A, int n, int *piv, double *red_v, int *red_i)
+// In-place LU with partial pivoting of the n x n ROW-major A (shared memory) by the whole CTA (8 warps); perm
+// (shared, n ints) receives the row permutation. scratch: 3n doubles + 1 int of shared memory. n <= 128.
+// Per column k: warp 0 finds the pivot (integer comparison of magnitudes, the first largest as idamax), forms the
+// multipliers (scaled by 1/pivot, as dgetf2) and stages the two swapped rows; then all warps write the swapped and
+// updated trailing rows (warps over rows, lanes over contiguous columns), each element by one thread.
+__device__ void cta_lu_perm(double *A, int n, int *perm, double *scratch)
 {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  double *mcol = scratch, *prow = scratch + n, *krow = scratch + 2 * n;
+  int *pvt = reinterpret_cast<int *>(scratch + 3 * n);
+  for (int i = tid; i < n; i += nt) perm[i] = i;
+  __syncthreads();
   for (int k = 0; k < n; ++k) {
     if (warp == 0) {
-      double best = -1.;
-      int bi = k;
+      unsigned long long best = 0ull;
+      int p = k;
+      bool any = false;
       for (int i = k + lane; i < n; i += 32) {
-        const double v = fabs(A[i + k * n]);
-        if (v > best) { best = v; bi = i; }
+        const unsigned long long key = (unsigned long long)__double_as_longlong(A[i * n + k]) & 0x7fffffffffffffffull;
+        if (!any || key > best) { best = key; p = i; any = true; }
       }
+      if (!any) p = n;  // lanes without rows lose every comparison
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, p, o);
+        if (oi < n && (p >= n || ob > best || (ob == best && oi < p))) { best = ob; p = oi; }
+      }
+      const double pv = A[p * n + k];
+      const double inv = pv != 0. ? 1. / pv : 0.;
+      for (int i = k + lane; i < n; i += 32) {
+        const double x = A[(i == k ? p : (i == p ? k : i)) * n + k];
+        mcol[i] = i == k ? x : x * inv;
+      }
+      for (int j = k + 1 + lane; j < n; j += 32) {
+        prow[j] = A[p * n + j];
+        krow[j] = A[k * n + j];
       }
       if (lane == 0) {
-        piv[k] = bi;
-        red_i[0] = bi;
+        *pvt = p;
+        if (p != k) {
+          const int t = perm[k];
+          perm[k] = perm[p];
+          perm[p] = t;
+        }
       }
     }
     __syncthreads();
-    const int bi = red_i[0];
-    if (bi != k)
-      for (int j = tid; j < n; j += nt) {
-        const double t = A[k + j * n];
-        A[k + j * n] = A[bi + j * n];
-        A[bi + j * n] = t;
+    const int p = *pvt;
+    for (int i = k + tid; i < n; i += nt) A[i * n + k] = mcol[i];
+    if (p != k)
+      for (int j = tid; j < k; j += nt) {
+        const double t = A[k * n + j];
+        A[k * n + j] = A[p * n + j];
+        A[p * n + j] = t;
       }
-    __syncthreads();
-    const double pv = A[k + k * n];
-    if (pv != 0.) {
-      const double inv = 1. / pv;
-      for (int i = k + 1 + tid; i < n; i += nt) A[i + k * n] *= inv;
-    }
-    __syncthreads();
-    if (pv != 0.) {
-      const int r = n - k - 1;
-      for (int t = tid; t < r * r; t += nt) {
-        const int jj = t / r, ii = t - jj * r;
-        A[(k + 1 + ii) + (k + 1 + jj) * n] -= A[(k + 1 + ii) + k * n] * A[k + (k + 1 + jj) * n];
+    for (int i = k + warp; i < n; i += nw) {
+      const double m = mcol[i];
+      for (int j = k + 1 + lane; j < n; j += 32) {
+        double v;
+        if (i == k) v = prow[j];
+        else if (i == p) v = krow[j] - m * prow[j];
+        else v = A[i * n + j] - m * prow[j];
+        A[i * n + j] = v;
       }
     }
     __syncthreads();
   }
-  (void)red_v;
 }
 
-// X <- LU^-1 X for `ncols` right-hand-side columns (column-major, leading dimension n), columns split over warps.
-__device__ void cta_lu_solve_cols(const double *LU, const int *piv, int n, double *X, int ncols)
+// X <- (LU)^-1 P for the row-major factors of cta_lu_perm (the inverse of the original block), X row-major, all
+// columns at once: warps over rows, lanes over columns. uinv: n doubles of shared scratch for the reciprocals of
+// U's diagonal, computed in parallel up front so that no division sits on the per-row critical path (a
+// multiplication by the reciprocal instead of dtrsm's division: at most one ulp apart).
+__device__ void cta_lu_inverse(const double *LU, const int *perm, int n, double *X, double *uinv)
 {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int c = warp; c < ncols; c += nw) {
-    double *x = X + (size_t)c * n;
-    if (lane == 0)
-      for (int k = 0; k < n; ++k) {
-        const int p = piv[k];
-        if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; }
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  for (int k = tid; k < n; k += nt) uinv[k] = 1. / LU[k * n + k];
+  for (int k = warp; k < n; k += nw)
+    for (int c = lane; c < n; c += 32) X[k * n + c] = perm[k] == c ? 1. : 0.;
+  __syncthreads();
+  if (n == 1) {
+    if (tid == 0) X[0] = X[0] * uinv[0];
+    __syncthreads();
+    return;
+  }
+  // unit-lower forward substitution (as dtrsm); the last row is scaled by 1/U(n-1,n-1) when complete
+  for (int j = 0; j < n - 1; ++j) {
+    for (int k = j + 1 + warp; k < n; k += nw) {
+      const double l = LU[k * n + j];
+      if (j == n - 2) {  // warp-uniform: only the last row is scaled
+        const double sc = uinv[k];
+        for (int c = lane; c < n; c += 32) X[k * n + c] = (X[k * n + c] - l * X[j * n + c]) * sc;
+      } else {
+        for (int c = lane; c < n; c += 32) X[k * n + c] -= l * X[j * n + c];
       }
-    __syncwarp();
-    for (int j = 0; j < n; ++j) {
-      const double xj = x[j];
-      for (int i = j + 1 + lane; i < n; i += 32) x[i] -= LU[i + j * n] * xj;
-      __syncwarp();
     }
-    for (int j = n - 1; j >= 0; --j) {
-      if (lane == 0) x[j] /= LU[j + j * n];
-      __syncwarp();
-      const double xj = x[j];
-      for (int i = lane; i < j; i += 32) x[i] -= LU[i + j * n] * xj;
-      __syncwarp();
+    __syncthreads();
+  }
+  // upper back substitution; row j-1 is scaled by its pivot's reciprocal once its last update (from row j) is in
+  for (int j = n - 1; j >= 1; --j) {
+    for (int k = warp; k < j; k += nw) {
+      const double u = LU[k * n + j];
+      if (k == j - 1) {  // warp-uniform: the row completed in this step is scaled
+        const double sc = uinv[k];
+        for (int c = lane; c < n; c += 32) X[k * n + c] = (X[k * n + c] - u * X[j * n + c]) * sc;
+      } else {
+        for (int c = lane; c < n; c += 32) X[k * n + c] -= u * X[j * n + c];
+      }
     }
+    __syncthreads();
   }
 }
 
 __global__ void __launch_bounds__(kFactorThreads) btddod_factor_kernel(int nf, int ns, const int *offz,
                                                                        const long long *offv, double *values,
-                                                                       double *lvals, int *pivots)
+                                                                       double *lvals, int *perms, const int *active)
 {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double red_v[32];
-  __shared__ int red_i[32];
   const int f = blockIdx.x;
-  if (f >= nf) return;
+  if (f >= nf || (active && !active[f])) return;
   const int z0 = offz[f], nb = offz[f + 1] - z0;
   const int bs2 = ns * ns;
   double *vals = values + offv[f];
   double *lv = lvals + (size_t)z0 * bs2;
-  int *pv = pivots + (size_t)z0 * ns;
+  int *pv = perms + (size_t)z0 * ns;
   const double *sub = vals + (size_t)nb * bs2;
   const double *sup = sub + (size_t)(nb - 1) * ns;
-  double *Dprev = reinterpret_cast<double *>(smem);  // factors of D_{i-1}
-  double *Dcur = Dprev + bs2;                         // D_i
-  double *Lc = Dcur + bs2;                            // L_i
-  int *ppiv = reinterpret_cast<int *>(Lc + bs2);      // pivots of D_{i-1}
+  // row-major shared copies: factors of D_{i-1}, D_i, inverse of D_{i-1}
+  double *bufA = reinterpret_cast<double *>(smem);
+  double *bufB = bufA + bs2;
+  double *X = bufB + bs2;
+  double *lu_scratch = X + bs2;  // 3 ns doubles + 1 int (cta_lu_perm)
+  double *uinv = lu_scratch + 3 * ns + 1;
+  int *permA = reinterpret_cast<int *>(uinv + ns);
+  int *permB = permA + ns;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < bs2; e += nt) Dprev[e] = vals[e];
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    bufA[r * ns + c] = vals[e];
+  }
   __syncthreads();
-  cta_lu(Dprev, ns, ppiv, red_v, red_i);
-  for (int e = tid; e < bs2; e += nt) vals[e] = Dprev[e];
-  for (int k = tid; k < ns; k += nt) pv[k] = ppiv[k];
-  __syncthreads();
+  cta_lu_perm(bufA, ns, permA, lu_scratch);
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    vals[e] = bufA[r * ns + c];
+  }
+  for (int k = tid; k < ns; k += nt) pv[k] = permA[k];
   for (int i = 1; i < nb; ++i) {
-    // L_i = diag(sub_{i-1}) * D_{i-1}^-1: solve D_{i-1} X = I, then scale rows
-    for (int e = tid; e < bs2; e += nt) {
-      const int col = e / ns, row = e - col * ns;
-      Lc[e] = row == col ? 1. : 0.;
-      Dcur[e] = vals[(size_t)i * bs2 + e];
-    }
-    __syncthreads();
-    cta_lu_solve_cols(Dprev, ppiv, ns, Lc, ns);
-    __syncthreads();
+    cta_lu_inverse(bufA, permA, ns, X, uinv);
     const double *sb = sub + (size_t)(i - 1) * ns;
     const double *sp = sup + (size_t)(i - 1) * ns;
-    for (int e = tid; e < bs2; e += nt) {
-      const int col = e / ns, row = e - col * ns;
-      const double l = Lc[e] * sb[row];
-      Lc[e] = l;
-      lv[(size_t)i * bs2 + e] = l;
-      Dcur[e] += -sp[col] * l;
+    double *Di = vals + (size_t)i * bs2;
+    double *Li = lv + (size_t)i * bs2;
+    for (int e = tid; e < bs2; e += nt) {  // e: column-major index of the global arrays
+      const int c = e / ns, r = e - c * ns;
+      const double l = X[r * ns + c] * sb[r];
+      Li[e] = l;
+      bufB[r * ns + c] = Di[e] + (-sp[c]) * l;
     }
     __syncthreads();
-    cta_lu(Dcur, ns, ppiv, red_v, red_i);
+    cta_lu_perm(bufB, ns, permB, lu_scratch);
     for (int e = tid; e < bs2; e += nt) {
-      vals[(size_t)i * bs2 + e] = Dcur[e];
-      Dprev[e] = Dcur[e];
+      const int c = e / ns, r = e - c * ns;
+      Di[e] = bufB[r * ns + c];
     }
-    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = ppiv[k];
+    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = permB[k];
+    double *tb = bufA;
+    bufA = bufB;
+    bufB = tb;
+    int *tp = permA;
+    permA = permB;
+    permB = tp;
     __syncthreads();
   }
+}
+
+// Per-lane asynchronous 8-byte copies global -> shared (cp.async, completion tracked by commit groups; no
+// mbarrier wait is involved).
+__device__ __forceinline__ void async_copy_doubles(double *dst, const double *src, int n)
+{
+  const int lane = threadIdx.x & 31;
+  for (int e = lane; e < n; e += 32)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst + e)), "l"(src + e) : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void async_wait_all_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Register-distributed vector of a warp: element k lives in lane k % 32, register k / 32 (R registers).
+template <int R>
+__device__ __forceinline__ double vec_get(const double (&v)[R], int k)
+{
+  double out = 0.;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const double t = __shfl_sync(0xffffffffu, v[s], k & 31);
+    if ((k >> 5) == s) out = t;
+  }
+  return out;
 }
 
 // Solve (btddod_matrix_kernels.cpp:82-119), one warp per flamelet:
-//   y_0 = b_0, y_i = b_i - L_i y_{i-1};  x_{nb-1} = D^-1 y_{nb-1};  x_i = D_i^-1 (y_i - sup_i o x_{i+1})
-__global__ void btddod_solve_kernel(int nf, int ns, const int *offz, const long long *offv, const double *values,
-                                    const double *lvals, const int *pivots, const double *rhs, double *x)
+//   y_0 = b_0, y_i = b_i - L_i y_{i-1};  x_{nb-1} = D_{nb-1}^-1 y_{nb-1};  x_i = D_i^-1 (y_i - sup_i o x_{i+1}).
+// Vectors stay in registers; the next block's matrix is copied into shared memory while the current one is used.
+template <int R>
+__global__ void __launch_bounds__(32) btddod_solve_kernel(int nf, int ns, const int *offz, const long long *offv,
+                                                          const double *values, const double *lvals,
+                                                          const int *perms, const double *rhs, double *x,
+                                                          const int *active)
 {
-  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (f >= nf) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int f = blockIdx.x;
+  if (f >= nf || (active && !active[f])) return;
   const int lane = threadIdx.x & 31;
   const int z0 = offz[f], nb = offz[f + 1] - z0;
   const int bs2 = ns * ns;
+  double *buf[2] = {reinterpret_cast<double *>(smem), reinterpret_cast<double *>(smem) + bs2};
   const double *vals = values + offv[f];
   const double *lv = lvals + (size_t)z0 * bs2;
-  const int *pv = pivots + (size_t)z0 * ns;
+  const int *pv = perms + (size_t)z0 * ns;
   const double *sup = vals + (size_t)nb * bs2 + (size_t)(nb - 1) * ns;
   const double *b = rhs + (size_t)z0 * ns;
   double *xs = x + (size_t)z0 * ns;
-  // forward sweep into x (y values)
-  for (int k = lane; k < ns; k += 32) xs[k] = b[k];
-  __syncwarp();
+  double y[R];
+  // ---- forward sweep with the L blocks
+  if (nb > 1) async_copy_doubles(buf[1], lv + (size_t)bs2, bs2);
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int k = lane + 32 * s;
+    y[s] = k < ns ? b[k] : 0.;
+    if (k < ns) xs[k] = y[s];
+  }
   for (int i = 1; i < nb; ++i) {
-    const double *Li = lv + (size_t)i * bs2;
-    const double *yp = xs + (size_t)(i - 1) * ns;
-    for (int r = lane; r < ns; r += 32) {
-      double v = b[(size_t)i * ns + r];
-      for (int c = 0; c < ns; ++c) v += Li[(size_t)c * ns + r] * (-yp[c]);
-      xs[(size_t)i * ns + r] = v;
+    __syncwarp();
+    if (i + 1 < nb) {
+      async_copy_doubles(buf[(i + 1) & 1], lv + (size_t)(i + 1) * bs2, bs2);
+      async_wait_all_but_one();
+    } else {
+      async_wait_all();
     }
     __syncwarp();
+    const double *Li = buf[i & 1];
+    double acc[R];
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      acc[s] = k < ns ? b[(size_t)i * ns + k] : 0.;
+    }
+    for (int c = 0; c < ns; ++c) {
+      const double yc = vec_get<R>(y, c);
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const int k = lane + 32 * s;
+        if (k < ns) acc[s] += (-Li[k + c * ns]) * yc;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      y[s] = acc[s];
+      if (k < ns) xs[(size_t)i * ns + k] = acc[s];
+    }
   }
-  // backward sweep with the block LU factors (serial triangular solves per block)
+  // ---- backward sweep with the LU factors of the modified diagonal blocks
+  __syncwarp();
+  async_copy_doubles(buf[(nb - 1) & 1], vals + (size_t)(nb - 1) * bs2, bs2);
+  double xn[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) xn[s] = 0.;
   for (int i = nb - 1; i >= 0; --i) {
-    double *xi = xs + (size_t)i * ns;
-    if (i < nb - 1) {
-      for (int j = lane; j < ns; j += 32) xi[j] -= sup[(size_t)i * ns + j] * xs[(size_t)(i + 1) * ns + j];
-      __syncwarp();
-    }
-    warp_lu_solve(vals + (size_t)i * bs2, ns, pv + (size_t)i * ns, xi);
     __syncwarp();
+    if (i >= 1) {
+      async_copy_doubles(buf[(i - 1) & 1], vals + (size_t)(i - 1) * bs2, bs2);
+      async_wait_all_but_one();
+    } else {
+      async_wait_all();
+    }
+    __syncwarp();
+    const double *LU = buf[i & 1];
+    double v[R];
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      double t = 0.;
+      if (k < ns) {
+        t = xs[(size_t)i * ns + k];
+        if (i < nb - 1) t = t - sup[(size_t)i * ns + k] * xn[s];
+      }
+      v[s] = t;
+    }
+    // apply the row permutation: v'[k] = v[perm[k]]
+    double w[R];
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      const int src = k < ns ? pv[(size_t)i * ns + k] : 0;
+      double out = 0.;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const double t = __shfl_sync(0xffffffffu, v[q], src & 31);
+        if ((src >> 5) == q) out = t;
+      }
+      w[s] = out;
+    }
+    // reciprocals of U's diagonal for this lane's rows, off the per-row critical path
+    double rinv[R];
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      rinv[s] = k < ns ? 1. / LU[k + k * ns] : 0.;
+    }
+    // unit-lower then upper triangular solves (column-oriented, as dtrsm; 1/U(j,j) multiplies instead of the
+    // division, at most one ulp apart)
+    for (int j = 0; j < ns - 1; ++j) {
+      const double xj = vec_get<R>(w, j);
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const int k = lane + 32 * s;
+        if (k > j && k < ns) w[s] -= xj * LU[k + j * ns];
+      }
+    }
+    for (int j = ns - 1; j >= 0; --j) {
+      const double xj = vec_get<R>(w, j) * vec_get<R>(rinv, j);
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const int k = lane + 32 * s;
+        if (k == j) w[s] = xj;
+        else if (k < j) w[s] -= xj * LU[k + j * ns];
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      if (k < ns) xs[(size_t)i * ns + k] = w[s];
+      xn[s] = w[s];
+    }
   }
 }
 
-// y = A x (btddod_matrix_kernels.cpp:121-160), one warp per flamelet
-__global__ void btddod_matvec_kernel(int nf, int ns, const int *offz, const long long *offv, const double *values,
-                                     const double *x, double *y)
+// y = A x (btddod_matrix_kernels.cpp:121-160): one thread per row of every point of every flamelet.
+__global__ void btddod_matvec_kernel(int n_points, int nf, int ns, const int *offz, const long long *offv,
+                                     const double *values, const double *x, double *y, const int *active)
 {
-  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (f >= nf) return;
-  const int lane = threadIdx.x & 31;
-  const int z0 = offz[f], nb = offz[f + 1] - z0;
-  const int bs2 = ns * ns;
-  const double *vals = values + offv[f];
-  const double *sub = vals + (size_t)nb * bs2;
-  const double *sup = sub + (size_t)(nb - 1) * ns;
-  const double *xs = x + (size_t)z0 * ns;
-  double *ys = y + (size_t)z0 * ns;
-  for (int i = 0; i < nb; ++i)
-    for (int r = lane; r < ns; r += 32) {
-      double v = 0.;
-      for (int c = 0; c < ns; ++c) v += vals[(size_t)i * bs2 + (size_t)c * ns + r] * xs[(size_t)i * ns + c];
-      if (i >= 1) v += sub[(size_t)(i - 1) * ns + r] * xs[(size_t)(i - 1) * ns + r];
-      if (i <= nb - 2) v += sup[(size_t)i * ns + r] * xs[(size_t)(i + 1) * ns + r];
-      ys[(size_t)i * ns + r] = v;
-    }
+  const long long total = (long long)n_points * ns;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int pt = (int)(t / ns), r = (int)(t - (long long)pt * ns);
+    const int f = find_flamelet(offz, nf, pt);
+    if (active && !active[f]) continue;
+    const int z0 = offz[f], nb = offz[f + 1] - z0, iz = pt - z0;
+    const double *vals = values + offv[f];
+    const double *D = vals + (size_t)iz * ns * ns;
+    const double *xs = x + (size_t)z0 * ns;
+    double v = 0.;
+    for (int c = 0; c < ns; ++c) v += D[r + c * ns] * xs[(size_t)iz * ns + c];
+    const double *sub = vals + (size_t)nb * ns * ns;
+    const double *sup = sub + (size_t)(nb - 1) * ns;
+    if (iz >= 1) v += sub[(size_t)(iz - 1) * ns + r] * xs[(size_t)(iz - 1) * ns + r];
+    if (iz <= nb - 2) v += sup[(size_t)iz * ns + r] * xs[(size_t)(iz + 1) * ns + r];
+    y[t] = v;
+  }
 }
 
-// A <- matrix_scale*A + diag_scale*diag(d) (btddod_matrix_kernels.cpp:448-465), one CTA per flamelet
+// A <- matrix_scale*A + diag_scale*diag(d) (btddod_matrix_kernels.cpp:448-465): grid (chunks, flamelets), one
+// value per thread per chunk step, the diagonal entries of the blocks getting the added term.
 __global__ void btddod_scale_diag_kernel(int nf, int ns, const int *offz, const long long *offv, double *values,
-                                         double ms, const double *diag, double ds)
+                                         double ms, const double *diag, double ds, const int *active)
 {
-  const int f = blockIdx.x;
-  if (f >= nf) return;
+  const int f = blockIdx.y;
+  if (f >= nf || (active && !active[f])) return;
   const int z0 = offz[f], nb = offz[f + 1] - z0;
+  const long long bs2 = (long long)ns * ns;
   const long long ne = (long long)ns * (nb * ns + 2 * (nb - 1));
   double *vals = values + offv[f];
-  for (long long e = threadIdx.x; e < ne; e += blockDim.x) vals[e] *= ms;
-  __syncthreads();
-  for (int e = threadIdx.x; e < nb * ns; e += blockDim.x) {
-    const int iz = e / ns, q = e - iz * ns;
-    vals[(size_t)iz * ns * ns + (size_t)q * (ns + 1)] += ds * diag[(size_t)z0 * ns + e];
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+    double v = __dmul_rn(vals[e], ms);
+    if (e < nb * bs2) {
+      const long long iz = e / bs2, rem = e - iz * bs2;
+      if (rem % (ns + 1) == 0) v = __dadd_rn(v, __dmul_rn(ds, diag[(size_t)(z0 + iz) * ns + rem / (ns + 1)]));
+    }
+    vals[e] = v;
   }
 }
 
@@ -492,6 +672,7 @@ void fill(FlmParams &p, const sf_flamelet_batch *fb)
   p.chi = fb->chi;
   p.eflux = fb->include_enthalpy_flux;
   p.vcp = fb->include_variable_cp;
+  p.active = fb->active;
 }
 
 template <class F>
@@ -513,6 +694,22 @@ int check_launch()
     return SF_ERR_CUDA;
   }
   return SF_OK;
+}
+
+template <int R>
+int launch_solve(int nf, int ns, const int *offz, const long long *offv, const double *values,
+                 const double *l_values, const int *pivots, const double *rhs, double *out_x, const int *active,
+                 cudaStream_t st)
+{
+  const size_t smem = (size_t)2 * ns * ns * 8;
+  int dev, smem_max;
+  CUDA_THROW(cudaGetDevice(&dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)smem_max)
+    throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas solve");
+  CUDA_THROW(cudaFuncSetAttribute(btddod_solve_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  btddod_solve_kernel<R><<<nf, 32, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active);
+  return check_launch();
 }
 
 }  // namespace
@@ -613,15 +810,15 @@ int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
       CUDA_THROW(cudaGetDevice(&dev));
       CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
       CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-      const size_t per = (size_t)(ns * ns + ns) * 8;
+      const size_t per = (size_t)(ns * ns + 2 * ns) * 8;
       const int warps = (int)std::min<size_t>(8, (size_t)smem_max / per);
       if (warps < 1) throw sf_error(SF_ERR_UNSUPPORTED, "block too large for the eigenvalue kernel");
       CUDA_THROW(cudaFuncSetAttribute(flamelet_expeig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(per * warps)));
       const int grid = (int)std::min<long long>((long long)nsm * 2, ((long long)p.n_points + warps - 1) / warps);
       flamelet_expeig_kernel<<<grid, 32 * warps, per * warps, st>>>(p.n_points, p.n_flamelets, ns, p.offz, p.offv,
-                                                                    out_values, p.cmajor, diffterm, out_expeig,
-                                                                    hm.d_status, warps);
+                                                                    out_values, p.cmajor, diffterm, fb->diffterm,
+                                                                    fb->active, out_expeig, hm.d_status, warps);
       CUDA_THROW(cudaGetLastError());
     }
     return SF_OK;
@@ -629,14 +826,14 @@ int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
 }
 
 int sf_btddod_factor_batch(int nf, int ns, const int *offz, const long long *offv, const int *offz_host,
-                           double *values, double *l_values, int *pivots, void *stream)
+                           double *values, double *l_values, int *pivots, const int *active, void *stream)
 {
   if (nf < 1 || ns < 1 || ns > 128 || !offz || !offv || !values || !l_values || !pivots) {
     set_error("sf_btddod_factor_batch: bad argument");
     return SF_ERR_INVALID_ARGUMENT;
   }
   (void)offz_host;
-  const size_t smem = (size_t)3 * ns * ns * 8 + (size_t)ns * 4 + 16;
+  const size_t smem = (size_t)3 * ns * ns * 8 + (size_t)(4 * ns + 1) * 8 + (size_t)2 * ns * 4 + 16;
   return guarded([&] {
     int dev, smem_max;
     CUDA_THROW(cudaGetDevice(&dev));
@@ -645,46 +842,59 @@ int sf_btddod_factor_batch(int nf, int ns, const int *offz, const long long *off
       throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas factorization");
     CUDA_THROW(cudaFuncSetAttribute(btddod_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     btddod_factor_kernel<<<nf, kFactorThreads, smem, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, l_values,
-                                                                             pivots);
+                                                                             pivots, active);
     return check_launch();
   });
 }
 
 int sf_btddod_solve_batch(int nf, int ns, const int *offz, const long long *offv, const int *offz_host,
                           const double *values, const double *l_values, const int *pivots, const double *rhs,
-                          double *out_x, void *stream)
+                          double *out_x, const int *active, void *stream)
 {
-  if (nf < 1 || ns < 1 || !offz || !offv || !values || !l_values || !pivots || !rhs || !out_x) {
+  if (nf < 1 || ns < 1 || ns > 128 || !offz || !offv || !values || !l_values || !pivots || !rhs || !out_x) {
     set_error("sf_btddod_solve_batch: bad argument");
     return SF_ERR_INVALID_ARGUMENT;
   }
   (void)offz_host;
-  btddod_solve_kernel<<<(nf + 3) / 4, 128, 0, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, l_values, pivots,
-                                                                      rhs, out_x);
-  return check_launch();
+  cudaStream_t st = (cudaStream_t)stream;
+  return guarded([&] {
+    if (ns <= 32) return launch_solve<1>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active, st);
+    if (ns <= 64) return launch_solve<2>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active, st);
+    if (ns <= 96) return launch_solve<3>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active, st);
+    return launch_solve<4>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active, st);
+  });
 }
 
-int sf_btddod_matvec_batch(int nf, int ns, const int *offz, const long long *offv, const double *values,
-                           const double *x, double *out_y, void *stream)
+int sf_btddod_matvec_batch(int nf, int ns, const int *offz, const long long *offv, const int *offz_host,
+                           const double *values, const double *x, double *out_y, const int *active, void *stream)
 {
-  if (nf < 1 || ns < 1 || !offz || !offv || !values || !x || !out_y) {
+  if (nf < 1 || ns < 1 || !offz || !offv || !offz_host || !values || !x || !out_y) {
     set_error("sf_btddod_matvec_batch: bad argument");
     return SF_ERR_INVALID_ARGUMENT;
   }
-  btddod_matvec_kernel<<<(nf + 3) / 4, 128, 0, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, x, out_y);
+  const int npts = offz_host[nf];
+  const long long rows = (long long)npts * ns;
+  const int grid = (int)std::max<long long>(1, std::min<long long>((rows + 255) / 256, 152LL * 16));
+  btddod_matvec_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(npts, nf, ns, offz, offv, values, x, out_y, active);
   return check_launch();
 }
 
 int sf_btddod_scale_and_add_diagonal_batch(int nf, int ns, const int *offz, const long long *offv,
                                            const int *offz_host, double *values, double ms, const double *diag,
-                                           double ds, void *stream)
+                                           double ds, const int *active, void *stream)
 {
-  if (nf < 1 || ns < 1 || !offz || !offv || !values || !diag) {
+  if (nf < 1 || ns < 1 || nf > 65535 || !offz || !offv || !offz_host || !values || !diag) {
     set_error("sf_btddod_scale_and_add_diagonal_batch: bad argument");
     return SF_ERR_INVALID_ARGUMENT;
   }
-  (void)offz_host;
-  btddod_scale_diag_kernel<<<nf, 256, 0, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, ms, diag, ds);
+  long long max_ne = 0;
+  for (int f = 0; f < nf; ++f) {
+    const long long nb = offz_host[f + 1] - offz_host[f];
+    max_ne = std::max(max_ne, (long long)ns * (nb * ns + 2 * (nb - 1)));
+  }
+  const int chunks = (int)std::max<long long>(1, std::min<long long>((max_ne + 1023) / 1024, 1024));
+  btddod_scale_diag_kernel<<<dim3(chunks, nf), 256, 0, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, ms, diag,
+                                                                               ds, active);
   return check_launch();
 }
 

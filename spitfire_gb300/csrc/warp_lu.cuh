@@ -6,6 +6,15 @@
 
 namespace sfgb {
 
+__device__ __forceinline__ unsigned long long abs_key(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long abs_key(float x)
+{
+  return (unsigned long long)((unsigned)__float_as_int(x) & 0x7fffffffu);
+}
+
 // Right-looking LU with partial pivoting of an m x m column-major matrix in shared memory, one warp.
 // Pivot rows are 0-based. Returns info (0, or k+1 for an exactly zero pivot at step k).
 template <typename F>
@@ -14,17 +23,18 @@ __device__ __forceinline__ int warp_lu(F *A, int m, int *piv)
   const int lane = threadIdx.x & 31;
   int info = 0;
   for (int k = 0; k < m; ++k) {
-    // pivot: first index of the largest |A[i,k]|, i >= k (as idamax)
-    F best = -1;
-    int bi = k;
+    // pivot: first index of the largest |A[i,k]|, i >= k (as idamax); magnitudes are compared as the integer bit
+    // patterns of |x|, which order finite non-negative values like the values themselves
+    unsigned long long best = 0ull;
+    int bi = m;
     for (int i = k + lane; i < m; i += 32) {
-      const F v = fabs(A[i + k * m]);
-      if (v > best) { best = v; bi = i; }
+      const unsigned long long key = abs_key(A[i + k * m]);
+      if (bi == m || key > best) { best = key; bi = i; }
     }
     for (int o = 16; o > 0; o >>= 1) {
-      const F ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      if (oi < m && (bi >= m || ob > best || (ob == best && oi < bi))) { best = ob; bi = oi; }
     }
     if (lane == 0) piv[k] = bi;
     if (bi != k)

@@ -268,65 +268,91 @@ class FlameletBatch:
         scales[::ns] = 1.e3
         self.inv_scales = 1. / scales
         self.rates_option = self.setups[0].rates_option
-        self._cnt_v = torch.tensor(np.diff(offv), device=dev)
-        self._cnt_l = torch.tensor(np.diff(offz).astype(np.int64) * ns * ns, device=dev)
-        self._cnt_p = torch.tensor(np.diff(offz).astype(np.int64) * ns, device=dev)
         self.diffterm = 4. * np.array([s.max_dissipation_rate for s in self.setups])
+        self.zeros_dof = torch.zeros(self.npts * ns, dtype=torch.float64, device=dev)
 
     # ------------------------------------------------------------------------------------------ operations
+    # Every operation takes `active`: None (all flamelets) or a bool tensor [nf]; flamelets outside it are left
+    # untouched (their values, factors and outputs keep what they held).
+    def _mask(self, active):
+        if active is None:
+            return None
+        self._mask_keep = active.to(dtype=_torch().int32).contiguous()
+        return self._mask_keep
+
     def initial_state(self):
         torch = _torch()
         return torch.tensor(np.concatenate([s.initial_state for s in self.setups]), dtype=torch.float64,
                             device=self.values.device)
 
-    def rhs(self, state, out=None):
+    def rhs(self, state, out=None, active=None):
         torch = _torch()
         out = torch.empty_like(state) if out is None else out
-        N.check(N.load().sf_flamelet_rhs_batch(self.g.handle, C.byref(self.fb), N.ptr(state), N.ptr(out),
-                                               N.stream_handle()))
+        m = self._mask(active)
+        self.fb.active = C.cast(m.data_ptr(), C.POINTER(C.c_int)) if m is not None else None
+        try:
+            N.check(N.load().sf_flamelet_rhs_batch(self.g.handle, C.byref(self.fb), N.ptr(state), N.ptr(out),
+                                                   N.stream_handle()))
+        finally:
+            self.fb.active = None
         return out
 
-    def jacobian(self, state, scale_and_offset=False, prefactor=0., eig=False, diffterm=0.):
+    def jacobian(self, state, scale_and_offset=False, prefactor=0., eig=False, diffterm=0., diffterm_per_flamelet=None,
+                 active=None):
+        """BTDDOD Jacobian values into self.values; with eig also the eigenvalue bound per row, using
+        diffterm_per_flamelet (CUDA FP64 [nf]) when given, else the scalar diffterm."""
         torch = _torch()
         expeig = torch.empty(self.npts * self.ns, dtype=torch.float64, device=state.device) if eig else None
-        N.check(N.load().sf_flamelet_jac_batch(self.g.handle, C.byref(self.fb), N.ptr(state), self.rates_option,
-                                               int(scale_and_offset), float(prefactor), float(diffterm),
-                                               N.ptr(expeig), N.ptr(self.values), N.stream_handle()))
+        m = self._mask(active)
+        self.fb.active = C.cast(m.data_ptr(), C.POINTER(C.c_int)) if m is not None else None
+        self.fb.diffterm = C.cast(diffterm_per_flamelet.data_ptr(), C.POINTER(C.c_double)) \
+            if diffterm_per_flamelet is not None else None
+        try:
+            N.check(N.load().sf_flamelet_jac_batch(self.g.handle, C.byref(self.fb), N.ptr(state), self.rates_option,
+                                                   int(scale_and_offset), float(prefactor), float(diffterm),
+                                                   N.ptr(expeig), N.ptr(self.values), N.stream_handle()))
+        finally:
+            self.fb.active = None
+            self.fb.diffterm = None
         return (self.values, expeig) if eig else self.values
 
-    def expeig_per_flamelet_diffterm(self, state):
-        """Eigenvalue bounds with each flamelet's own diffterm = 4 max(chi) (flamelet.py:1587)."""
+    def diffterm_tensor(self, diffusion_factor=4.):
+        """Per-flamelet diffusion term diffusion_factor * max(chi) of steady_solve_psitc (flamelet.py:1587)."""
         torch = _torch()
-        _, e = self.jacobian(state, eig=True, diffterm=0.)
-        dt = torch.tensor(self.diffterm, dtype=torch.float64, device=state.device)[self.dof_flamelet]
-        return torch.clamp(e - dt, min=0.)
+        return torch.tensor(diffusion_factor / 4. * self.diffterm, dtype=torch.float64, device=self.values.device)
 
-    def factor(self):
+    def expeig_per_flamelet_diffterm(self, state):
+        """Eigenvalue bounds with each flamelet's own diffterm = 4 max(chi)."""
+        return self.jacobian(state, eig=True, diffterm_per_flamelet=self.diffterm_tensor())[1]
+
+    def factor(self, active=None):
         N.check(N.load().sf_btddod_factor_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
                                                 N.ptr(self.offz_host), N.ptr(self.values), N.ptr(self.lvalues),
-                                                N.ptr(self.pivots), N.stream_handle()))
+                                                N.ptr(self.pivots), N.ptr(self._mask(active)), N.stream_handle()))
 
-    def solve(self, rhs, out=None):
+    def solve(self, rhs, out=None, active=None):
         torch = _torch()
         out = torch.empty_like(rhs) if out is None else out
         N.check(N.load().sf_btddod_solve_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
                                                N.ptr(self.offz_host), N.ptr(self.values), N.ptr(self.lvalues),
-                                               N.ptr(self.pivots), N.ptr(rhs), N.ptr(out), N.stream_handle()))
+                                               N.ptr(self.pivots), N.ptr(rhs), N.ptr(out), N.ptr(self._mask(active)),
+                                               N.stream_handle()))
         return out
 
-    def matvec(self, x, out=None):
+    def matvec(self, x, out=None, active=None):
         torch = _torch()
         out = torch.empty_like(x) if out is None else out
         N.check(N.load().sf_btddod_matvec_batch(self.nf, self.ns, N.ptr(self.t_offz), N.ptr(self.t_offv),
-                                                N.ptr(self.values), N.ptr(x), N.ptr(out), N.stream_handle()))
+                                                N.ptr(self.offz_host), N.ptr(self.values), N.ptr(x), N.ptr(out),
+                                                N.ptr(self._mask(active)), N.stream_handle()))
         return out
 
-    def scale_and_add_diagonal(self, matrix_scale, diagonal, diag_scale):
+    def scale_and_add_diagonal(self, matrix_scale, diagonal, diag_scale, active=None):
         N.check(N.load().sf_btddod_scale_and_add_diagonal_batch(self.nf, self.ns, N.ptr(self.t_offz),
                                                                 N.ptr(self.t_offv), N.ptr(self.offz_host),
                                                                 N.ptr(self.values), float(matrix_scale),
                                                                 N.ptr(diagonal), float(diag_scale),
-                                                                N.stream_handle()))
+                                                                N.ptr(self._mask(active)), N.stream_handle()))
 
     def norms(self, v):
         """Weighted inf-norm per flamelet (scales 1e3 on T)."""
@@ -354,7 +380,7 @@ class FlameletBatch:
     def steady_solve_newton(self, state, active=None, tolerance=1.e-6, max_iterations=10,
                             max_factor_line_search=1.5, max_allowed_residual=1.e6, min_allowable_state_var=-1.e-6):
         """Batched restatement of Flamelet.steady_solve_newton (flamelet.py:1352-1485). Returns (state,
-        converged[nf] bool, iterations[nf])."""
+        converged[nf] bool, iterations[nf]). The factors of a flamelet stay in place until it needs new ones."""
         torch = _torch()
         dev = state.device
         nf = self.nf
@@ -363,9 +389,9 @@ class FlameletBatch:
         failed = torch.zeros(nf, dtype=torch.bool, device=dev)
         it = torch.zeros(nf, dtype=torch.int64, device=dev)
         res = torch.full((nf,), tolerance + 1., dtype=torch.float64, device=dev)
-        rhs = self.rhs(state)
+        rhs = self.rhs(state, active=run)
         eval_j = torch.ones(nf, dtype=torch.bool, device=dev)
-        store = (torch.zeros_like(self.values), torch.zeros_like(self.lvalues), torch.zeros_like(self.pivots))
+        dstate = torch.zeros_like(state)
         for _ in range(max_iterations + 1):
             go = run & ~failed & (res > tolerance) & (it < max_iterations)
             if not bool(go.any()):
@@ -373,19 +399,17 @@ class FlameletBatch:
             it = it + go.long()
             need = go & eval_j
             if bool(need.any()):
-                self.jacobian(state)
-                self.values.neg_()
-                self.factor()
-                store = self._keep_factors(need, store)
+                self.jacobian(state, active=need)
+                self.scale_and_add_diagonal(-1., self.zeros_dof, 0., active=need)  # J <- -J
+                self.factor(active=need)
                 eval_j = eval_j & ~need
-            self._use_factors(store)
-            dstate = self.solve(rhs)
+            self.solve(rhs, out=dstate, active=go)
             ok = self.finite(dstate)
             failed = failed | (go & ~ok)
             go = go & ok
             dstate = torch.where(self.expand(go), dstate, torch.zeros_like(dstate))
             norm_old = self.norms(rhs)
-            rhs_new = self.rhs(state + dstate)
+            rhs_new = self.rhs(state + dstate, active=go)
             ok = self.finite(rhs_new)
             failed = failed | (go & ~ok)
             go = go & ok
@@ -397,7 +421,7 @@ class FlameletBatch:
                     break
                 alpha = torch.where(cut, alpha * 0.5, alpha)
                 dstate = torch.where(self.expand(cut), dstate * self.expand(alpha), dstate)
-                trial = self.rhs(state + dstate)
+                trial = self.rhs(state + dstate, active=cut)
                 rhs_new = torch.where(self.expand(cut), trial, rhs_new)
                 eval_j = eval_j | cut
             state = torch.where(self.expand(go), state + dstate, state)
@@ -408,29 +432,6 @@ class FlameletBatch:
         state = torch.clamp(state, min=0.)
         conv = run & ~failed & (res <= tolerance) & (it <= max_iterations)
         return state, conv, it
-
-    def _values_mask(self, per_flamelet):
-        return per_flamelet.repeat_interleave(self._cnt_v)
-
-    def _lval_mask(self, per_flamelet):
-        return per_flamelet.repeat_interleave(self._cnt_l)
-
-    def _piv_mask(self, per_flamelet):
-        return per_flamelet.repeat_interleave(self._cnt_p)
-
-    def _keep_factors(self, need, store):
-        """Copy the freshly factorized BTDDOD arrays of the flamelets in `need` into `store` (vals, lvals, pivots)."""
-        torch = _torch()
-        v, l, p = store
-        v = torch.where(self._values_mask(need), self.values, v)
-        l = torch.where(self._lval_mask(need), self.lvalues, l)
-        p = torch.where(self._piv_mask(need), self.pivots, p)
-        return v, l, p
-
-    def _use_factors(self, store):
-        self.values.copy_(store[0])
-        self.lvalues.copy_(store[1])
-        self.pivots.copy_(store[2])
 
     def steady_solve_psitc(self, initial, active=None, tolerance=1.e-6, max_iterations=400,
                            min_allowable_state_var=-1.e-6, ds_init=1., ds_init_decrease=4., diffusion_factor=4.,
@@ -443,7 +444,7 @@ class FlameletBatch:
         dev = initial.device
         nf, ns = self.nf, self.ns
         run = torch.ones(nf, dtype=torch.bool, device=dev) if active is None else active.clone()
-        diffterm = torch.tensor(diffusion_factor / 4. * self.diffterm, dtype=torch.float64, device=dev)
+        dterm = self.diffterm_tensor(diffusion_factor)
         state = initial.clone()
         depth = torch.zeros(nf, dtype=torch.int64, device=dev)
         dsi = torch.full((nf,), float(ds_init), dtype=torch.float64, device=dev)
@@ -452,9 +453,9 @@ class FlameletBatch:
         jac_age = torch.zeros(nf, dtype=torch.int64, device=dev)
         res = torch.full((nf,), tolerance + 1., dtype=torch.float64, device=dev)
         dead = torch.zeros(nf, dtype=torch.bool, device=dev)
-        rhs = self.rhs(state)
+        rhs = self.rhs(state, active=run)
         eval_j = torch.ones(nf, dtype=torch.bool, device=dev)
-        store = (torch.zeros_like(self.values), torch.zeros_like(self.lvalues), torch.zeros_like(self.pivots))
+        dstate = torch.zeros_like(state)
         total_cap = (max_iterations + 1) * (max_recursion_depth + 3)
         for _ in range(total_cap):
             go = run & ~dead & (res > tolerance) & (it < max_iterations)
@@ -463,8 +464,7 @@ class FlameletBatch:
             it = it + go.long()
             need = go & eval_j
             if bool(need.any()):
-                _, expeig = self.jacobian(state, eig=True, diffterm=0.)
-                expeig = torch.clamp(expeig - self.expand(diffterm), min=0.)
+                _, expeig = self.jacobian(state, eig=True, diffterm_per_flamelet=dterm, active=need)
                 new_ds = torch.minimum(torch.minimum(ds_safety / (expeig + 1.e-16), ds_ramp * ds),
                                        torch.full_like(ds, ds_max))
                 first = need & ((it == 1) | global_ds)
@@ -472,18 +472,16 @@ class FlameletBatch:
                     0, self.dof_flamelet, new_ds, reduce='amin', include_self=True)
                 new_ds = torch.where(self.expand(first), self.expand(mn), new_ds)
                 ds = torch.where(self.expand(need), new_ds, ds)
-                self.scale_and_add_diagonal(-1., 1. / ds, 1.)
-                self.factor()
-                store = self._keep_factors(need, store)
+                self.scale_and_add_diagonal(-1., 1. / ds, 1., active=need)
+                self.factor(active=need)
                 jac_age = torch.where(need, torch.zeros_like(jac_age), jac_age)
             jac_age = torch.where(go & ~need, jac_age + 1, jac_age)
             eval_j = torch.where(go, (jac_age == 8) | (res > 1.e-2), eval_j)
-            self._use_factors(store)
-            dstate = self.solve(rhs)
+            self.solve(rhs, out=dstate, active=go)
             bad = go & ~self.finite(dstate)
             dstate = torch.where(self.expand(go), torch.nan_to_num(dstate), torch.zeros_like(dstate))
             norm_old = self.norms(rhs)
-            rhs_new = self.rhs(state + dstate)
+            rhs_new = self.rhs(state + dstate, active=go)
             bad = bad | (go & ~self.finite(rhs_new))
             rhs_new = torch.nan_to_num(rhs_new, nan=1e300, posinf=1e300, neginf=-1e300)
             alpha = torch.ones(nf, dtype=torch.float64, device=dev)
@@ -494,7 +492,7 @@ class FlameletBatch:
                     break
                 alpha = torch.where(cut, alpha * 0.5, alpha)
                 dstate = torch.where(self.expand(cut), dstate * self.expand(alpha), dstate)
-                trial = self.rhs(state + dstate)
+                trial = self.rhs(state + dstate, active=cut)
                 rhs_new = torch.where(self.expand(cut), trial, rhs_new)
                 eval_j = eval_j | cut
             state = torch.where(self.expand(ok_go), state + dstate, state)
@@ -516,7 +514,7 @@ class FlameletBatch:
                     jac_age = torch.where(rst, torch.zeros_like(jac_age), jac_age)
                     res = torch.where(rst, torch.full_like(res, tolerance + 1.), res)
                     eval_j = eval_j | rst
-                    rhs = torch.where(e, self.rhs(state), rhs)
+                    rhs = torch.where(e, self.rhs(state, active=rst), rhs)
         state = torch.clamp(state, min=0.)
         conv = run & ~dead & (res <= tolerance)
         return state, conv, it

@@ -41,8 +41,8 @@ def test_argument_errors_are_reported_without_a_device():
     L = N.load()
     assert L.sf_flamelet_stencils(None, None, 0, None, None, None, None, None, None, None) == 1
     assert 'bad argument' in L.sf_last_error().decode()
-    assert L.sf_btddod_matvec_batch(0, 0, None, None, None, None, None, None) == 1
-    assert L.sf_btddod_solve_batch(0, 0, None, None, None, None, None, None, None, None, None) == 1
+    assert L.sf_btddod_matvec_batch(0, 0, None, None, None, None, None, None, None, None) == 1
+    assert L.sf_btddod_solve_batch(0, 0, None, None, None, None, None, None, None, None, None, None) == 1
 
 
 def test_shard_ranges_cover_contiguously():
