@@ -239,7 +239,7 @@ typedef struct sf_integrate_params {
 /* Per-reactor outcome codes written to out_status. */
 enum sf_integrate_status {
   SF_INT_RUNNING = 0, SF_INT_DONE = 1, SF_INT_IGNITED = 2, SF_INT_STEADY = 3, SF_INT_MAX_STEPS = 4,
-  SF_INT_NAN = 5, SF_INT_NO_IGNITION = 6
+  SF_INT_NAN = 5, SF_INT_NO_IGNITION = 6, SF_INT_RECORD_FULL = 7
 };
 
 size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
@@ -252,6 +252,27 @@ size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params 
 int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *params, const sf_integrate_params *iparams,
                        int n, const double *q0, const double *pressures, double *out_q, double *out_t,
                        int *out_counts, int *out_status, void *workspace, size_t workspace_bytes, void *stream);
+
+/* sf_integrate_batch that also records every accepted step for adjoint sensitivities: trajectory is DEVICE
+ * [n][capacity_steps][2 + 6*neq] doubles, per step (t_n, dt_n, Y_1..Y_6) with Y_1 = y_n and Y_2..Y_6 the converged
+ * ESDIRK64 stage values (in the integrator's order). A reactor that needs more steps than the capacity stops with
+ * SF_INT_RECORD_FULL. No reference counterpart (the reference computes no parameter sensitivities). */
+int sf_integrate_record_batch(const sf_mech *mech, const sf_reactor_params *params, const sf_integrate_params *iparams,
+                              int n, const double *q0, const double *pressures, double *out_q, double *out_t,
+                              int *out_counts, int *out_status, void *workspace, size_t workspace_bytes,
+                              double *trajectory, int capacity_steps, void *stream);
+
+/* ------------------------------------------------------------------------------------------ rate parameters */
+/* Parameter adjoint of the closed adiabatic reactor right-hand side f(q; theta), theta = (ln A_r, E_a,r) per
+ * reaction (forward, or high-pressure for falloff, Arrhenius coefficients; E_a in J/kmol), reactions in the
+ * mechanism's internal order (simple, three-body, Lindemann, Troe, as the setters were called):
+ *   out_grad[i][2r] += sum_s w_is^T df/d ln A_r (q_is),  out_grad[i][2r+1] += sum_s w_is^T df/d E_a,r (q_is)
+ * for items i < n_items and stages s < stages; q and w are DEVICE [n_items][stages][neq] (isobaric [T, Y] or
+ * isochoric [rho, T, Y] per params->configuration), pressures DEVICE [n_items] (isobaric; NULL = params->pressure),
+ * out_grad DEVICE [n_items][2*n_reactions], accumulated. No reference counterpart. */
+int sf_rate_param_adjoint_batch(const sf_mech *mech, const sf_reactor_params *params, int n_items, int stages,
+                                const double *q, const double *pressures, const double *w, double *out_grad,
+                                void *stream);
 
 /* ------------------------------------------------------------------------------------------------ flamelets */
 /* Stencil coefficients (flamelet_kernels.cpp:31-48); host pointers, host computation (setup only). */

@@ -445,6 +445,65 @@ void production_rates(const Mech &m, double T, double rho, double mmw, const dou
   }
 }
 
+// Net rate of progress q_r of every reaction (as production_rates computes it) and s_r = dq_r / d ln k_r, k_r the
+// forward (high-pressure for falloff) rate constant: k_r enters q_r linearly except through Pr = k0 [M] / k_inf of
+// the falloff factor, so s_r = q_r for simple and three-body reactions, q_r Pr/(1+Pr) for Lindemann and
+// q_r (Pr/(1+Pr) - d ln F / d ln Pr) for Troe (log10 F = log10 Fc / (1 + f1^2)). Project-written: the reference has
+// no parameter sensitivities.
+void rate_param_sens(const Mech &m, double T, double rho, double mmw, const double *y, double *q, double *sr)
+{
+  const int ns = m.ns;
+  const double invT = 1. / T, logT = std::log(T), conc = rho / mmw;
+  const double invRu = 1. / m.Ru, port = m.pref * invT * invRu;
+  std::vector<double> g(ns);
+  gibbs(m, T, g.data(), nullptr);
+  int r = 0;
+  for (const Rxn &x : m.rx) {
+    double k = kf_of(x, T, invT, logT);
+    double fac = 1.;
+    if (x.kind == SF_RXN_THIRD_BODY) {
+      k *= third_body(x, y, rho, conc);
+    } else if (x.kind == SF_RXN_LINDEMANN) {
+      const double pr = arrh(x.kp, logT, invT) / k * third_body(x, y, rho, conc);
+      k /= (1 + k / (arrh(x.kp, logT, invT) * third_body(x, y, rho, conc)));
+      fac = pr / (1 + pr);
+    } else if (x.kind == SF_RXN_TROE) {
+      const double pr = arrh(x.kp, logT, invT) / k * third_body(x, y, rho, conc);
+      const double lfc = log10_fcent(x, T, invT);
+      const double lpc = std::log10(std::max(pr, 1.e-300)) + (-0.4 - 0.67 * lfc);
+      const double nn = 0.75 - 1.27 * lfc;
+      const double den = nn - 0.14 * lpc;
+      const double f1 = lpc / den;
+      k = k * std::pow(10, lfc / (1 + f1 * f1)) * pr / (1 + pr);
+      fac = pr / (1 + pr);
+      if (pr > 1.e-300) fac -= lfc * (-2. * f1 / ((1 + f1 * f1) * (1 + f1 * f1))) * nn / (den * den);
+    }
+    double kr = 0.;
+    if (x.has_orders) {
+      for (size_t i = 0; i < x.sp.size(); ++i)
+        if (x.sp_nonzero[i]) k *= std::pow(std::max(y[x.sp[i]] * rho * m.invmw[x.sp[i]], 0.), x.sp_order[i]);
+    } else {
+      if (x.reversible) {
+        double sg = 0.;
+        for (size_t i = 0; i < x.net.size(); ++i) sg += x.net_nu[i] * g[x.net[i]];
+        kr = k * std::exp(x.sum_nu * std::log(port) - invT * invRu * sg);
+      }
+      for (size_t i = 0; i < x.reac.size(); ++i) {
+        const double C = y[x.reac[i]] * rho * m.invmw[x.reac[i]];
+        for (int p = 0; p < x.reac_nu[i]; ++p) k *= C;
+      }
+      if (x.reversible)
+        for (size_t i = 0; i < x.prod.size(); ++i) {
+          const double C = y[x.prod[i]] * rho * m.invmw[x.prod[i]];
+          for (int p = 0; p < x.prod_nu[i]; ++p) kr *= C;
+        }
+    }
+    q[r] = k - kr;
+    sr[r] = (k - kr) * fac;
+    ++r;
+  }
+}
+
 // d(prod_j C_j^nu_j)/dY_s for the species at list position `at` (its stoich counted once), times rho/M_s
 inline double dprod(const Mech &m, const std::vector<int> &idx, const std::vector<int> &nu, const double *y,
                     double rho, int at)
@@ -1152,7 +1211,7 @@ int oracle_thermo(const void *mp, int what, int n, const double *T, const double
 {
   const Mech &m = *static_cast<const Mech *>(mp);
   const int ns = m.ns;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     std::vector<double> a(ns), b(ns);
     const double *y = Y + (size_t)s * ns;
@@ -1181,7 +1240,7 @@ int oracle_thermo(const void *mp, int what, int n, const double *T, const double
 int oracle_production_rates(const void *mp, int n, const double *T, const double *rho, const double *Y, double *w)
 {
   const Mech &m = *static_cast<const Mech *>(mp);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     const double *y = Y + (size_t)s * m.ns;
     production_rates(m, T[s], rho[s], mmw_of(m, y), y, w + (size_t)s * m.ns);
@@ -1194,7 +1253,7 @@ int oracle_rates_sens(const void *mp, int n, const double *rho, const double *T,
 {
   const Mech &m = *static_cast<const Mech *>(mp);
   const size_t n1 = m.ns + 1;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     const double *y = Y + (size_t)s * m.ns;
     rates_sens(m, T[s], rho[s], mmw_of(m, y), y, opt, w + (size_t)s * m.ns, S + (size_t)s * n1 * n1);
@@ -1207,7 +1266,7 @@ int oracle_reactor_rhs(const void *mp, const sf_reactor_params *P, int n, const 
 {
   const Mech &m = *static_cast<const Mech *>(mp);
   const int neq = P->configuration == 0 ? m.ns : m.ns + 1;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     if (P->configuration == 0)
       rhs_isobaric(m, *P, pres ? pres[s] : P->pressure, q + (size_t)s * neq, rhs + (size_t)s * neq);
@@ -1222,7 +1281,7 @@ int oracle_reactor_jac(const void *mp, const sf_reactor_params *P, int opt, int 
 {
   const Mech &m = *static_cast<const Mech *>(mp);
   const int neq = P->configuration == 0 ? m.ns : m.ns + 1;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     if (P->configuration == 0)
       jac_isobaric(m, *P, opt, pres ? pres[s] : P->pressure, q + (size_t)s * neq, rhs + (size_t)s * neq,
@@ -1233,9 +1292,24 @@ int oracle_reactor_jac(const void *mp, const sf_reactor_params *P, int opt, int 
   return 0;
 }
 
+int oracle_rate_param_sens(const void *mp, int n, const double *T, const double *rho, const double *Y, double *q,
+                           double *sr)
+{
+  const Mech &m = *static_cast<const Mech *>(mp);
+  const int nr = (int)m.rx.size();
+#pragma omp parallel for schedule(static) if (n >= 64)
+  for (int i = 0; i < n; ++i) {
+    const double *y = Y + (size_t)i * m.ns;
+    double sim = 0.;
+    for (int s = 0; s < m.ns; ++s) sim += y[s] * m.invmw[s];
+    rate_param_sens(m, T[i], rho[i], 1. / sim, y, q + (size_t)i * nr, sr + (size_t)i * nr);
+  }
+  return 0;
+}
+
 int oracle_lu_factor(int n, int m, double *A, int *piv, int *info)
 {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) {
     const int r = lu_factor(m, A + (size_t)s * m * m, piv + (size_t)s * m);
     if (info) info[s] = r;
@@ -1245,7 +1319,7 @@ int oracle_lu_factor(int n, int m, double *A, int *piv, int *info)
 
 int oracle_lu_solve(int n, int m, const double *LU, const int *piv, double *b)
 {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n >= 64)
   for (int s = 0; s < n; ++s) lu_solve(m, LU + (size_t)s * m * m, piv + (size_t)s * m, b + (size_t)s * m);
   return 0;
 }

@@ -50,6 +50,7 @@ def lib():
         L.oracle_reactor_jac.argtypes = [C.c_void_p, C.POINTER(SfReactorParams), C.c_int, C.c_int, _dp, _dp, _dp,
                                          _dp]
         L.oracle_lu_factor.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip]
+        L.oracle_rate_param_sens.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp]
         L.oracle_lu_solve.argtypes = [C.c_int, C.c_int, _dp, _ip, _dp]
         L.oracle_flamelet_stencils.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.oracle_flamelet_rhs.argtypes = [C.c_void_p, _dp, C.c_double, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp, C.c_int,
@@ -171,6 +172,16 @@ class OracleGriffon(GriffonSetters):
         out = np.zeros_like(Y)
         lib().oracle_production_rates(self.handle, T.size, _p(T), _p(rho), _p(Y), _p(out))
         return out
+
+    def rate_param_sens_batch(self, T, rho, Y):
+        """(q [n][nr], s [n][nr]): net rates of progress and their derivatives with respect to the log of the forward
+        (high-pressure for falloff) rate constant, reactions in the internal (setter) order."""
+        T, rho, Y = _d(T), _d(rho), _d(Y)
+        nr = len(self._rec.reactions)
+        q = np.zeros((T.size, nr))
+        sr = np.zeros((T.size, nr))
+        lib().oracle_rate_param_sens(self.handle, T.size, _p(T), _p(rho), _p(Y), _p(q), _p(sr))
+        return q, sr
 
     def prod_rates_primitive_sensitivities(self, density, temperature, mass_fractions, rates_sensitivity_option,
                                            prod_rates_sens):

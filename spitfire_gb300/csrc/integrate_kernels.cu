@@ -50,6 +50,8 @@ struct IntParams {
   int *out_counts, *out_status;
   unsigned int *queue;
   size_t per_warp;  // doubles of shared memory per warp
+  double *rec;      // optional trajectory record: [n][rec_cap][2 + 6 neq] = (t_n, dt_n, stage values Y_1..Y_6)
+  int rec_cap;
 };
 
 // Writes A = pref * J - I straight from the Jacobian evaluation.
@@ -134,6 +136,20 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
         ++njac;
       }
       ++count;
+      // trajectory record of this attempt (slot of the next accepted step; a rejected attempt is overwritten)
+      double *slot = nullptr;
+      if (p.rec) {
+        if (nsteps >= p.rec_cap) {
+          status = SF_INT_RECORD_FULL;
+          break;
+        }
+        slot = p.rec + ((size_t)r * p.rec_cap + nsteps) * (2 + 6 * (size_t)neq);
+        if (lane == 0) {
+          slot[0] = t;
+          slot[1] = dt;
+        }
+        for (int i = lane; i < neq; i += 32) slot[2 + i] = y[i];
+      }
       // ---------------- one ESDIRK64 step (methods.py:502-612)
       reactor_eval<32, false>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, k, noj);
       for (int i = lane; i < neq; i += 32) Y[i] = y[i];
@@ -191,6 +207,8 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
           }
         }
         for (int i = lane; i < neq; i += 32) k[s * neq + i] = f[i];
+        if (slot)
+          for (int i = lane; i < neq; i += 32) slot[2 + (size_t)s * neq + i] = Y[i];
         __syncwarp();
         if (!conv) nl_ok = false;
       }
@@ -306,9 +324,10 @@ size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params 
   return 256;
 }
 
-int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
-                       const double *q0, const double *pressures, double *out_q, double *out_t, int *out_counts,
-                       int *out_status, void *workspace, size_t workspace_bytes, void *stream)
+static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
+                          const double *q0, const double *pressures, double *out_q, double *out_t, int *out_counts,
+                          int *out_status, void *workspace, size_t workspace_bytes, double *record, int record_cap,
+                          void *stream)
 {
   try {
     if (!mech || !rp || !ip || n < 0 || (n > 0 && (!q0 || !out_q || !out_t || !out_counts || !out_status)))
@@ -355,6 +374,8 @@ int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *rp, const s
     p.out_counts = out_counts;
     p.out_status = out_status;
     p.queue = static_cast<unsigned int *>(workspace);
+    p.rec = record;
+    p.rec_cap = record_cap;
     p.per_warp = per_warp_doubles(hm, p.neq, p.prec);
     int dev, smem_max, nsm;
     CUDA_THROW(cudaGetDevice(&dev));
@@ -375,6 +396,27 @@ int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *rp, const s
     set_error(e.what());
     return e.code;
   }
+}
+
+int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
+                       const double *q0, const double *pressures, double *out_q, double *out_t, int *out_counts,
+                       int *out_status, void *workspace, size_t workspace_bytes, void *stream)
+{
+  return integrate_impl(mech, rp, ip, n, q0, pressures, out_q, out_t, out_counts, out_status, workspace,
+                        workspace_bytes, nullptr, 0, stream);
+}
+
+int sf_integrate_record_batch(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
+                              const double *q0, const double *pressures, double *out_q, double *out_t,
+                              int *out_counts, int *out_status, void *workspace, size_t workspace_bytes,
+                              double *trajectory, int capacity_steps, void *stream)
+{
+  if (!trajectory || capacity_steps < 1) {
+    set_error("sf_integrate_record_batch: trajectory buffer and a positive capacity are required");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  return integrate_impl(mech, rp, ip, n, q0, pressures, out_q, out_t, out_counts, out_status, workspace,
+                        workspace_bytes, trajectory, capacity_steps, stream);
 }
 
 }  // extern "C"

@@ -34,10 +34,19 @@ class NewtonSystems:
                                             N.stream_handle()))
         return self
 
-    def solve(self, b, out=None):
+    def solve(self, b, out=None, start=0, count=None):
+        """Solve systems start .. start+count-1 (all by default) for the rows of b ([count, m])."""
+        import ctypes as C
         torch = _torch()
+        count = self.n - start if count is None else count
+        if not (0 <= start and count >= 0 and start + count <= self.n) or b.shape[0] != count:
+            raise ValueError('system range out of bounds or right-hand sides of the wrong count')
         out = torch.empty_like(b) if out is None else out
-        N.check(N.load().sf_newton_solve_batch(self.n, self.m, N.ptr(self.A), N.ptr(self.lu), N.ptr(self.piv),
+        mm = self.m * self.m
+        esz = self.lu.element_size()
+        N.check(N.load().sf_newton_solve_batch(count, self.m, C.c_void_p(self.A.data_ptr() + start * mm * 8),
+                                               C.c_void_p(self.lu.data_ptr() + start * mm * esz),
+                                               C.c_void_p(self.piv.data_ptr() + start * self.m * 4),
                                                self.precision, self.refine, N.ptr(b), N.ptr(out),
                                                N.stream_handle()))
         return out

@@ -209,6 +209,7 @@ def load_cantera_yaml(path, group_name=None):
             raise ValueError(f'unsupported reaction type "{rtype}" in: {rx["equation"]}')
         if orders:
             d['orders'] = orders
+        d['yaml_index'] = len(temp)
         temp.append((key, d))
     reactions = [d for _, d in sorted(temp, key=lambda x: x[0])]
     element_mw_map = {e: ELEMENT_WEIGHTS[e] for e in elements}
@@ -448,6 +449,7 @@ class ChemicalMechanismSpec:
             if sp:
                 tup = tup + (rx['orders'],)
             md['reactions'].append(tup)
+        self._reaction_yaml_index = [rx['yaml_index'] for rx in ext['reactions']]
         self._mech_data = md
         self._species_names = list(ext['species'])
         self._finish_species()
@@ -533,6 +535,7 @@ class ChemicalMechanismSpec:
     def mech_data_json(self):
         md = dict(self._mech_data)
         md['species_order'] = list(self._species_names)
+        md['reaction_yaml_index'] = [int(i) for i in self.reaction_yaml_index]
         md['element_mw_map'] = {k: float(v) for k, v in md['element_mw_map'].items()}
         md['species'] = {s: {'atom_map': v['atom_map'], 'cp': [float(c) if not isinstance(c, (str, list)) else c
                                                                  for c in v['cp']]}
@@ -546,10 +549,14 @@ class ChemicalMechanismSpec:
         with open(path) as f:
             md = json.load(f)
         order = md.pop('species_order')
+        yaml_index = md.pop('reaction_yaml_index', None)
         md['species'] = {s: {'atom_map': md['species'][s]['atom_map'], 'cp': tuple(md['species'][s]['cp'])}
                          for s in order}
         md['reactions'] = [tuple(r) for r in md['reactions']]
-        return cls(mech_data=md)
+        spec = cls(mech_data=md)
+        if yaml_index is not None:
+            spec._reaction_yaml_index = list(yaml_index)
+        return spec
 
     @classmethod
     def bundled(cls, name):
@@ -583,6 +590,14 @@ class ChemicalMechanismSpec:
     @property
     def griffon(self):
         return self._griffon
+
+    @property
+    def reaction_yaml_index(self):
+        """Position in the mechanism file of each reaction, in the internal order (reactions are stably sorted
+        simple, three-body, Lindemann, Troe as the reference does, mechanism.py:540); identity when the mechanism
+        was built from a mech_data dict without file order."""
+        idx = getattr(self, '_reaction_yaml_index', None)
+        return np.array(idx if idx is not None else range(len(self._mech_data['reactions'])), dtype=np.int64)
 
     @property
     def mech_file_path(self):

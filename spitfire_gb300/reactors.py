@@ -18,7 +18,8 @@ import numpy as np
 from . import _native as N
 from ._desc import SfIntegrateParams, reactor_params
 
-STATUS_NAMES = {0: 'running', 1: 'done', 2: 'ignited', 3: 'steady', 4: 'max_steps', 5: 'nan', 6: 'no_ignition'}
+STATUS_NAMES = {0: 'running', 1: 'done', 2: 'ignited', 3: 'steady', 4: 'max_steps', 5: 'nan', 6: 'no_ignition',
+                7: 'record_full'}
 
 
 def _torch():

@@ -8,6 +8,7 @@ There is no public benchmark for this path; states are drawn as follows.
   CH4/air at phi (lean: CO2, H2O, N2, O2 excess; rich: CO2, CO, H2O, H2, N2 with the carbon and hydrogen deficit
   split 1:1 between CO and H2); Newton factor gamma*h = exp(U(ln 1e-9, ln 1e-5)) s.
 * Ignition (config 3): isobaric CH4/air, T0 ~ U(900, 1500) K, phi ~ U(0.5, 2), p = 101325 exp(U(0, ln 20)).
+* Adjoint (config 5): isobaric CH4/air, T0 ~ U(1000, 1400) K, phi ~ U(0.7, 1.5), p = 10 atm, t_end = 5e-3 s.
 * Steady flamelets (config 4): GRI-3.0, oxidizer air 300 K (O2:N2 = 1:3.76 molar), fuel CH4 300 K, 1 atm;
   64 stoichiometric dissipation rates log-spaced 1e-2 - 1e3 1/s (Peters profile); flamelet k has a grid of
   nz_k = 64 + floor(192 k / 63) points clustered at the stoichiometric mixture fraction (intensity 4), the grid
@@ -120,3 +121,8 @@ def slfm_flamelet_setups(mech: ChemicalMechanismSpec, n=64, seed=1004, chi_range
                           stoich_dissipation_rate=float(chis[k]), initial_condition='Burke-Schumann')
         out.append(FlameletSetup(fs))
     return out
+
+
+def adjoint_batch(mech: ChemicalMechanismSpec, n, seed=1005):
+    """Reactors of the adjoint workload: isobaric CH4/air, T0 ~ U(1000, 1400) K, phi ~ U(0.7, 1.5), p = 10 atm."""
+    return ignition_batch(mech, n, seed=seed, T_range=(1000., 1400.), phi_range=(0.7, 1.5), p_log_range=(10., 10.))
