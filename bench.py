@@ -20,6 +20,10 @@ Further blocks of the same line (each measured once after warm-up, inputs reside
              atm) integrated to T0 + 400 K or t = 0.1 s in one persistent launch replayed from a CUDA graph;
              ignitions/s, ignition-delay error against the oracle integrator on a sample, the oracle's rate on the
              host cores
+  adjoint    gradients of the final temperature and a smoothed ignition delay with respect to ln A and E_a of all
+             325 reactions for 2048 isobaric GRI-3.0 reactors (T0 ~ U(1000, 1400) K, phi ~ U(0.7, 1.5), 10 atm,
+             t_end = 5 ms): recorded forward integration plus batched discrete adjoint; gradients/s and peak
+             memory, the oracle's CPU forward sensitivity on a sample
   flamelet   64 steady GRI-3.0 CH4/air flamelets (chi_st log-spaced 1e-2 - 1e3 1/s, grids of 64 - 256 points)
              solved together from Burke-Schumann profiles (batched Newton, then pseudo-transient continuation);
              flamelets/s, per-kernel times and rooflines of one batched launch, the oracle solver on a sample
@@ -46,6 +50,7 @@ METRIC = 'batched ignitions/s at 1e-6 rel τ_ign err; RHS+Jac states/s vs plain 
 N_STATES = 65536
 N_REACTORS = 8192
 N_FLAMELETS = 64
+N_ADJOINT = 2048
 # executed FP64 flops per GRI state of the batched Jacobian kernel (thread-level DADD + DMUL + 2*DFMA counted by
 # ncu, profiles/chem_kernel_jac_gri30_8192.md)
 FP64_FLOPS_PER_STATE = float(os.environ.get('SF_FP64_FLOPS_PER_STATE', '104960'))
@@ -292,9 +297,11 @@ def bench_ignition(spec, rank, stream, cpu):
     from spitfire_gb300 import workloads as W
     from spitfire_gb300.reactors import BatchIntegrator
     d = W.ignition_batch(spec, N_REACTORS, seed=1003 + rank)
+    from spitfire_gb300 import autotune as AT
     bi = BatchIntegrator(spec, 'isobaric')
     kw = dict(delta_temperature_ignition=400., stop_at_time=0.1)
-    bi.run(d['q0'][:256], pressures=d['p'][:256], **kw)
+    # launch shape from the autotuner, on a 1024-reactor sample of the batch (not timed)
+    best, cand = AT.tune_integrator(bi, d['q0'][:1024], pressures=d['p'][:1024], **kw)
     out = bi.run(d['q0'], pressures=d['p'], graph=True, **kw)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -312,7 +319,10 @@ def bench_ignition(spec, rank, stream, cpu):
            'ms': ms, 'graph': 'one persistent launch captured in a CUDA graph, replay timed',
            'status_counts': {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
            'steps': {'min': int(steps.min()), 'median': float(np.median(steps)), 'max': int(steps.max())},
-           'device_status': spec.griffon.device_status()}
+           'device_status': spec.griffon.device_status(),
+           'autotune': {'chosen': {'scratch': 'global' if best[0] else 'shared', 'warps_per_block': best[1]},
+                        'candidates_ms_1024_reactors': {f'{"global" if k[0] else "shared"}/{k[1]}w': v
+                                                        for k, v in cand.items()}}}
     # FP32-LU + FP64-refinement integrator on the first 512 reactors against the FP64 run
     o32 = BatchIntegrator(spec, 'isobaric', linear_precision=1, refine_sweeps=2).run(
         d['q0'][:512], pressures=d['p'][:512], **kw)
@@ -420,6 +430,75 @@ def bench_flamelet(spec, rank, stream, cpu):
     return res
 
 
+def _fwd_sens_sample(args):
+    """CPU forward sensitivity (oracle) over the first `nsteps` recorded steps of one reactor; returns seconds."""
+    q0, p, dts, nsteps = args
+    import oracle as orc
+    import integrate as I
+    import sensitivity as SE
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    orc.set_threads(1)
+    spec = ChemicalMechanismSpec.bundled('methane-gri30')
+    og = orc.OracleGriffon()
+    spec._populate_griffon(og)
+    prob = I.ReactorProblem(og, 'isobaric', pressure=p)
+    dts = dts[:nsteps]
+    fs, st = SE.frozen_integrate(prob, q0, dts)
+    pj = SE.ParamJacobian(spec, og, 'isobaric', p)
+    t0 = time.perf_counter()
+    SE.forward_sensitivity(prob, pj, q0, dts, st)
+    return time.perf_counter() - t0
+
+
+def bench_adjoint(spec, rank, stream, cpu):
+    import numpy as np
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.adjoint import ReactorAdjoint
+    d = W.adjoint_batch(spec, N_ADJOINT, seed=1005 + rank)
+    adj = ReactorAdjoint(spec, 'isobaric')
+    tr = adj.forward(d['q0'][:32], d['p'][:32], 5.e-3)
+    adj.backward(tr)
+    del tr
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    t0 = time.perf_counter()
+    tr = adj.forward(d['q0'], d['p'], 5.e-3)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    g = adj.backward(tr)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    peak = torch.cuda.max_memory_allocated()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    total = max_over_ranks(t2 - t0)
+    steps = tr.steps.cpu().numpy()
+    theta = g['theta']
+    res = {'reactors': N_ADJOINT, 'parameters': int(theta.shape[2] * 2), 'outputs': ['T_end', 'tau_s'],
+           'value': world * N_ADJOINT / total, 'unit': 'reactor gradients/s (650 parameters x 2 outputs)',
+           'forward_s': t1 - t0, 'backward_s': t2 - t1, 'peak_memory_gb': peak / 1e9,
+           'steps': {'min': int(steps.min()), 'median': float(np.median(steps)), 'max': int(steps.max())},
+           'finite': bool(torch.isfinite(theta).all().item()), 'device_status': spec.griffon.device_status(),
+           'central_fd_equivalent': '1300 integrations per reactor gradient'}
+    if cpu:
+        import multiprocessing as mp
+        nsample, nst = min(16, os.cpu_count()), 12
+        rec = tr.rec.cpu().numpy()
+        jobs = [(d['q0'][i], d['p'][i], rec[i, :steps[i], 1], nst) for i in range(nsample)]
+        ctx = mp.get_context('spawn')
+        with ctx.Pool(nsample, initializer=_worker_init, initargs=(ROOT,)) as pool:
+            t0 = time.perf_counter()
+            secs = pool.map(_fwd_sens_sample, jobs)
+            wall = time.perf_counter() - t0
+        per_reactor = [secs[i] / min(nst, steps[i]) * steps[i] for i in range(nsample)]
+        res['cpu_baseline'] = {'value': nsample / sum(per_reactor) * nsample, 'unit': 'reactor gradients/s',
+                               'cores': nsample, 'kind': 'port',
+                               'sample': f'oracle forward sensitivity (650 parameters, both outputs) over the first '
+                                         f'{nst} recorded steps of {nsample} reactors, one per core ({wall:.1f} s), '
+                                         f'scaled to each reactor\'s step count'}
+    return res
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle C++ restatement of Griffon on the host cores (the reference's own code path
     cannot run on the GPU machine: it is not present there)."""
@@ -495,6 +574,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
+
+    # lanes per state of the Jacobian kernel from the autotuner, on 8192 of the states (not timed)
+    from spitfire_gb300 import autotune as AT
+    tuned = AT.tune_chemistry(spec, qh[:8192], kinds=('jac',))
 
     def step():
         g.reactor_jac_batch(P, q, 0, out_rhs=rhs, out_jac=J)
@@ -588,6 +671,7 @@ def main():
     cpu = rank == 0 and world == 1 and not args.no_cpu
     ignition = bench_ignition(spec, rank, stream, cpu)
     flamelet = bench_flamelet(spec, rank, stream, cpu)
+    adjoint = bench_adjoint(spec, rank, stream, cpu)
 
     line = {'metric': METRIC, 'value': value, 'unit': 'states/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
@@ -597,9 +681,11 @@ def main():
                        'states_per_gpu': N_STATES, 'parallelism': f'replicas x{world}',
                        'l2': 'flushed between steps (256 MB write outside the timed events)'},
             'e2e': e2e, 'roofline': roof, 'clocks': clk.summary(), 'gpu_launches': args.steps,
+            'autotune': {'group_jac': tuned['group_jac'][0],
+                         'candidates_ms_8192_states': tuned['group_jac'][1]},
             'plain_gpu_form': {'value': N_STATES / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
                                'speedup_batched_over_plain': plain_ms / ms},
-            'newton': newton, 'ignition': ignition, 'flamelet': flamelet}
+            'newton': newton, 'ignition': ignition, 'flamelet': flamelet, 'adjoint': adjoint}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(spec, qh)
     if rank == 0:

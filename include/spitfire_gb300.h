@@ -118,6 +118,24 @@ int sf_device_status(const sf_mech *mech, int clear);
  * (Jacobian rows that need the dense term), special-order. Any output pointer may be NULL. */
 int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *counts6);
 
+/* Launch shapes of the kernels that use a mechanism, as chosen by an autotuner (spitfire_gb300/autotune.py times
+ * the candidates on the device). 0 restores the built-in choice. Knobs and values:
+ *   SF_TUNE_GROUP_{RATES,SENS,RHS,JAC}: lanes per state of the batched kernels, 8, 16 or 32;
+ *   SF_TUNE_INTEGRATE_WARPS: warps (reactors) per block of sf_integrate_batch, 1..8 (0: as many as fit);
+ *   SF_TUNE_INTEGRATE_SCRATCH: 1 keeps each integrating warp's Griffon scratch in global memory (L2-resident)
+ *     instead of shared memory, so that more warps fit per SM (0: shared memory).
+ * The integrator knobs do not change results; the lane-group width changes the order of per-species sums, so those
+ * results agree to rounding. No reference counterpart. */
+enum sf_tune_knob {
+  SF_TUNE_GROUP_RATES = 0, SF_TUNE_GROUP_SENS = 1, SF_TUNE_GROUP_RHS = 2, SF_TUNE_GROUP_JAC = 3,
+  SF_TUNE_INTEGRATE_WARPS = 4, SF_TUNE_INTEGRATE_SCRATCH = 5, SF_TUNE_KNOBS = 6
+};
+int sf_mech_set_tuning(sf_mech *mech, int knob, int value);
+int sf_mech_get_tuning(const sf_mech *mech, int knob, int *value);
+/* Per-state scratch of the kernels (doubles: right-hand side only, and with the Jacobian) and the size of the
+ * mechanism blob staged into shared memory; any output pointer may be NULL. */
+int sf_mech_layout(const sf_mech *mech, int *scratch_rhs_doubles, int *scratch_total_doubles, long long *blob_bytes);
+
 /* ------------------------------------------------------------------------------------------- thermodynamics */
 /* what: 0 cp_mix[n], 1 cv_mix[n], 2 enthalpy_mix[n], 3 energy_mix[n], 4 species_cp[n][ns], 5 species_cv[n][ns],
  *       6 species_enthalpies[n][ns], 7 species_energies[n][ns], 8 mixture_molecular_weight[n],

@@ -28,6 +28,9 @@ def _declare(L):
     L.sf_mech_create.argtypes = [C.POINTER(SfMechDesc), C.POINTER(_vp)]
     L.sf_mech_destroy.argtypes = [_vp]
     L.sf_mech_info.argtypes = [_vp, C.POINTER(_ip), C.POINTER(_ip), C.POINTER(_ip)]
+    L.sf_mech_set_tuning.argtypes = [_vp, _ip, _ip]
+    L.sf_mech_get_tuning.argtypes = [_vp, _ip, C.POINTER(_ip)]
+    L.sf_mech_layout.argtypes = [_vp, C.POINTER(_ip), C.POINTER(_ip), C.POINTER(C.c_longlong)]
     L.sf_device_status.argtypes = [_vp, _ip]
     L.sf_thermo_batch.argtypes = [_vp, _ip, _ip, _vp, _vp, _vp, _vp]
     L.sf_production_rates_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _vp, _vp]
@@ -70,7 +73,8 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',
             'sf_btddod_scale_and_add_diagonal_batch', 'sf_fp64_peak_probe', 'sf_integrate_record_batch',
-            'sf_rate_param_adjoint_batch']
+            'sf_rate_param_adjoint_batch', 'sf_mech_set_tuning', 'sf_mech_get_tuning',
+            'sf_mech_layout']
 
 
 def load(path=None):

@@ -219,10 +219,11 @@ int guard(F f)
     return SF_ERR_INVALID_ARGUMENT;
   }
 }
-int group_override()
+// lanes per state for a kernel family: the autotuned value if one was set, else the built-in rule
+int group_of(const HostMech &hm, int knob)
 {
-  const char *e = getenv("SF_GROUP_LANES");
-  return e ? atoi(e) : 0;
+  const int g = hm.tune[knob];
+  return (g == 8 || g == 16 || g == 32) ? g : 0;
 }
 }  // namespace
 
@@ -231,6 +232,46 @@ void sfgb::set_error(const std::string &msg) { t_err = msg; }
 extern "C" {
 
 const char *sf_last_error(void) { return t_err.c_str(); }
+
+int sf_mech_set_tuning(sf_mech *mech, int knob, int value)
+{
+  if (!mech || knob < 0 || knob >= SF_TUNE_KNOBS) {
+    t_err = "sf_mech_set_tuning: bad argument";
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  const bool ok = (knob <= SF_TUNE_GROUP_JAC) ? (value == 0 || value == 8 || value == 16 || value == 32)
+                  : (knob == SF_TUNE_INTEGRATE_WARPS) ? (value >= 0 && value <= 8)
+                  : (value == 0 || value == 1);
+  if (!ok) {
+    t_err = "sf_mech_set_tuning: value out of range for this knob";
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  mech->m.tune[knob] = value;
+  return SF_OK;
+}
+
+int sf_mech_layout(const sf_mech *mech, int *scratch_rhs_doubles, int *scratch_total_doubles,
+                   long long *blob_bytes)
+{
+  if (!mech) {
+    t_err = "sf_mech_layout: null mechanism";
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  if (scratch_rhs_doubles) *scratch_rhs_doubles = mech->m.sl.total_rhs;
+  if (scratch_total_doubles) *scratch_total_doubles = mech->m.sl.total;
+  if (blob_bytes) *blob_bytes = (long long)mech->m.dm.blob_bytes;
+  return SF_OK;
+}
+
+int sf_mech_get_tuning(const sf_mech *mech, int knob, int *value)
+{
+  if (!mech || !value || knob < 0 || knob >= SF_TUNE_KNOBS) {
+    t_err = "sf_mech_get_tuning: bad argument";
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  *value = mech->m.tune[knob];
+  return SF_OK;
+}
 const char *sf_version(void) { return "spitfire_gb300 0.1 (sm_103a)"; }
 
 int sf_mech_create(const sf_mech_desc *desc, sf_mech **out)
@@ -288,7 +329,8 @@ int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const
     p.Y = Y;
     p.out_w = out_w;
     p.configuration = 0;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RATES, p, (cudaStream_t)stream, group_override());
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RATES, p, (cudaStream_t)stream,
+                       group_of(mech->m, SF_TUNE_GROUP_RATES));
   });
 }
 
@@ -307,7 +349,8 @@ int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const dou
     p.option = option;
     p.out_w = out_w;
     p.out_S = out_sens;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_SENS, p, (cudaStream_t)stream, group_override());
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_SENS, p, (cudaStream_t)stream,
+                       group_of(mech->m, SF_TUNE_GROUP_SENS));
   });
 }
 
@@ -338,7 +381,8 @@ int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *rp, int n
     p.q = q;
     p.pressures = pressures;
     p.out_rhs = out_rhs;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RHS, p, (cudaStream_t)stream, group_override());
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RHS, p, (cudaStream_t)stream,
+                       group_of(mech->m, SF_TUNE_GROUP_RHS));
   });
 }
 
@@ -356,7 +400,8 @@ int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int r
     p.option = rates_option;
     p.out_rhs = out_rhs;
     p.out_J = out_jac;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_JAC, p, (cudaStream_t)stream, group_override());
+    return chem_launch(const_cast<HostMech &>(mech->m), MODE_JAC, p, (cudaStream_t)stream,
+                       group_of(mech->m, SF_TUNE_GROUP_JAC));
   });
 }
 

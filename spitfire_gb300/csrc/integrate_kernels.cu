@@ -52,6 +52,8 @@ struct IntParams {
   size_t per_warp;  // doubles of shared memory per warp
   double *rec;      // optional trajectory record: [n][rec_cap][2 + 6 neq] = (t_n, dt_n, stage values Y_1..Y_6)
   int rec_cap;
+  double *gscratch; // if set: Griffon scratch of every resident warp in global memory ([grid * warps][L.total])
+  int warps;
 };
 
 // Writes A = pref * J - I straight from the Jacobian evaluation.
@@ -93,8 +95,9 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   double *prior = f + neq;                                // sum_j a_sj k_j
   double *x = prior + neq;                                // linear-solve work vector
   double *k = x + neq;                                    // 6 stage derivatives
-  double *scr = k + 6 * neq;                              // Griffon scratch
-  double *after = scr + L.total;
+  // Griffon scratch: in shared memory, or in this warp's slot of the global scratch array (L2-resident)
+  double *scr = p.gscratch ? p.gscratch + ((size_t)blockIdx.x * p.warps + warp) * L.total : k + 6 * neq;
+  double *after = p.gscratch ? k + 6 * neq : scr + L.total;
   float *LU32 = reinterpret_cast<float *>(after);         // FP32 factors (precision 1)
   float *xf = reinterpret_cast<float *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 : 0));  // 2*neq floats
   int *piv = reinterpret_cast<int *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 + neq : 0));
@@ -303,10 +306,37 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   }
 }
 
-size_t per_warp_doubles(const HostMech &hm, int neq, int prec)
+size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scratch)
 {
-  return (size_t)neq * neq + 12 * (size_t)neq + hm.sl.total +
+  return (size_t)neq * neq + 12 * (size_t)neq + (global_scratch ? 0 : hm.sl.total) +
          (prec == 1 ? ((size_t)neq * neq + 1) / 2 + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2;
+}
+
+struct IntShape {
+  int warps, grid;
+  size_t per_warp, smem, scratch_bytes;
+};
+
+// Warps per block and grid of the persistent launch (autotuned knobs, else as many warps as fit)
+IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n)
+{
+  int dev, smem_max, nsm;
+  CUDA_THROW(cudaGetDevice(&dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  IntShape s{};
+  const bool gs = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] == 1;
+  s.per_warp = per_warp_doubles(hm, neq, prec, gs);
+  const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
+  int fit = (int)std::min<size_t>(8, avail / (s.per_warp * 8));
+  if (fit < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory integrator");
+  const int want = hm.tune[SF_TUNE_INTEGRATE_WARPS];
+  s.warps = (want > 0 && want < fit) ? want : fit;
+  s.smem = hm.dm.blob_bytes + (size_t)s.warps * s.per_warp * 8;
+  const int per_sm = std::max(1, (int)((size_t)smem_max / s.smem));
+  s.grid = (int)std::max<long long>(1, std::min<long long>((long long)nsm * per_sm, ((long long)n + s.warps - 1) / s.warps));
+  s.scratch_bytes = gs ? (size_t)nsm * per_sm * s.warps * hm.sl.total * 8 : 0;
+  return s;
 }
 
 }  // namespace
@@ -318,10 +348,16 @@ extern "C" {
 
 size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n)
 {
-  (void)mech;
-  (void)params;
-  (void)n;
-  return 256;
+  if (!mech || !params) return 256;
+  try {
+    const HostMech &hm = mech->m;
+    const int neq = params->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
+    // both linear precisions: the larger of the two scratch needs
+    const IntShape a = integrate_shape(hm, neq, 0, n < 1 ? 1 : n), b = integrate_shape(hm, neq, 1, n < 1 ? 1 : n);
+    return 256 + std::max(a.scratch_bytes, b.scratch_bytes);
+  } catch (...) {
+    return 256;
+  }
 }
 
 static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, const sf_integrate_params *ip, int n,
@@ -340,7 +376,7 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     if (ip->max_nonlinear_iter < 1 || ip->maximum_steps_per_jacobian < 1 || ip->max_attempts < 1 ||
         !(ip->first_time_step > 0.))
       throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad integration controls");
-    if (!workspace || workspace_bytes < 256) throw sf_error(SF_ERR_WORKSPACE, "workspace of 256 bytes required");
+    if (!workspace || workspace_bytes < 256) throw sf_error(SF_ERR_WORKSPACE, "workspace too small");
     if (mech->m.dm.ns + 1 > 128) throw sf_error(SF_ERR_UNSUPPORTED, "the integrator supports up to 127 species");
     if (n == 0) return SF_OK;
     HostMech &hm = const_cast<HostMech &>(mech->m);
@@ -376,20 +412,16 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.queue = static_cast<unsigned int *>(workspace);
     p.rec = record;
     p.rec_cap = record_cap;
-    p.per_warp = per_warp_doubles(hm, p.neq, p.prec);
-    int dev, smem_max, nsm;
-    CUDA_THROW(cudaGetDevice(&dev));
-    CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
-    const int warps = (int)std::min<size_t>(8, avail / (p.per_warp * 8));
-    if (warps < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory integrator");
-    const size_t smem = hm.dm.blob_bytes + (size_t)warps * p.per_warp * 8;
-    CUDA_THROW(cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const IntShape sh = integrate_shape(hm, p.neq, p.prec, n);
+    if (workspace_bytes < 256 + sh.scratch_bytes)
+      throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_integrate_workspace_size reports");
+    p.per_warp = sh.per_warp;
+    p.warps = sh.warps;
+    p.gscratch = sh.scratch_bytes ? reinterpret_cast<double *>(static_cast<char *>(workspace) + 256) : nullptr;
+    CUDA_THROW(cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_THROW(cudaMemsetAsync(workspace, 0, 256, st));
-    const int grid = (int)std::min<long long>((long long)nsm, ((long long)n + warps - 1) / warps);
-    integrate_kernel<<<grid, 32 * warps, smem, st>>>(p);
+    integrate_kernel<<<sh.grid, 32 * sh.warps, sh.smem, st>>>(p);
     CUDA_THROW(cudaGetLastError());
     return SF_OK;
   } catch (sf_error &e) {

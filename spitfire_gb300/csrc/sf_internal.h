@@ -45,6 +45,7 @@ struct HostMech {
   void *d_blob = nullptr;
   int *d_status = nullptr;  // device error word of kernels using this mechanism
   int device = 0;
+  int tune[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // launch shapes chosen by the autotuner (sf_tune_knob), 0 = default
 
   struct Programs {
     DevProgram progs[4]{};  // 0: w only, 1: w/S_rho/S_T/P/Q, 2: Y block + T row, 3: all species rows (sens)

@@ -12,6 +12,8 @@ the current CUDA device at the first evaluation (``sf_mech_create``). Two kinds 
 There is no CPU fallback: without the native library or a CUDA device these methods raise.
 """
 
+import ctypes as C
+
 import numpy as np
 
 from . import _native as N
@@ -79,6 +81,12 @@ class PyCombustionKernels(GriffonSetters):
     @property
     def n_reactions(self):
         return len(self._rec.reactions)
+
+    def scratch_layout(self):
+        """{'rhs': doubles, 'total': doubles, 'blob_bytes': bytes} of the kernels' per-state scratch and blob."""
+        a, b, c = C.c_int(), C.c_int(), C.c_longlong()
+        N.check(N.load().sf_mech_layout(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return {'rhs': a.value, 'total': b.value, 'blob_bytes': c.value}
 
     def device_status(self, clear=True):
         return N.load().sf_device_status(self.handle, int(clear))

@@ -72,7 +72,10 @@ class BatchIntegrator:
                     t=torch.empty(n, dtype=torch.float64, device=dev),
                     counts=torch.empty((n, 4), dtype=torch.int32, device=dev),
                     status=torch.empty(n, dtype=torch.int32, device=dev),
-                    ws=torch.empty(64, dtype=torch.int32, device=dev))
+                    ws=torch.empty(self.workspace_bytes(n) // 4 + 1, dtype=torch.int32, device=dev))
+
+    def workspace_bytes(self, n):
+        return int(N.load().sf_integrate_workspace_size(self.g.handle, C.byref(self.params), int(n)))
 
     def launch(self, q0, pressures, out, ip):
         L = N.load()

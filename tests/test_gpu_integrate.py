@@ -105,3 +105,29 @@ def test_graph_replay_and_drop_in_reactor(cuda):
     torch.cuda.synchronize()
     assert torch.equal(t1, bi._graph[3]['t'])
     assert abs(float(t1[0]) - c['tau']) / c['tau'] <= 1e-6
+
+
+def test_autotuned_shapes_do_not_change_results(cuda):
+    """The autotuner's candidates (lanes per state of the Jacobian kernel; integrator scratch placement and warps
+    per block) give bit-identical results (the tuner itself checks this), and the chosen shapes are applied."""
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec, og = pair('methane-gri30')
+    d = W.gri_states(spec, 2048, seed=31)
+    res = AT.tune_chemistry(spec, W.isochoric_state(d), kinds=('rhs', 'jac'))
+    assert AT.get_tuning(spec, 'group_jac') == res['group_jac'][0]
+    b = W.ignition_batch(spec, 256, seed=32, T_range=(1200., 1500.))
+    bi = BatchIntegrator(spec, 'isobaric')
+    best, times = AT.tune_integrator(bi, b['q0'], pressures=b['p'], delta_temperature_ignition=400.,
+                                     stop_at_time=0.1)
+    assert (AT.get_tuning(spec, 'integrate_scratch'), AT.get_tuning(spec, 'integrate_warps')) == best
+    assert len(times) >= 2
+    out = bi.run(b['q0'], pressures=b['p'], delta_temperature_ignition=400., stop_at_time=0.1)
+    import integrate as I
+    for i in range(0, 256, 64):
+        r = I.integrate(I.ReactorProblem(og, 'isobaric', pressure=b['p'][i]), b['q0'][i],
+                        delta_temperature_ignition=400., stop_at_time=0.1)
+        assert abs(out['t'][i].item() - r['t']) / r['t'] <= 1e-6
+    for k in AT.KNOBS:
+        AT.set_tuning(spec, k, 0)
