@@ -54,6 +54,8 @@ N_ADJOINT = 2048
 # executed FP64 flops per GRI state of the batched Jacobian kernel (thread-level DADD + DMUL + 2*DFMA counted by
 # ncu, profiles/chem_kernel_jac_gri30_8192.md)
 FP64_FLOPS_PER_STATE = float(os.environ.get('SF_FP64_FLOPS_PER_STATE', '104960'))
+# warp-level FP64 instructions per GRI state of the same kernel (ncu smsp__inst_executed_pipe_fp64.sum / states)
+FP64_WARP_INSTR_PER_STATE = 4301.
 
 
 def griffon_dense_flops(spec):
@@ -658,6 +660,13 @@ def main():
         roof['achieved'] = None
         roof['frac'] = None
     roof['traffic'] = None
+    issue = C.c_double()
+    N.check(N.load().sf_fp64_issue_probe(4000, 32, C.byref(issue), N.ptr(sink), N.stream_handle()))
+    ach_issue = FP64_WARP_INSTR_PER_STATE * N_STATES / (ms * 1e-3)
+    roof['fp64_issue'] = {'unit': 'warp FP64 instructions/s', 'per_state': FP64_WARP_INSTR_PER_STATE,
+                          'achieved': ach_issue, 'peak': issue.value, 'frac': ach_issue / issue.value,
+                          'note': 'GB300 charges FP64 per warp instruction whatever the active lanes; this is '
+                                  'the pipe-occupancy roofline, the TFLOP/s one above counts useful lanes'}
     roof['griffon_dense_flops_per_state'] = dense
     roof['griffon_dense_equiv_tflops'] = dense * N_STATES / (ms * 1e-3) / 1e12
     hbm_bytes = N_STATES * (neq + neq + neq * neq) * 8

@@ -366,6 +366,10 @@ int sf_btddod_scale_and_add_diagonal_batch(int n_flamelets, int ns, const int *o
  * timed with CUDA events; synchronizes the stream. sink: DEVICE pointer to one double. No reference counterpart:
  * it gives the FP64 roofline denominator of the benchmark. */
 int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream);
+/* The same FMA chains with only `active_lanes` (1..32) lanes of every warp working: warp-level FP64 instructions
+ * issued per second. Equal rates for every lane count mean FP64 work is charged per warp instruction, whatever the
+ * number of active lanes. */
+int sf_fp64_issue_probe(int iters, int active_lanes, double *out_warp_instr_per_s, double *sink, void *stream);
 
 #ifdef __cplusplus
 }

@@ -60,6 +60,7 @@ def _declare(L):
     L.sf_btddod_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_btddod_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_fp64_peak_probe.argtypes = [_ip, C.POINTER(C.c_double), _vp, _vp]
+    L.sf_fp64_issue_probe.argtypes = [_ip, _ip, C.POINTER(C.c_double), _vp, _vp]
     L.sf_btddod_scale_and_add_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                                          C.c_double, _vp, _vp]
 
@@ -74,7 +75,7 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',
             'sf_btddod_scale_and_add_diagonal_batch', 'sf_fp64_peak_probe', 'sf_integrate_record_batch',
             'sf_rate_param_adjoint_batch', 'sf_mech_set_tuning', 'sf_mech_get_tuning',
-            'sf_mech_layout']
+            'sf_mech_layout', 'sf_fp64_issue_probe']
 
 
 def load(path=None):

@@ -221,16 +221,17 @@ int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const i
 // the measured-peaks file of this machine has HBM and bf16 figures only.
 namespace sfgb {
 namespace {
-__global__ void fp64_probe_kernel(int iters, double seed, double *sink)
+__global__ void fp64_probe_kernel(int iters, double seed, double *sink, int active_lanes)
 {
   double a[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) a[k] = seed + k * 1e-3 + threadIdx.x * 1e-7;
   const double b = 0.999999999, c = 1e-9;
-  for (int i = 0; i < iters; ++i) {
+  if ((int)(threadIdx.x & 31) < active_lanes)
+    for (int i = 0; i < iters; ++i) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
-  }
+      for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
   double s = 0.;
 #pragma unroll
   for (int k = 0; k < 8; ++k) s += a[k];
@@ -239,27 +240,25 @@ __global__ void fp64_probe_kernel(int iters, double seed, double *sink)
 }  // namespace
 }  // namespace sfgb
 
-extern "C" int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream)
+namespace {
+// Elapsed milliseconds of one probe launch (8 blocks per SM, 256 threads, `active_lanes` lanes of every warp
+// running 8 independent FMA chains of `iters` steps), after a short warm-up launch.
+int probe_ms(int iters, int active_lanes, double *sink, cudaStream_t st, float *ms, int *blocks, int *threads)
 {
-  if (!out_tflops || !sink || iters < 1) {
-    set_error("sf_fp64_peak_probe: bad argument");
-    return SF_ERR_INVALID_ARGUMENT;
-  }
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaStream_t st = (cudaStream_t)stream;
-  const int blocks = nsm * 8, threads = 256;
-  fp64_probe_kernel<<<blocks, threads, 0, st>>>(16, 1.0, sink);
+  *blocks = nsm * 8;
+  *threads = 256;
+  sfgb::fp64_probe_kernel<<<*blocks, *threads, 0, st>>>(16, 1.0, sink, 32);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, st);
-  fp64_probe_kernel<<<blocks, threads, 0, st>>>(iters, 1.0, sink);
+  sfgb::fp64_probe_kernel<<<*blocks, *threads, 0, st>>>(iters, 1.0, sink, active_lanes);
   cudaEventRecord(e1, st);
   cudaEventSynchronize(e1);
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventElapsedTime(ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   const cudaError_t e = cudaGetLastError();
@@ -267,7 +266,37 @@ extern "C" int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, v
     set_error(cudaGetErrorString(e));
     return SF_ERR_CUDA;
   }
+  return SF_OK;
+}
+}  // namespace
+
+extern "C" int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream)
+{
+  if (!out_tflops || !sink || iters < 1) {
+    set_error("sf_fp64_peak_probe: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  float ms = 0.f;
+  int blocks, threads;
+  const int rc = probe_ms(iters, 32, sink, (cudaStream_t)stream, &ms, &blocks, &threads);
+  if (rc) return rc;
   const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
   *out_tflops = flops / (ms * 1e-3) / 1e12;
+  return SF_OK;
+}
+
+extern "C" int sf_fp64_issue_probe(int iters, int active_lanes, double *out_warp_instr_per_s, double *sink,
+                                   void *stream)
+{
+  if (!out_warp_instr_per_s || !sink || iters < 1 || active_lanes < 1 || active_lanes > 32) {
+    set_error("sf_fp64_issue_probe: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  float ms = 0.f;
+  int blocks, threads;
+  const int rc = probe_ms(iters, active_lanes, sink, (cudaStream_t)stream, &ms, &blocks, &threads);
+  if (rc) return rc;
+  const double warp_instr = 8.0 * (double)iters * blocks * (threads / 32);
+  *out_warp_instr_per_s = warp_instr / (ms * 1e-3);
   return SF_OK;
 }

@@ -1,0 +1,106 @@
+"""Small, self-contained runs of each kernel family for profiling (``ncu``) and quick checks.
+
+    python -m spitfire_gb300.profile_cases <case>
+
+Cases (GRI-3.0 unless stated; each ends by checking the device error word):
+  jac        isochoric RHS + Jacobian of 8192 states (chem_kernel MODE_JAC), 3 launches
+  integrate  256 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s (integrate_kernel)
+  flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
+             block-Thomas factorization, solve and matvec
+  adjoint    64 reactors of the adjoint distribution recorded to 1 ms, then the batched adjoint
+  fp64issue  warp-level FP64 FMA instructions per second with 1, 2, 4, 8, 16 and 32 active lanes per warp
+"""
+
+import sys
+
+import numpy as np
+
+
+def _spec():
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    return ChemicalMechanismSpec.bundled('methane-gri30')
+
+
+def case_jac():
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    q = torch.tensor(W.isochoric_state(W.gri_states(spec, 8192)), device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(3):
+        spec.griffon.reactor_jac_batch(P, q, 0)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_integrate():
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec = _spec()
+    d = W.ignition_batch(spec, 256, seed=1003)
+    BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                          stop_at_time=0.1)
+    return spec
+
+
+def case_flamelet():
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.flamelet import FlameletBatch
+    spec = _spec()
+    setups = W.slfm_flamelet_setups(spec, 8, seed=1004, nz_range=(64, 120))
+    b = FlameletBatch(setups)
+    x = b.initial_state()
+    y = b.rhs(x)
+    b.jacobian(x, eig=True, diffterm_per_flamelet=b.diffterm_tensor())
+    b.factor()
+    b.solve(y)
+    b.matvec(x)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_adjoint():
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.adjoint import ReactorAdjoint
+    spec = _spec()
+    d = W.adjoint_batch(spec, 64, seed=1005)
+    adj = ReactorAdjoint(spec, 'isobaric')
+    tr = adj.forward(d['q0'], pressures=d['p'], t_end=1.e-3)
+    g = adj.backward(tr)
+    assert bool(np.isfinite(g['theta'].cpu().numpy()).all())
+    return spec
+
+
+def case_fp64issue():
+    import ctypes as C
+    import torch
+    from spitfire_gb300 import _native as N
+    sink = torch.zeros(1, dtype=torch.float64, device='cuda')
+    out = C.c_double()
+    for lanes in (1, 2, 4, 8, 16, 32):
+        N.check(N.load().sf_fp64_issue_probe(4000, lanes, C.byref(out), N.ptr(sink), N.stream_handle()))
+        print(f'active lanes {lanes:2d}: {out.value:.4e} warp FP64 FMA instructions/s, '
+              f'{out.value * lanes * 2 / 1e12:.3f} TFLOP/s of useful lanes')
+    return None
+
+
+CASES = {'jac': case_jac, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
+         'fp64issue': case_fp64issue}
+
+
+def main(argv):
+    if len(argv) != 1 or argv[0] not in CASES:
+        print(__doc__)
+        return 2
+    from spitfire_gb300 import build
+    build.build()
+    spec = CASES[argv[0]]()
+    status = spec.griffon.device_status() if spec is not None else 0
+    print(f'{argv[0]}: done, device status {status}')
+    return 0 if status == 0 else 1
+
+
+if __name__ == '__main__':
+    sys.exit(main(sys.argv[1:]))
