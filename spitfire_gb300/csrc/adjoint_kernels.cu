@@ -137,8 +137,9 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
           B += b.d[m.d_netc + j] * (wy - wTc * scr[L.eh + sp]);
         }
         const double g = sr * B * s.invRho;
-        out[2 * r] += g;
-        out[2 * r + 1] += -g * s.invT * m.invRu;
+        const int ro = b.i[m.i_orig + r];  // reported in the order the mechanism was described
+        out[2 * ro] += g;
+        out[2 * ro + 1] += -g * s.invT * m.invRu;
       }
       grp.sync();
     }

@@ -166,6 +166,27 @@ void HostMech::build(const sf_mech_desc *d)
     x.dense = (x.kind != SF_RXN_SIMPLE) || last_involved;
     x.dense_idx = x.dense ? n_dense++ : -1;
   }
+  // Device order: reactions grouped by kind and, within a kind, by their number of Jacobian slots (stable).
+  // Lanes of a state group take reactions in strides of the group width, so the per-reaction slot loop of a
+  // group iteration then runs about as many times for every lane. Per-reaction outputs map back through i_orig.
+  std::vector<int> order(nr);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (rx[a].kind != rx[b].kind) return rx[a].kind < rx[b].kind;
+    return rx[a].slots.size() < rx[b].slots.size();
+  });
+  {
+    std::vector<HRxn> sorted(nr);
+    for (int k = 0; k < nr; ++k) sorted[k] = std::move(rx[order[k]]);
+    rx = std::move(sorted);
+    n_fall = 0;
+    n_dense = 0;
+    for (HRxn &x : rx) {
+      x.fall = x.kind >= SF_RXN_LINDEMANN ? n_fall++ : -1;
+      x.dense_idx = x.dense ? n_dense++ : -1;
+    }
+  }
+  orig_index = order;
   m.n_fall = n_fall;
   m.n_dense = n_dense;
 
@@ -214,6 +235,8 @@ void HostMech::build(const sf_mech_desc *d)
   m.d_one = dsec(1);
   D[m.d_one] = 1.;
   m.i_info = isec(nr);
+  m.i_orig = isec(nr);
+  for (int r = 0; r < nr; ++r) I[m.i_orig + r] = orig_index[r];
   m.i_sums = isec(nr);
   m.i_fall = isec(nr);
   m.i_dense = isec(nr);

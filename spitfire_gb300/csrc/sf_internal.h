@@ -40,7 +40,8 @@ struct HostMech {
   ScratchLayout sl{};
   std::vector<double> host_dbl, mw, invmw;
   std::vector<int> host_int;
-  std::vector<HRxn> rx;
+  std::vector<HRxn> rx;               // device order (see build)
+  std::vector<int> orig_index;        // device reaction -> index in the description
   std::vector<std::vector<int>> net_entry_of, slot_entry_of;
   void *d_blob = nullptr;
   int *d_status = nullptr;  // device error word of kernels using this mechanism

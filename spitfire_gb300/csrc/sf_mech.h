@@ -47,6 +47,7 @@ struct DevMech {
 
   // ---- int section offsets ----
   int i_info;    // [nr]
+  int i_orig;    // [nr] index of each device-order reaction in the order the mechanism was described
   int i_sums;    // [nr] sum_nu (low 16 bits, signed) | sum_reac_nu << 16 (8 bits) | sum_prod_nu << 24
   int i_fall;    // [nr] falloff index or -1
   int i_dense;   // [nr] dense index or -1
