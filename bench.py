@@ -51,11 +51,13 @@ N_STATES = 65536
 N_REACTORS = 8192
 N_FLAMELETS = 64
 N_ADJOINT = 2048
-# executed FP64 flops per GRI state of the batched Jacobian kernel (thread-level DADD + DMUL + 2*DFMA counted by
-# ncu, profiles/chem_kernel_jac_gri30_8192.md)
-FP64_FLOPS_PER_STATE = float(os.environ.get('SF_FP64_FLOPS_PER_STATE', '104960'))
-# warp-level FP64 instructions per GRI state of the same kernel (ncu smsp__inst_executed_pipe_fp64.sum / states)
-FP64_WARP_INSTR_PER_STATE = 4301.
+# Per GRI state of each Jacobian kernel the autotuner can choose, from ncu on the profiling cases
+# (python -m spitfire_gb300.profile_cases jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA) and
+# warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states).
+FP64_PER_STATE = {
+    32: {'kernel': 'chem_kernel<32, MODE_JAC>', 'flops': 105050., 'warp_instr': 4189.},
+    1: {'kernel': 'chem_kernel_tps<MODE_JAC>', 'flops': 96855., 'warp_instr': 2150.},
+}
 
 
 def griffon_dense_flops(spec):
@@ -407,7 +409,8 @@ def bench_flamelet(spec, rank, stream, cpu):
                       'achieved_gbs': rhs_bytes / (k['rhs_ms'] * 1e-3) / 1e9,
                       'points_per_s': pts / (k['rhs_ms'] * 1e-3)},
         'jacobian': {'points_per_s': pts / (k['jacobian_ms'] * 1e-3),
-                     'fp64_tflops_executed_est': FP64_FLOPS_PER_STATE * pts / (k['jacobian_ms'] * 1e-3) / 1e12},
+                     'fp64_tflops_executed_est': FP64_PER_STATE[32]['flops'] * pts / (k['jacobian_ms'] * 1e-3)
+                     / 1e12},
         'factor': {'bound': 'fp64', 'flops_per_point': 2. / 3. * ns ** 3 + 2. * ns ** 3,
                    'achieved_tflops': fac_flops / (k['factor_ms'] * 1e-3) / 1e12}}
     res['kernels'] = k
@@ -577,9 +580,13 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    # lanes per state of the Jacobian kernel from the autotuner, on 8192 of the states (not timed)
+    # lanes per state of the Jacobian kernel from the autotuner, on the whole batch (not timed): a sample smaller than
+    # the resident lanes would leave the thread-per-state kernel's grid mostly idle
     from spitfire_gb300 import autotune as AT
-    tuned = AT.tune_chemistry(spec, qh[:8192], kinds=('jac',))
+    tuned = AT.tune_chemistry(spec, qh, kinds=('jac',))
+    group = tuned['group_jac'][0]
+    kern = FP64_PER_STATE.get(group, {'kernel': f'chem_kernel<{group}, MODE_JAC>', 'flops': None,
+                                      'warp_instr': None})
 
     def step():
         g.reactor_jac_batch(P, q, 0, out_rhs=rhs, out_jac=J)
@@ -647,11 +654,11 @@ def main():
     peak = C.c_double()
     N.check(N.load().sf_fp64_peak_probe(20000, C.byref(peak), N.ptr(sink), N.stream_handle()))
     dense = griffon_dense_flops(spec)
-    algo = FP64_FLOPS_PER_STATE
+    algo = kern['flops']
     roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': peak.value,
             'peak_source': 'measured live by sf_fp64_peak_probe (FP64 FMA chains on every SM); the measured-peaks '
                            'file has no FP64 figure',
-            'kernel': 'chem_kernel<32, MODE_JAC>'}
+            'kernel': kern['kernel']}
     if algo:
         roof['achieved'] = algo * N_STATES / (ms * 1e-3) / 1e12
         roof['frac'] = roof['achieved'] / peak.value
@@ -662,11 +669,12 @@ def main():
     roof['traffic'] = None
     issue = C.c_double()
     N.check(N.load().sf_fp64_issue_probe(4000, 32, C.byref(issue), N.ptr(sink), N.stream_handle()))
-    ach_issue = FP64_WARP_INSTR_PER_STATE * N_STATES / (ms * 1e-3)
-    roof['fp64_issue'] = {'unit': 'warp FP64 instructions/s', 'per_state': FP64_WARP_INSTR_PER_STATE,
-                          'achieved': ach_issue, 'peak': issue.value, 'frac': ach_issue / issue.value,
-                          'note': 'GB300 charges FP64 per warp instruction whatever the active lanes; this is '
-                                  'the pipe-occupancy roofline, the TFLOP/s one above counts useful lanes'}
+    if kern['warp_instr']:
+        ach_issue = kern['warp_instr'] * N_STATES / (ms * 1e-3)
+        roof['fp64_issue'] = {'unit': 'warp FP64 instructions/s', 'per_state': kern['warp_instr'],
+                              'achieved': ach_issue, 'peak': issue.value, 'frac': ach_issue / issue.value,
+                              'note': 'GB300 charges FP64 per warp instruction whatever the active lanes; this is '
+                                      'the pipe-occupancy roofline, the TFLOP/s one above counts useful lanes'}
     roof['griffon_dense_flops_per_state'] = dense
     roof['griffon_dense_equiv_tflops'] = dense * N_STATES / (ms * 1e-3) / 1e12
     hbm_bytes = N_STATES * (neq + neq + neq * neq) * 8
@@ -690,8 +698,8 @@ def main():
                        'states_per_gpu': N_STATES, 'parallelism': f'replicas x{world}',
                        'l2': 'flushed between steps (256 MB write outside the timed events)'},
             'e2e': e2e, 'roofline': roof, 'clocks': clk.summary(), 'gpu_launches': args.steps,
-            'autotune': {'group_jac': tuned['group_jac'][0],
-                         'candidates_ms_8192_states': tuned['group_jac'][1]},
+            'autotune': {'group_jac': group, 'tps_ctas': tuned.get('tps_ctas', (None,))[0],
+                         'candidates_ms': {str(k): v for k, v in tuned['group_jac'][1].items()}},
             'plain_gpu_form': {'value': N_STATES / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
                                'speedup_batched_over_plain': plain_ms / ms},
             'newton': newton, 'ignition': ignition, 'flamelet': flamelet, 'adjoint': adjoint}

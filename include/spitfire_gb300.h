@@ -120,15 +120,19 @@ int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *cou
 
 /* Launch shapes of the kernels that use a mechanism, as chosen by an autotuner (spitfire_gb300/autotune.py times
  * the candidates on the device). 0 restores the built-in choice. Knobs and values:
- *   SF_TUNE_GROUP_{RATES,SENS,RHS,JAC}: lanes per state of the batched kernels, 8, 16 or 32;
+ *   SF_TUNE_GROUP_{RATES,SENS,RHS,JAC}: lanes per state of the batched kernels, 8, 16 or 32, or 1 for the
+ *     thread-per-state kernels (each lane one state, scratch interleaved across the warp in a device buffer the
+ *     mechanism allocates when the knob is set);
  *   SF_TUNE_INTEGRATE_WARPS: warps (reactors) per block of sf_integrate_batch, 1..8 (0: as many as fit);
  *   SF_TUNE_INTEGRATE_SCRATCH: 1 keeps each integrating warp's Griffon scratch in global memory (L2-resident)
- *     instead of shared memory, so that more warps fit per SM (0: shared memory).
+ *     instead of shared memory, so that more warps fit per SM (0: shared memory);
+ *   SF_TUNE_TPS_CTAS: resident 4-warp blocks per SM of the thread-per-state kernels, 1..16 (0: as many as fit);
+ *     fewer keep more of their interleaved scratch in L2.
  * The integrator knobs do not change results; the lane-group width changes the order of per-species sums, so those
  * results agree to rounding. No reference counterpart. */
 enum sf_tune_knob {
   SF_TUNE_GROUP_RATES = 0, SF_TUNE_GROUP_SENS = 1, SF_TUNE_GROUP_RHS = 2, SF_TUNE_GROUP_JAC = 3,
-  SF_TUNE_INTEGRATE_WARPS = 4, SF_TUNE_INTEGRATE_SCRATCH = 5, SF_TUNE_KNOBS = 6
+  SF_TUNE_INTEGRATE_WARPS = 4, SF_TUNE_INTEGRATE_SCRATCH = 5, SF_TUNE_TPS_CTAS = 6, SF_TUNE_KNOBS = 7
 };
 int sf_mech_set_tuning(sf_mech *mech, int knob, int value);
 int sf_mech_get_tuning(const sf_mech *mech, int knob, int *value);

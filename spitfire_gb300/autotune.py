@@ -2,7 +2,8 @@
 
 For one mechanism on the current device it times the candidate shapes on a sample of the caller's workload with
 CUDA events and applies the fastest through ``sf_mech_set_tuning``:
-  * lanes per state (8, 16, 32) of the production-rate, right-hand-side and Jacobian kernels;
+  * lanes per state (8, 16, 32, or 1: the thread-per-state kernels, with their resident blocks per SM) of the
+    production-rate, right-hand-side and Jacobian kernels;
   * for the persistent ESDIRK64 integrator: where each warp keeps its Griffon scratch (shared memory, or an
     L2-resident global slot, which leaves room for more warps per SM) and how many warps (reactors) share a block.
 The knobs change launch shapes only. The integrator's candidates produce bit-identical results; the lane-group
@@ -20,7 +21,7 @@ import numpy as np
 from . import _native as N
 
 KNOBS = {'group_rates': 0, 'group_sens': 1, 'group_rhs': 2, 'group_jac': 3, 'integrate_warps': 4,
-         'integrate_scratch': 5}
+         'integrate_scratch': 5, 'tps_ctas': 6}
 CACHE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_tuning')
 
 
@@ -62,9 +63,12 @@ def _key(mech):
     return f'{h}_{dev}'
 
 
-def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kinds=('rates', 'rhs', 'jac'), reps=3):
+def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kinds=('rates', 'rhs', 'jac'), reps=3,
+                   thread_per_state=True):
     """Choose lanes per state for each kernel family on `states` (a batch of reactor states of the given
-    configuration). Returns {knob: (best value, {value: ms})}."""
+    configuration): 8, 16 or 32, or (with thread_per_state) 1 at a few resident-block counts of the thread-per-state
+    kernels. Returns {knob: (best value, {candidate: ms})}, candidates labelled G or '1/<blocks per SM>', and, when
+    a family chose 1, 'tps_ctas': (blocks per SM, None)."""
     torch = _torch()
     from ._desc import reactor_params
     g = mech.griffon
@@ -83,12 +87,20 @@ def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kind
              'rhs': lambda: g.reactor_rhs_batch(P, q, pressures=pr),
              'jac': lambda: g.reactor_jac_batch(P, q, 0, pressures=pr)}
     out = {}
+    tps_choice = {}
     for kind in kinds:
         knob = 'group_' + kind
         times = {}
         ref = None
-        for G in (8, 16, 32):
-            set_tuning(mech, knob, G)
+        cands = {8: 8, 16: 16, 32: 32}
+        if thread_per_state:
+            cands.update({f'1/{c}': (1, c) for c in (0, 2, 1)})  # label '1/<blocks per SM>' (0: all that fit)
+        for label, cand in cands.items():
+            if isinstance(cand, tuple):
+                set_tuning(mech, 'tps_ctas', cand[1])
+                set_tuning(mech, knob, 1)
+            else:
+                set_tuning(mech, knob, cand)
             res = calls[kind]()
             res = res if isinstance(res, tuple) else (res,)
             if ref is None:
@@ -97,11 +109,24 @@ def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kind
                 for a, b in zip(ref, res):
                     scale = a.abs().amax(dim=-1, keepdim=True).clamp_min(1e-300)
                     if float(((a - b).abs() / scale).max()) > 1e-12:
-                        raise RuntimeError(f'{knob}={G} changed the results beyond rounding')
-            times[G] = _time(calls[kind], reps)
-        best = min(times, key=times.get)
+                        set_tuning(mech, knob, 0)
+                        raise RuntimeError(f'{knob}={label} changed the results beyond rounding')
+            times[label] = _time(calls[kind], reps)
+            del res
+        best = cands[min(times, key=times.get)]
+        if isinstance(best, tuple):
+            tps_choice[kind] = best[1]
+            best = 1
         set_tuning(mech, knob, best)
         out[knob] = (best, times)
+    # one resident-block count serves every thread-per-state family: that of the heaviest family that chose it
+    for kind in ('jac', 'rhs', 'rates'):
+        if kind in tps_choice:
+            set_tuning(mech, 'tps_ctas', tps_choice[kind])
+            out['tps_ctas'] = (tps_choice[kind], None)
+            break
+    else:
+        set_tuning(mech, 'tps_ctas', 0)
     return out
 
 

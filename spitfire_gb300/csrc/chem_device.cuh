@@ -102,6 +102,16 @@ struct Blob {
   const int *i;
 };
 
+// Scratch of one state interleaved with the states of the other 31 lanes of its warp (thread-per-state kernels):
+// element i of this lane's state lives at p[32 i], so the lanes of a warp touch one contiguous 256-byte row.
+// The state-group kernels use a plain double * into their shared-memory area instead; the device code below is
+// written for either.
+struct ScrStrided {
+  double *p;  // base + lane
+  __device__ __forceinline__ double &operator[](int i) const { return p[(size_t)i << 5]; }
+  __device__ __forceinline__ ScrStrided operator+(int o) const { return ScrStrided{p + ((size_t)o << 5)}; }
+};
+
 __device__ __forceinline__ Blob blob_at(const DevMech &m, const void *base)
 {
   Blob b;
@@ -177,7 +187,8 @@ struct StateCtx {
 
 // Product of C_j^nu_j over a reactant/product list, with the factor of list position `at` differentiated
 // with respect to Y of that species (nu * rho/M * C^(nu-1)); at < 0: no differentiation.
-__device__ __forceinline__ double mass_action(const int *lst, int n, const double *C, const double *invmw_d,
+template <class SC>
+__device__ __forceinline__ double mass_action(const int *lst, int n, const SC &C, const double *invmw_d,
                                               double rho, int at)
 {
   double v = 1.;
@@ -195,7 +206,8 @@ __device__ __forceinline__ double mass_action(const int *lst, int n, const doubl
 
 // Special-order rate law (chemistry_kernels.cpp:316-325) and its Y derivative for order-list position `at`
 // (rates_sensitivities_exact.cpp:177-261).
-__device__ __forceinline__ double special_orders(const DevMech &m, Blob b, int r, const double *C, double rho, int at,
+template <class SC>
+__device__ __forceinline__ double special_orders(const DevMech &m, Blob b, int r, const SC &C, double rho, int at,
                                                  bool last_closure)
 {
   const int o0 = b.i[m.i_ord_off + r], o1 = b.i[m.i_ord_off + r + 1];
@@ -228,8 +240,8 @@ struct RxnOut {
 
 // Evaluate reaction r. Always writes q[r]; with JAC also dq/drho, dq/dT, the sparse slot derivatives D (scaled by
 // 1/rho), the dense coefficients alpha, beta (scaled by 1/rho) and E_r = sum_i c_ir * eh_i.
-template <bool JAC>
-__device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const ScratchLayout &L, double *scr,
+template <bool JAC, class S>
+__device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const ScratchLayout &L, S scr,
                                               const StateCtx &s, int r, double *Eacc_a, double *Eacc_b)
 {
   const int info = b.i[m.i_info + r];
@@ -238,8 +250,8 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
   const bool rev = (info >> RI_REV_BIT) & 1;
   const bool has_ord = (info >> RI_ORD_BIT) & 1;
   const double *kc = b.d + m.d_kf + 3 * r;
-  const double *C = scr + L.C;
-  const double *y = scr + L.y;
+  const auto C = scr + L.C;
+  const auto y = scr + L.y;
   const double *invmw_d = b.d + m.d_invmw;
   // forward rate constant (chemistry_kernels.cpp:140-157)
   double kf;
@@ -437,29 +449,64 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
 // ------------------------------------------------------------------------------------------ gather programs
 // Execute a gather program for one state: every lane runs prog.len items (see sf_mech.h). Destination kinds:
 // DST_SCRATCH / DST_TROW write scratch[index]; DST_JBLOCK calls jw(row, col, value).
-template <int G, class JW>
-__device__ __forceinline__ void run_program(const DevProgram &prog, int lane, const double *blobd, double *scr,
+// Items are processed in batches of U (each lane's item count is padded to a multiple of GATHER_UNROLL): the
+// operands of a whole batch are loaded before its FMAs, and the next batch's items while they run. This is sound
+// because no program reads a scratch location that it writes (checked when the program is built), so no load
+// can overtake a store it depends on.
+
+// One lane per state reads its scratch from global memory and gains most from loads in flight; the lane groups
+// (scratch in shared memory or L2) take half the batch, which keeps their larger kernels free of register spills.
+__host__ __device__ constexpr int default_unroll(int G) { return G == 1 ? GATHER_UNROLL : GATHER_UNROLL / 2; }
+
+template <class S>
+__device__ __forceinline__ double gather_operand(uint32_t ref, const double *blobd, const S &scr)
+{
+  return (ref & REF_SCRATCH) ? scr[ref & ~REF_SCRATCH] : blobd[ref];
+}
+
+template <int G, int U = default_unroll(G), class JW, class S>
+__device__ __forceinline__ void run_program(const DevProgram &prog, int lane, const double *blobd, S scr,
                                             JW &jw)
 {
+  static_assert(GATHER_UNROLL % U == 0, "batch must divide the program padding");
   const uint4 *it = reinterpret_cast<const uint4 *>(prog.items) + lane;
+  uint4 x[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) x[u] = prog.len > 0 ? __ldg(it + u * G) : make_uint4(0, 0, 0, F_NOP);
   double acc = 0.;
-  for (int j = 0; j < prog.len; ++j, it += G) {
-    const uint4 x = __ldg(it);
-    if (x.w & F_NOP) break;  // padding only follows a lane's last real item
-    const double a = ((x.x & REF_SCRATCH) ? scr : blobd)[x.x & ~REF_SCRATCH];
-    const double bv = ((x.y & REF_SCRATCH) ? scr : blobd)[x.y & ~REF_SCRATCH];
-    if (x.w & F_START) {
-      const uint32_t ii = x.w & INIT_MASK;
-      acc = ii ? scr[ii - 1] : 0.;
+  for (int j = 0; j < prog.len; j += U) {
+    double a[U], bv[U], c0[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      a[u] = gather_operand(x[u].x, blobd, scr);
+      bv[u] = gather_operand(x[u].y, blobd, scr);
+      const uint32_t ii = x[u].w & INIT_MASK;
+      c0[u] = ((x[u].w & F_START) && ii) ? scr[ii - 1] : 0.;
     }
-    acc = fma(a, bv, acc);
-    if (x.w & F_END) {
-      const uint32_t kindd = x.z & DST_KIND_MASK;
-      if (kindd == DST_JBLOCK)
-        jw(x.z & 0x7FFF, (x.z >> 15) & 0x7FFF, acc);
-      else
-        scr[x.z & ~DST_KIND_MASK] = acc;
+    uint4 y[U];
+    const bool more = j + U < prog.len;
+#pragma unroll
+    for (int u = 0; u < U; ++u) y[u] = more ? __ldg(it + (j + U + u) * G) : make_uint4(0, 0, 0, F_NOP);
+    bool stop = false;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (x[u].w & F_NOP) {
+        stop = true;  // padding only follows a lane's last real item
+      } else {
+        if (x[u].w & F_START) acc = c0[u];
+        acc = fma(a[u], bv[u], acc);
+        if (x[u].w & F_END) {
+          const uint32_t kindd = x[u].z & DST_KIND_MASK;
+          if (kindd == DST_JBLOCK)
+            jw(x[u].z & 0x7FFF, (x[u].z >> 15) & 0x7FFF, acc);
+          else
+            scr[x[u].z & ~DST_KIND_MASK] = acc;
+        }
+      }
     }
+    if (stop) break;
+#pragma unroll
+    for (int u = 0; u < U; ++u) x[u] = y[u];
   }
 }
 

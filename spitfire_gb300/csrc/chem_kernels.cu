@@ -35,6 +35,7 @@ struct KParams {
   // outputs
   double *out_w, *out_S, *out_rhs, *out_J;
   int groups_per_cta;
+  double *gscratch;  // thread-per-state kernels: interleaved per-warp scratch in global memory
 };
 
 template <int G>
@@ -57,6 +58,78 @@ struct GlobalJ {
   __device__ __forceinline__ void operator()(int row, int col, double v) const { J[(size_t)col * neq + row] = v; }
 };
 
+// One state: the body shared by the state-group kernel (scratch in shared memory) and the thread-per-state kernel
+// (interleaved scratch in global memory).
+template <int G, int MODE, class S>
+__device__ __forceinline__ void eval_state(const KParams &p, const DevMech &m, const Blob &b, const ScratchLayout &L,
+                                           S scr, const Group<G> &grp, const Progs &pg, const ReactorCfg &cfg, int st)
+{
+  constexpr bool JAC = (MODE == MODE_JAC || MODE == MODE_SENS);
+  const int lane = grp.lane;
+  const int ns = m.ns;
+  const int neq = p.configuration == 1 ? ns + 1 : ns;
+  if (MODE == MODE_RHS || MODE == MODE_JAC) {
+    const double *qs = p.q + (size_t)st * neq;
+    const double pres = p.configuration == 1 ? 0. : (p.pressures ? p.pressures[st] : p.pressure);
+    GlobalJ gj{JAC ? p.out_J + (size_t)st * neq * neq : nullptr, neq};
+    reactor_eval<G, JAC>(m, b, L, scr, grp, qs, pres, cfg, pg, p.out_rhs + (size_t)st * neq, gj);
+    return;
+  }
+  // ---------------- production rates / sensitivities at (T, rho, Y)
+  const double T = p.T[st], rho = p.rho[st];
+  for (int i = lane; i < ns; i += G) scr[L.y + i] = p.Y[(size_t)st * ns + i];
+  grp.sync();
+  double sim = 0.;
+  for (int i = lane; i < ns; i += G) sim += scr[L.y + i] * b.d[m.d_invmw + i];
+  sim = grp.sum(sim);
+  const double mmw = 1. / sim;
+  StateCtx s;
+  s.T = T;
+  s.logT = log(T);
+  s.invT = 1. / T;
+  s.rho = rho;
+  s.invRho = 1. / rho;
+  s.mmw = mmw;
+  s.invM = 1. / mmw;
+  s.ct = rho / mmw;
+  s.log_port = log(m.pref * s.invT * m.invRu);
+  s.option = p.option;
+  prep_species<G, JAC>(m, b, L, scr, grp, s, false, MODE == MODE_SENS);
+  reactions_and_gathers<G, JAC>(m, b, L, scr, grp, s, pg);
+  if (MODE == MODE_RATES) {
+    for (int i = lane; i < ns; i += G) p.out_w[(size_t)st * ns + i] = scr[L.w + i];
+    grp.sync();
+    return;
+  }
+  // Griffon's (ns+1)^2 column-major sensitivity block (rates_sensitivities_exact.cpp:1001-1026)
+  const int n1 = ns + 1;
+  double *Sb = p.out_S + (size_t)st * n1 * n1;
+  for (int i = lane; i < ns; i += G) {
+    p.out_w[(size_t)st * ns + i] = scr[L.w + i];
+    Sb[i] = scr[L.Srho + i];
+    Sb[n1 + i] = scr[L.ST + i];
+  }
+  for (int k = lane; k < n1; k += G) Sb[k * n1 + ns] = 0.;
+  grp.sync();
+  JWriter<G> jw{Sb, n1, 0, 2, rho};
+  run_program<G>(p.prog_j, lane, b.d, scr, jw);
+  grp.sync();
+}
+
+__device__ __forceinline__ ReactorCfg cfg_of(const KParams &p)
+{
+  ReactorCfg cfg;
+  cfg.configuration = p.configuration;
+  cfg.heat = p.heat;
+  cfg.option = p.option;
+  cfg.Tc = p.Tc;
+  cfg.Tr = p.Tr;
+  cfg.hc = p.hc;
+  cfg.eps = p.eps;
+  cfg.SoV = p.SoV;
+  return cfg;
+}
+
 template <int G, int MODE>
 __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
 {
@@ -70,72 +143,61 @@ __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
   const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? L.total : L.total_rhs;
   double *scr = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)gid * scr_doubles;
   const Group<G> grp;
-  const int lane = grp.lane;
-  const int ns = m.ns;
-  constexpr bool JAC = (MODE == MODE_JAC || MODE == MODE_SENS);
-  Progs pg;
-  pg.w = p.prog_w;
-  pg.full = p.prog_full;
-  pg.j = p.prog_j;
-  ReactorCfg cfg;
-  cfg.configuration = p.configuration;
-  cfg.heat = p.heat;
-  cfg.option = p.option;
-  cfg.Tc = p.Tc;
-  cfg.Tr = p.Tr;
-  cfg.hc = p.hc;
-  cfg.eps = p.eps;
-  cfg.SoV = p.SoV;
-  const int neq = p.configuration == 1 ? ns + 1 : ns;
+  const Progs pg{p.prog_w, p.prog_full, p.prog_j};
+  const ReactorCfg cfg = cfg_of(p);
+  for (int st = blockIdx.x * p.groups_per_cta + gid; st < p.n; st += gridDim.x * p.groups_per_cta)
+    eval_state<G, MODE>(p, m, b, L, scr, grp, pg, cfg, st);
+}
 
-  for (int st = blockIdx.x * p.groups_per_cta + gid; st < p.n; st += gridDim.x * p.groups_per_cta) {
-    if (MODE == MODE_RHS || MODE == MODE_JAC) {
-      const double *qs = p.q + (size_t)st * neq;
-      const double pres = p.configuration == 1 ? 0. : (p.pressures ? p.pressures[st] : p.pressure);
-      GlobalJ gj{JAC ? p.out_J + (size_t)st * neq * neq : nullptr, neq};
-      reactor_eval<G, JAC>(m, b, L, scr, grp, qs, pres, cfg, pg, p.out_rhs + (size_t)st * neq, gj);
-      continue;
-    }
-    // ---------------- production rates / sensitivities at (T, rho, Y)
-    const double T = p.T[st], rho = p.rho[st];
-    for (int i = lane; i < ns; i += G) scr[L.y + i] = p.Y[(size_t)st * ns + i];
-    grp.sync();
-    double sim = 0.;
-    for (int i = lane; i < ns; i += G) sim += scr[L.y + i] * b.d[m.d_invmw + i];
-    sim = grp.sum(sim);
-    const double mmw = 1. / sim;
-    StateCtx s;
-    s.T = T;
-    s.logT = log(T);
-    s.invT = 1. / T;
-    s.rho = rho;
-    s.invRho = 1. / rho;
-    s.mmw = mmw;
-    s.invM = 1. / mmw;
-    s.ct = rho / mmw;
-    s.log_port = log(m.pref * s.invT * m.invRu);
-    s.option = p.option;
-    prep_species<G, JAC>(m, b, L, scr, grp, s, false, MODE == MODE_SENS);
-    reactions_and_gathers<G, JAC>(m, b, L, scr, grp, s, pg);
-    if (MODE == MODE_RATES) {
-      for (int i = lane; i < ns; i += G) p.out_w[(size_t)st * ns + i] = scr[L.w + i];
-      grp.sync();
-      continue;
-    }
-    // Griffon's (ns+1)^2 column-major sensitivity block (rates_sensitivities_exact.cpp:1001-1026)
-    const int n1 = ns + 1;
-    double *S = p.out_S + (size_t)st * n1 * n1;
-    for (int i = lane; i < ns; i += G) {
-      p.out_w[(size_t)st * ns + i] = scr[L.w + i];
-      S[i] = scr[L.Srho + i];
-      S[n1 + i] = scr[L.ST + i];
-    }
-    for (int k = lane; k < n1; k += G) S[k * n1 + ns] = 0.;
-    grp.sync();
-    JWriter<G> jw{S, n1, 0, 2, rho};
-    run_program<G>(p.prog_j, lane, b.d, scr, jw);
-    grp.sync();
+// Thread per state: the 32 lanes of a warp evaluate 32 states in lockstep (the same mechanism, so the same
+// instruction stream), each FP64 instruction carrying 32 useful lanes. Scratch is interleaved per warp in global
+// memory (L2/HBM); the mechanism blob is in shared memory, read by all lanes at once.
+template <int MODE>
+__global__ void __launch_bounds__(128) chem_kernel_tps(const KParams p)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t bar;
+  const DevMech &m = p.m;
+  if (!stage_to_smem(smem, p.blob, m.blob_bytes, &bar, p.status)) return;
+  const Blob b = blob_at(m, smem);
+  const ScratchLayout &L = p.L;
+  const int lane = threadIdx.x & 31;
+  const int wg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int nwg = gridDim.x * (blockDim.x >> 5);
+  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? L.total : L.total_rhs;
+  const ScrStrided scr{p.gscratch + (size_t)wg * scr_doubles * 32 + lane};
+  const Group<1> grp;
+  const Progs pg{p.prog_w, p.prog_full, p.prog_j};
+  const ReactorCfg cfg = cfg_of(p);
+  for (int base = wg * 32; base < p.n; base += nwg * 32) {
+    const int st = base + lane;
+    if (st < p.n) eval_state<1, MODE>(p, m, b, L, scr, grp, pg, cfg, st);
   }
+}
+
+// Interleaved scratch of the thread-per-state kernels: one slot of 32 x (Jacobian scratch) doubles per warp that
+// can be resident at once (the CTAS knob, else the occupancy of the Jacobian kernel at the blob's shared memory).
+void ensure_tps_scratch(HostMech &hm)
+{
+  int dev, nsm;
+  CUDA_THROW(cudaGetDevice(&dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const size_t smem = hm.dm.blob_bytes;
+  CUDA_THROW(cudaFuncSetAttribute(chem_kernel_tps<MODE_JAC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int ctas = hm.tune[SF_TUNE_TPS_CTAS];
+  if (ctas <= 0) {
+    CUDA_THROW(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, chem_kernel_tps<MODE_JAC>, 128, smem));
+    if (ctas < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the thread-per-state kernels");
+  }
+  const size_t bytes = (size_t)nsm * ctas * 4 * 32 * hm.sl.total * sizeof(double);
+  if (hm.tps_scratch && hm.tps_scratch_bytes == bytes) return;
+  if (hm.tps_scratch) {
+    CUDA_THROW(cudaFree(hm.tps_scratch));
+    hm.tps_scratch = nullptr;
+    hm.tps_scratch_bytes = 0;
+  }
+  CUDA_THROW(cudaMalloc(&hm.tps_scratch, bytes));
+  hm.tps_scratch_bytes = bytes;
 }
 
 // ------------------------------------------------------------------------------------------------ launchers
@@ -143,9 +205,38 @@ namespace {
 
 int pick_group(const DevMech &m) { return m.nr >= 96 || m.ns >= 24 ? 32 : (m.nr >= 24 ? 16 : 8); }
 
+constexpr int kTpsThreads = 128;
+
+template <int MODE>
+int launch_tps(HostMech &hm, KParams &p, cudaStream_t st)
+{
+  const auto &progs = hm.programs_for(1);
+  p.m = hm.dm;
+  p.blob = hm.d_blob;
+  p.status = hm.d_status;
+  p.L = hm.sl;
+  p.prog_w = progs.progs[0];
+  p.prog_full = progs.progs[1];
+  p.prog_j = (MODE == MODE_SENS) ? progs.progs[3] : progs.progs[2];
+  if (p.n == 0) return SF_OK;
+  const size_t per_warp = (size_t)32 * ((MODE == MODE_JAC || MODE == MODE_SENS) ? hm.sl.total : hm.sl.total_rhs) * 8;
+  const int warps_avail = (int)std::min<size_t>(hm.tps_scratch_bytes / per_warp, (size_t)1 << 30);
+  if (warps_avail < kTpsThreads / 32)
+    throw sf_error(SF_ERR_UNSUPPORTED, "thread-per-state scratch not allocated (set the lanes-per-state knob to 1)");
+  p.gscratch = hm.tps_scratch;
+  const size_t smem = hm.dm.blob_bytes;
+  CUDA_THROW(cudaFuncSetAttribute(chem_kernel_tps<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long need = ((long long)p.n + kTpsThreads - 1) / kTpsThreads;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(need, warps_avail / (kTpsThreads / 32)));
+  chem_kernel_tps<MODE><<<grid, kTpsThreads, smem, st>>>(p);
+  CUDA_THROW(cudaGetLastError());
+  return SF_OK;
+}
+
 template <int MODE>
 int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
 {
+  if (G_req == 1) return launch_tps<MODE>(hm, p, st);
   const int G = G_req > 0 ? G_req : pick_group(hm.dm);
   const auto &progs = hm.programs_for(G);
   p.m = hm.dm;
@@ -223,7 +314,7 @@ int guard(F f)
 int group_of(const HostMech &hm, int knob)
 {
   const int g = hm.tune[knob];
-  return (g == 8 || g == 16 || g == 32) ? g : 0;
+  return (g == 1 || g == 8 || g == 16 || g == 32) ? g : 0;
 }
 }  // namespace
 
@@ -239,14 +330,34 @@ int sf_mech_set_tuning(sf_mech *mech, int knob, int value)
     t_err = "sf_mech_set_tuning: bad argument";
     return SF_ERR_INVALID_ARGUMENT;
   }
-  const bool ok = (knob <= SF_TUNE_GROUP_JAC) ? (value == 0 || value == 8 || value == 16 || value == 32)
+  const bool ok = (knob <= SF_TUNE_GROUP_JAC) ? (value == 0 || value == 1 || value == 8 || value == 16 || value == 32)
                   : (knob == SF_TUNE_INTEGRATE_WARPS) ? (value >= 0 && value <= 8)
+                  : (knob == SF_TUNE_TPS_CTAS) ? (value >= 0 && value <= 16)
                   : (value == 0 || value == 1);
   if (!ok) {
     t_err = "sf_mech_set_tuning: value out of range for this knob";
     return SF_ERR_INVALID_ARGUMENT;
   }
+  const int old = mech->m.tune[knob];
   mech->m.tune[knob] = value;
+  bool tps = false;
+  for (int k = SF_TUNE_GROUP_RATES; k <= SF_TUNE_GROUP_JAC; ++k) tps |= mech->m.tune[k] == 1;
+  if (tps && ((knob <= SF_TUNE_GROUP_JAC && value == 1) || knob == SF_TUNE_TPS_CTAS)) {
+    // thread-per-state kernels: interleaved scratch for every warp that can be resident, (re)allocated here so
+    // that the batched entry points themselves never allocate
+    try {
+      sfgb::ensure_tps_scratch(mech->m);
+    } catch (sfgb::sf_error &e) {
+      mech->m.tune[knob] = old;
+      t_err = e.what();
+      return e.code;
+    }
+  }
+  if (!tps && mech->m.tps_scratch) {
+    cudaFree(mech->m.tps_scratch);
+    mech->m.tps_scratch = nullptr;
+    mech->m.tps_scratch_bytes = 0;
+  }
   return SF_OK;
 }
 

@@ -28,6 +28,7 @@ HostMech::~HostMech()
   }
   if (d_blob) cudaFree(d_blob);
   if (d_status) cudaFree(d_status);
+  if (tps_scratch) cudaFree(tps_scratch);
 }
 
 void HostMech::build(const sf_mech_desc *d)
@@ -333,13 +334,46 @@ struct Entry {
   uint32_t dst;
 };
 
-// Longest-processing-time assignment of entries to G lanes, then the interleaved, padded item array.
+// The device runner loads operands ahead of the stores of earlier items, so a program must never read a scratch
+// location that it writes (as a destination or through an entry's initial value).
+void check_no_read_after_write(const std::vector<Entry> &entries)
+{
+  std::vector<uint32_t> written;
+  for (const Entry &e : entries)
+    if ((e.dst & DST_KIND_MASK) != DST_JBLOCK) written.push_back(e.dst & ~DST_KIND_MASK);
+  std::sort(written.begin(), written.end());
+  auto is_written = [&](uint32_t idx) { return std::binary_search(written.begin(), written.end(), idx); };
+  for (const Entry &e : entries) {
+    if (e.init && is_written(e.init - 1)) throw sf_error(SF_ERR_MECHANISM, "internal: gather program reads what it writes");
+    for (auto &it : e.items)
+      for (uint32_t ref : {it.first, it.second})
+        if ((ref & REF_SCRATCH) && is_written(ref & ~REF_SCRATCH))
+          throw sf_error(SF_ERR_MECHANISM, "internal: gather program reads what it writes");
+  }
+}
+
+// Assignment of entries to G lanes and the interleaved item array, each lane's items padded with no-ops to a
+// multiple of the device runner's batch. G > 1: longest-processing-time assignment (balanced lanes). G = 1 (one
+// lane per state): entries in destination order, Jacobian entries column-major, so that each thread writes its
+// Jacobian block sequentially through memory.
 std::vector<GatherItem> schedule(std::vector<Entry> &entries, int G, int *len_out)
 {
+  check_no_read_after_write(entries);
   std::vector<int> order(entries.size());
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return entries[a].items.size() > entries[b].items.size(); });
+  if (G == 1) {
+    auto key = [&](int e) {
+      const uint32_t d = entries[e].dst;
+      const uint64_t kind = d & DST_KIND_MASK;
+      const uint64_t pos = kind == DST_JBLOCK ? (uint64_t)((d >> 15) & 0x7FFF) << 15 | (d & 0x7FFF)
+                                              : (uint64_t)(d & ~DST_KIND_MASK);
+      return kind << 32 | pos;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
+  } else {
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return entries[a].items.size() > entries[b].items.size(); });
+  }
   std::vector<std::vector<int>> lane(G);
   std::vector<size_t> load(G, 0);
   for (int e : order) {
@@ -351,6 +385,7 @@ std::vector<GatherItem> schedule(std::vector<Entry> &entries, int G, int *len_ou
   }
   size_t len = 0;
   for (int l = 0; l < G; ++l) len = std::max(len, load[l]);
+  len = (len + GATHER_UNROLL - 1) / GATHER_UNROLL * GATHER_UNROLL;
   std::vector<GatherItem> out(len * G, GatherItem{0, 0, 0, F_NOP});
   for (int l = 0; l < G; ++l) {
     size_t j = 0;

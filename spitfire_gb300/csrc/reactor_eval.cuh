@@ -31,9 +31,9 @@ struct SpeciesSums {
 };
 
 // P1: concentrations and thermodynamics of every species; y must already be in scratch.
-template <int G, bool JAC>
+template <int G, bool JAC, class S>
 __device__ __forceinline__ SpeciesSums prep_species(const DevMech &m, const Blob &b, const ScratchLayout &L,
-                                                    double *scr, const Group<G> &grp, const StateCtx &s,
+                                                    S scr, const Group<G> &grp, const StateCtx &s,
                                                     bool isochoric, bool want_eh)
 {
   const int ns = m.ns, lane = grp.lane;
@@ -71,9 +71,9 @@ __device__ __forceinline__ SpeciesSums prep_species(const DevMech &m, const Blob
 }
 
 // P2 + P3: reaction rates (and derivatives) and the species gathers. Returns (EA, EB) of the T-row dense terms.
-template <int G, bool JAC>
+template <int G, bool JAC, int U = default_unroll(G), class S>
 __device__ __forceinline__ double2 reactions_and_gathers(const DevMech &m, const Blob &b, const ScratchLayout &L,
-                                                         double *scr, const Group<G> &grp, const StateCtx &s,
+                                                         S scr, const Group<G> &grp, const StateCtx &s,
                                                          const Progs &pg)
 {
   double EA = 0., EB = 0.;
@@ -84,15 +84,16 @@ __device__ __forceinline__ double2 reactions_and_gathers(const DevMech &m, const
   }
   grp.sync();
   NoJ noj;
-  run_program<G>(JAC ? pg.full : pg.w, grp.lane, b.d, scr, noj);
+  run_program<G, U>(JAC ? pg.full : pg.w, grp.lane, b.d, scr, noj);
   grp.sync();
   return make_double2(EA, EB);
 }
 
 // Reactor right-hand side (and, with JAC, the analytical Jacobian) of the state qs (neq values, any memory space).
 // rhs receives neq values; jset(row, col, value) receives every Jacobian entry exactly once.
-template <int G, bool JAC, class JSet>
-__device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayout &L, double *scr,
+// U: gather batch (loads in flight per lane); smaller batches use fewer registers.
+template <int G, bool JAC, int U = default_unroll(G), class JSet, class S>
+__device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayout &L, S scr,
                              const Group<G> &grp, const double *qs, double pres, const ReactorCfg &c,
                              const Progs &pg, double *rhs, JSet &jset)
 {
@@ -134,7 +135,7 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   s.option = c.option;
   // ---------------- P1-P3
   const SpeciesSums sums = prep_species<G, JAC>(m, b, L, scr, grp, s, isochoric, true);
-  const double2 E = reactions_and_gathers<G, JAC>(m, b, L, scr, grp, s, pg);
+  const double2 E = reactions_and_gathers<G, JAC, U>(m, b, L, scr, grp, s, pg);
   const double EA = E.x, EB = E.y;
   const double cmix = isochoric ? sums.cpmix - m.Ru / mmw : sums.cpmix;  // cv or cp
   const double cpsens = sums.cpsens;
@@ -199,7 +200,7 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   {
     const int off = isochoric ? 2 : 1;
     auto yblock = [&](int row, int col, double v) { jset(off + row, off + col, v); };
-    run_program<G>(pg.j, lane, b.d, scr, yblock);
+    run_program<G, U>(pg.j, lane, b.d, scr, yblock);
   }
   grp.sync();
 

@@ -47,6 +47,8 @@ struct HostMech {
   int *d_status = nullptr;  // device error word of kernels using this mechanism
   int device = 0;
   int tune[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // launch shapes chosen by the autotuner (sf_tune_knob), 0 = default
+  double *tps_scratch = nullptr;           // interleaved scratch of the thread-per-state kernels
+  size_t tps_scratch_bytes = 0;
 
   struct Programs {
     DevProgram progs[4]{};  // 0: w only, 1: w/S_rho/S_T/P/Q, 2: Y block + T row, 3: all species rows (sens)
@@ -63,6 +65,7 @@ struct HostMech {
 int launch_rates(const HostMech &m, int n, const double *T, const double *rho, const double *Y, double *w,
                  cudaStream_t st);
 void set_error(const std::string &msg);
+void ensure_tps_scratch(HostMech &m);
 
 }  // namespace sfgb
 

@@ -76,6 +76,7 @@ constexpr uint32_t F_START = 0x80000000u, F_END = 0x40000000u, F_NOP = 0x2000000
 constexpr uint32_t INIT_MASK = 0x00FFFFFFu;    // scratch index + 1 of the initial value
 constexpr uint32_t DST_SCRATCH = 0u << 30, DST_JBLOCK = 1u << 30, DST_TROW = 2u << 30;
 constexpr uint32_t DST_KIND_MASK = 3u << 30;
+constexpr int GATHER_UNROLL = 8;  // items per batch of the device runner; each lane's item count is a multiple
 
 // Per-state scratch layout (doubles), shared by every kernel of one mechanism.
 struct ScratchLayout {

@@ -4,6 +4,8 @@
 
 Cases (GRI-3.0 unless stated; each ends by checking the device error word):
   jac        isochoric RHS + Jacobian of 8192 states (chem_kernel MODE_JAC), 3 launches
+  jac_tps    the same with the thread-per-state kernel (chem_kernel_tps MODE_JAC) at 2 resident 4-warp blocks per
+             SM, on 38912 states (one warp batch per resident warp), 2 launches
   integrate  256 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s (integrate_kernel)
   flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
              block-Thomas factorization, solve and matvec
@@ -29,6 +31,23 @@ def case_jac():
     q = torch.tensor(W.isochoric_state(W.gri_states(spec, 8192)), device='cuda')
     P = reactor_params('isochoric')
     for _ in range(3):
+        spec.griffon.reactor_jac_batch(P, q, 0)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_jac_tps():
+    import torch
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    AT.set_tuning(spec, 'tps_ctas', 2)
+    AT.set_tuning(spec, 'group_jac', 1)
+    n = torch.cuda.get_device_properties(0).multi_processor_count * 2 * 4 * 32
+    q = torch.tensor(W.isochoric_state(W.gri_states(spec, n)), device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(2):
         spec.griffon.reactor_jac_batch(P, q, 0)
     torch.cuda.synchronize()
     return spec
@@ -86,7 +105,7 @@ def case_fp64issue():
     return None
 
 
-CASES = {'jac': case_jac, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
+CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
          'fp64issue': case_fp64issue}
 
 

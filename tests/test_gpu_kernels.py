@@ -151,3 +151,76 @@ def test_newton_lu_solve(cuda, precision):
     cond = np.array([np.linalg.cond(An[k], np.inf) for k in range(n)])
     fwd = np.abs(xg - xo).max(1) / np.abs(xo).max(1)
     assert (fwd <= 1e3 * cond * 2.2e-16 + 1e-13).all()
+
+
+def _tps_check(spec, og, d, heats, rates=True, species_only=False):
+    import oracle as orc
+    g = spec.griffon
+    if rates:
+        w = gpu_np(g.production_rates_batch(d['T'], d['rho'], d['Y']))
+        assert rownorm_err(w, og.production_rates_batch(d['T'], d['rho'], d['Y'])) <= TOL
+        ns = spec.n_species
+        for opt in (0, 1, 2):
+            w2, S = g.rates_sens_batch(d['rho'], d['T'], d['Y'], opt)
+            wo2, So = og.rates_sens_batch(d['rho'], d['T'], d['Y'], opt)
+            assert rownorm_err(gpu_np(w2), wo2) <= TOL, opt
+            assert rownorm_err(colmajor(gpu_np(S), ns + 1)[:, :ns], colmajor(So, ns + 1)[:, :ns]) <= TOL, opt
+    for configuration in ('isochoric', 'isobaric'):
+        q = W.isochoric_state(d) if configuration == 'isochoric' else W.isobaric_state(d)
+        neq = q.shape[1]
+        for heat in heats:
+            P = reactor_params(configuration, heat, pressure=101325., fluid_temperature=600.,
+                               surface_temperature=900., h_convection=50., eps_radiation=0.3,
+                               surface_area_to_volume=20.)
+            P.inflow_Y = orc._p(np.zeros(spec.n_species))
+            pres = d['p'] if configuration == 'isobaric' else None
+            # species entries only where the temperature row cancels catastrophically (the artificial test
+            # mechanism, see the test above)
+            sp = slice(neq - spec.n_species + 1, None) if species_only else slice(None)
+            rhs = gpu_np(g.reactor_rhs_batch(P, q, pressures=pres))
+            assert rownorm_err(rhs[:, sp], og.reactor_rhs_batch(P, q, pressures=pres)[:, sp]) <= TOL
+            r2, J = g.reactor_jac_batch(P, q, 0, pressures=pres)
+            ro2, Jo = og.reactor_jac_batch(P, q, 0, pressures=pres)
+            assert rownorm_err(gpu_np(r2)[:, sp], ro2[:, sp]) <= TOL
+            assert rownorm_err(colmajor(gpu_np(J), neq)[:, sp], colmajor(Jo, neq)[:, sp]) <= TOL
+    assert g.device_status() == 0
+
+
+def _tps_on(spec, ctas):
+    from spitfire_gb300 import autotune as AT
+    for k in ('group_rates', 'group_sens', 'group_rhs', 'group_jac'):
+        AT.set_tuning(spec, k, 1)
+    AT.set_tuning(spec, 'tps_ctas', ctas)
+
+
+def _tps_off(spec):
+    from spitfire_gb300 import autotune as AT
+    for k in AT.KNOBS:
+        AT.set_tuning(spec, k, 0)
+
+
+@pytest.mark.parametrize('name', ['h2-burke', 'methane-gri30', 'reaction-test'] + UNIT_MECHS)
+def test_thread_per_state_kernels(cuda, name):
+    """Lanes-per-state knob 1 (each lane one state, scratch interleaved across the warp in global memory): rates,
+    sensitivities, right-hand sides and Jacobians at the same bar, on a batch that is not a multiple of 32."""
+    spec, og = pair(name)
+    try:
+        _tps_on(spec, 0)
+        _tps_check(spec, og, random_states(spec, 100, 23), ('adiabatic', 'diathermal'),
+                   species_only=name == 'reaction-test')
+    finally:
+        _tps_off(spec)
+
+
+@pytest.mark.parametrize('name', ['h2-burke', 'methane-gri30'])
+def test_thread_per_state_grid_stride(cuda, name):
+    """One 4-warp block per SM and more states than resident lanes: the thread-per-state kernels loop over warp
+    batches (ignition-range states of the workload distributions)."""
+    spec, og = pair(name)
+    n = 152 * 128 + 77
+    d = W.h2_states(spec, n) if name == 'h2-burke' else W.gri_states(spec, n)
+    try:
+        _tps_on(spec, 1)
+        _tps_check(spec, og, d, ('adiabatic',), rates=name == 'methane-gri30')
+    finally:
+        _tps_off(spec)
