@@ -178,10 +178,42 @@ __device__ __forceinline__ double ipow(double x, int n)
   return r;
 }
 
+// exp(-g/RT) of one species as m 2^k with |ln m| <= ln(2)/2, formed once per state so that the equilibrium factor
+// of every reversible reaction, exp(-sum_i nu_i g_i/RT), becomes a product of mantissas and an exact power-of-two
+// scaling instead of one exponential per reaction. The reduction r = x - k ln 2 splits ln 2 into a head of 32
+// significant bits and a tail (Cody and Waite, "Software Manual for the Elementary Functions", 1980), so that
+// k * LN2_HI is exact for |k| < 2^21 and LN2_HI + LN2_LO equals ln 2 to 1e-26.
+template <class S>
+__device__ __forceinline__ void store_gibbs_factor(S scr, const ScratchLayout &L, int i, double gRT)
+{
+  constexpr double LOG2E = 1.4426950408889634;
+  constexpr double LN2_HI = 6.93147180369123816490e-01;  // ln 2 with the low 21 mantissa bits cleared
+  constexpr double LN2_LO = 1.90821492927058770002e-10;  // ln 2 - LN2_HI
+  const double x = -gRT;
+  const double kd = rint(x * LOG2E);
+  const double rr = fma(-kd, LN2_LO, fma(-kd, LN2_HI, x));
+  const double mm = exp(rr);
+  scr[L.gm + i] = mm;
+  scr[L.gmi + i] = 1. / mm;
+  scr[L.gk + i] = __longlong_as_double((long long)kd);
+}
+
+// x 2^K, exact unless the result leaves the normal range; |K| beyond 2044 already takes any factor of a rate
+// expression to 0 or infinity.
+__device__ __forceinline__ double scale_pow2(double x, long long K)
+{
+  const int k = (int)(K < -2044 ? -2044 : (K > 2046 ? 2046 : K));
+  const int k1 = k / 2, k2 = k - k1;  // both within [-1022, 1023]
+  const double f1 = __longlong_as_double((long long)(k1 + 1023) << 52);
+  const double f2 = __longlong_as_double((long long)(k2 + 1023) << 52);
+  return x * f1 * f2;
+}
+
 // ------------------------------------------------------------------------------------------ reaction phase
 // Per-state quantities every reaction needs.
 struct StateCtx {
-  double T, logT, invT, rho, invRho, mmw, invM, ct, log_port;
+  double T, logT, invT, rho, invRho, mmw, invM, ct;
+  double port, invport;  // p_ref / (R T) and its reciprocal
   int option;  // rates-sensitivity option: 0 / 2 exact, 1 without third-body/falloff derivatives
 };
 
@@ -202,6 +234,57 @@ __device__ __forceinline__ double mass_action(const int *lst, int n, const SC &C
       v *= ipow(c, nu);
   }
   return v;
+}
+
+// Mass-action factors of a reactant or product list of at most three entries, formed once per reaction: the
+// product P = prod_i C_i^nu_i and, per list position j, g_j = d P / d Y_j / rho = nu_j / M_j C_j^(nu_j - 1)
+// prod_{i != j} C_i^nu_i (C_i = rho Y_i / M_i). The Jacobian slots of the reaction then cost one multiply each.
+struct MassAction3 {
+  double P, g0, g1, g2;
+  __device__ __forceinline__ double g(int j) const { return j == 0 ? g0 : (j == 1 ? g1 : g2); }
+};
+
+template <class SC>
+__device__ __forceinline__ MassAction3 mass_action3(const int *lst, int n, const SC &C, const double *invmw_d)
+{
+  double p[3], d[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    p[j] = 1.;
+    d[j] = 0.;
+    if (j < n) {
+      const int e = lst[j];
+      const int sp = e & 0xFFFF, nu = e >> 16;
+      const double c = C[sp];
+      const double im = invmw_d[sp];
+      if (nu == 1) {
+        p[j] = c;
+        d[j] = im;
+      } else {
+        const double cm = ipow(c, nu - 1);
+        p[j] = cm * c;
+        d[j] = (double)nu * im * cm;
+      }
+    }
+  }
+  MassAction3 o;
+  if (n <= 1) {
+    o.P = p[0];
+    o.g0 = d[0];
+    o.g1 = o.g2 = 0.;
+  } else if (n == 2) {
+    o.P = p[0] * p[1];
+    o.g0 = d[0] * p[1];
+    o.g1 = p[0] * d[1];
+    o.g2 = 0.;
+  } else {
+    const double t = p[0] * p[1];
+    o.P = t * p[2];
+    o.g0 = d[0] * (p[1] * p[2]);
+    o.g1 = d[1] * (p[0] * p[2]);
+    o.g2 = d[2] * t;
+  }
+  return o;
 }
 
 // Special-order rate law (chemistry_kernels.cpp:316-325) and its Y derivative for order-list position `at`
@@ -342,27 +425,50 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
   double Rf, kr = 0., Rr = 0.;
   const int sums = b.i[m.i_sums + r];
   const int sum_nu = (int)(short)(sums & 0xFFFF);
+  // lists of at most three entries (every reaction of common mechanisms) use the factored form
+  const bool short_lists = !orders && nre <= 3 && npr <= 3;
+  MassAction3 mr, mp;
+  mp.P = mp.g0 = mp.g1 = mp.g2 = 0.;
   if (orders) {
     Rf = kf * special_orders(m, b, r, C, s.rho, -1, false);
   } else {
-    Rf = kf * mass_action(rl, nre, C, invmw_d, s.rho, -1);
+    if (short_lists) {
+      mr = mass_action3(rl, nre, C, invmw_d);
+      Rf = kf * mr.P;
+    } else {
+      Rf = kf * mass_action(rl, nre, C, invmw_d, s.rho, -1);
+    }
     // rates of a special-order reaction have no reverse part (chemistry_kernels.cpp:316-326)
     if (rev && !has_ord) {
+      // kr = kf exp(sum_nu ln(p_ref/RT) - sum_i nu_i g_i/RT) (chemistry_kernels.cpp:327-341), with
+      // exp(-g_i/RT) = gm_i 2^gk_i
       const int n0 = b.i[m.i_net_off + r], n1 = b.i[m.i_net_off + r + 1];
-      double sg = 0.;
+      double mant = 1.;
+      long long K = 0;
       for (int j = n0; j < n1; ++j) {
         const int e = b.i[m.i_net + j];
-        sg += (double)((e >> 16) - 128) * scr[L.gRT + (e & 0xFFFF)];
+        const int sp = e & 0xFFFF, nu = (e >> 16) - 128;
+        const double mi = scr[(nu > 0 ? L.gm : L.gmi) + sp];
+        const int a = nu > 0 ? nu : -nu;
+        mant *= a == 1 ? mi : ipow(mi, a);
+        K += (long long)nu * __double_as_longlong(scr[L.gk + sp]);
       }
-      kr = kf * exp(sum_nu * s.log_port - sg);
-      Rr = kr * mass_action(pl, npr, C, invmw_d, s.rho, -1);
+      const double pw = sum_nu >= 0 ? ipow(s.port, sum_nu) : ipow(s.invport, -sum_nu);
+      kr = scale_pow2(kf * pw * mant, K);
+      if (short_lists) {
+        mp = mass_action3(pl, npr, C, invmw_d);
+        Rr = kr * mp.P;
+      } else {
+        Rr = kr * mass_action(pl, npr, C, invmw_d, s.rho, -1);
+      }
     }
   }
   const double Rnet = Rf - Rr;
   scr[L.q + r] = Rnet * Ctbaf;
   if (!JAC) return;
 
-  const double sum_reac_nu = (double)((sums >> 16) & 0xFF), sum_prod_nu = (double)((sums >> 24) & 0xFF);
+  const double *smallint = b.d + m.d_smallint + 128;
+  const double sum_reac_nu = smallint[(sums >> 16) & 0xFF], sum_prod_nu = smallint[(sums >> 24) & 0xFF];
   double dRdrho, dRdT;
   if (orders) {
     double sumo = 0.;
@@ -377,7 +483,7 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
       const int n0 = b.i[m.i_net_off + r], n1 = b.i[m.i_net_off + r + 1];
       for (int j = n0; j < n1; ++j) {
         const int e = b.i[m.i_net + j];
-        dKc -= (double)((e >> 16) - 128) * scr[L.dB + (e & 0xFFFF)];
+        dKc -= smallint[(e >> 16) - 128] * scr[L.dB + (e & 0xFFFF)];
       }
     }
     dRdrho = (Rf * sum_reac_nu - Rr * sum_prod_nu) * s.invRho;
@@ -386,8 +492,9 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
   const bool tbaf = s.option != 1;
   scr[L.dqdrho + r] = dRdrho * Ctbaf + (tbaf ? dCdrho * Rnet : 0.);
   scr[L.dqdT + r] = dRdT * Ctbaf + (tbaf ? dCdT * Rnet : 0.);
-  const double RK = tbaf ? Rnet * K * s.rho : 0.;
-  // sparse slots
+  // d q / d Y_k / rho through the third-body concentration: rho * Rnet * K * eff_k / rho
+  const double RK = tbaf ? Rnet * K : 0.;
+  // sparse slots: D_j = d q / d Y_k / rho for the slot's species k
   const int ns = m.ns;
   const int s0 = b.i[m.i_slot_off + r], s1 = b.i[m.i_slot_off + r + 1];
   const int tb0 = b.i[m.i_tb_off + r];
@@ -395,19 +502,22 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
     const int e = b.i[m.i_slot + j];
     const int rp = ((e >> 16) & 15) - 1, pp = ((e >> 20) & 15) - 1, tp = ((e >> 24) & 15) - 1;
     const int op = ((unsigned)e >> 28) - 1;
-    double v = 0.;
+    double v = 0.;  // d (Rf - Rr) / d Y_k / rho
     if (orders) {
       if (op >= 0) {
         const int oe = b.i[m.i_ord + b.i[m.i_ord_off + r] + op];
-        if (oe >> 16) v = kf * special_orders(m, b, r, C, s.rho, op, false);
+        if (oe >> 16) v = kf * special_orders(m, b, r, C, s.rho, op, false) * s.invRho;
       }
+    } else if (short_lists) {
+      if (rp >= 0) v += kf * mr.g(rp);
+      if (pp >= 0 && kr != 0.) v -= kr * mp.g(pp);
     } else {
-      if (rp >= 0) v += kf * mass_action(rl, nre, C, invmw_d, s.rho, rp);
-      if (pp >= 0 && kr != 0.) v -= kr * mass_action(pl, npr, C, invmw_d, s.rho, pp);
+      if (rp >= 0) v += kf * mass_action(rl, nre, C, invmw_d, s.rho, rp) * s.invRho;
+      if (pp >= 0 && kr != 0.) v -= kr * mass_action(pl, npr, C, invmw_d, s.rho, pp) * s.invRho;
     }
     double Dv = Ctbaf * v;
     if (tp >= 0) Dv += RK * b.d[m.d_tbeff + tb0 + tp];
-    scr[L.D + j] = Dv * s.invRho;
+    scr[L.D + j] = Dv;
   }
   const int di = b.i[m.i_dense + r];
   double Er = 0.;
@@ -417,20 +527,27 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
   }
   scr[L.E + r] = Er;
   if (di >= 0) {
-    // closure species ns-1 and third-body terms common to every Y column
+    // closure species ns-1 and third-body terms common to every Y column (all divided by rho)
     double closure = 0.;
     if (orders) {
       const int o0 = b.i[m.i_ord_off + r], o1 = b.i[m.i_ord_off + r + 1];
       for (int j = o0; j < o1; ++j) {
         const int oe = b.i[m.i_ord + j];
-        if ((oe & 0xFFFF) == ns - 1 && (oe >> 16)) closure -= kf * special_orders(m, b, r, C, s.rho, j - o0, true);
+        if ((oe & 0xFFFF) == ns - 1 && (oe >> 16))
+          closure -= kf * special_orders(m, b, r, C, s.rho, j - o0, true) * s.invRho;
       }
-    } else {
+    } else if (short_lists) {
       for (int j = 0; j < nre; ++j)
-        if ((rl[j] & 0xFFFF) == ns - 1) closure -= kf * mass_action(rl, nre, C, invmw_d, s.rho, j);
+        if ((rl[j] & 0xFFFF) == ns - 1) closure -= kf * mr.g(j);
       if (kr != 0.)
         for (int j = 0; j < npr; ++j)
-          if ((pl[j] & 0xFFFF) == ns - 1) closure += kr * mass_action(pl, npr, C, invmw_d, s.rho, j);
+          if ((pl[j] & 0xFFFF) == ns - 1) closure += kr * mp.g(j);
+    } else {
+      for (int j = 0; j < nre; ++j)
+        if ((rl[j] & 0xFFFF) == ns - 1) closure -= kf * mass_action(rl, nre, C, invmw_d, s.rho, j) * s.invRho;
+      if (kr != 0.)
+        for (int j = 0; j < npr; ++j)
+          if ((pl[j] & 0xFFFF) == ns - 1) closure += kr * mass_action(pl, npr, C, invmw_d, s.rho, j) * s.invRho;
     }
     double beta = Ctbaf * closure;
     if (tbaf && kind != 1) {
@@ -439,10 +556,10 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
         if (b.i[m.i_tb + j] == ns - 1) beta -= RK * b.d[m.d_tbeff + j];
     }
     const double alpha = (kind != 1) ? RK * b.d[m.d_beff + r] : 0.;
-    scr[L.alpha + di] = alpha * s.invRho;
-    scr[L.beta + di] = beta * s.invRho;
-    *Eacc_a += Er * alpha * s.invRho;
-    *Eacc_b += Er * beta * s.invRho;
+    scr[L.alpha + di] = alpha;
+    scr[L.beta + di] = beta;
+    *Eacc_a += Er * alpha;
+    *Eacc_b += Er * beta;
   }
 }
 

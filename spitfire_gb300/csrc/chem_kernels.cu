@@ -92,7 +92,8 @@ __device__ __forceinline__ void eval_state(const KParams &p, const DevMech &m, c
   s.mmw = mmw;
   s.invM = 1. / mmw;
   s.ct = rho / mmw;
-  s.log_port = log(m.pref * s.invT * m.invRu);
+  s.port = m.pref * s.invT * m.invRu;
+  s.invport = 1. / s.port;
   s.option = p.option;
   prep_species<G, JAC>(m, b, L, scr, grp, s, false, MODE == MODE_SENS);
   reactions_and_gathers<G, JAC>(m, b, L, scr, grp, s, pg);

@@ -22,6 +22,10 @@
 namespace sfgb {
 namespace {
 
+// Gather batch of the reactor evaluations inside the integrator: unbatched measured fastest there (the warp's scratch
+// is in shared memory or L2, and the integrator kernel has no registers to spare for operands in flight).
+constexpr int kIntegratorUnroll = 1;
+
 constexpr double kGamma = 0.25;
 // ESDIRK64 stage coefficients a_sj (methods.py:464-500)
 __constant__ double c_a[6][6] = {
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
       if (coerce && t + dt > ip.stop_at_time) dt = ip.stop_at_time - t;
       if (setup) {
         IterMatrix im{A, neq, dt * kGamma};
-        reactor_eval<32, true>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, f, im);
+        reactor_eval<32, true, kIntegratorUnroll>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, f, im);
         __syncwarp();
         if (p.prec == 1) {
           for (int e = lane; e < neq * neq; e += 32) LU32[e] = (float)A[e];
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
         for (int i = lane; i < neq; i += 32) slot[2 + i] = y[i];
       }
       // ---------------- one ESDIRK64 step (methods.py:502-612)
-      reactor_eval<32, false>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, k, noj);
+      reactor_eval<32, false, kIntegratorUnroll>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, k, noj);
       for (int i = lane; i < neq; i += 32) Y[i] = y[i];
       __syncwarp();
       bool nl_ok = true;
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
           }
           for (int i = lane; i < neq; i += 32) Y[i] -= x[i];
           __syncwarp();
-          reactor_eval<32, false>(m, b, L, scr, grp, Y, pres, p.cfg, p.pg, f, noj);
+          reactor_eval<32, false, kIntegratorUnroll>(m, b, L, scr, grp, Y, pres, p.cfg, p.pg, f, noj);
           double nrm = 0.;
           for (int i = lane; i < neq; i += 32) {
             res[i] = dt * (kGamma * f[i] + prior[i]) - (Y[i] - y[i]);

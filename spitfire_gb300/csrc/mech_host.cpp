@@ -128,6 +128,9 @@ void HostMech::build(const sf_mech_desc *d)
     for (int v : x.reac_nu) x.sum_reac_nu += std::abs(v);
     x.sum_prod_nu = 0;
     for (int v : x.prod_nu) x.sum_prod_nu += std::abs(v);
+    // coefficients and their sums are read through the device's table of small integers
+    if (x.sum_reac_nu > 127 || x.sum_prod_nu > 127)
+      throw sf_error(SF_ERR_MECHANISM, "reaction " + std::to_string(r) + ": stoichiometric coefficients above 127");
     if (std::abs(x.kf[2]) < 1.e-6) {
       if (std::abs(x.kf[1]) < 1.e-6) x.kform = 0;
       else if (std::abs(x.kf[1] - 1) < 1.e-6) x.kform = 1;
@@ -235,6 +238,8 @@ void HostMech::build(const sf_mech_desc *d)
   m.d_ord = dsec(nord);
   m.d_one = dsec(1);
   D[m.d_one] = 1.;
+  m.d_smallint = dsec(256);
+  for (int k = 0; k < 256; ++k) D[m.d_smallint + k] = k - 128;
   m.i_info = isec(nr);
   m.i_orig = isec(nr);
   for (int r = 0; r < nr; ++r) I[m.i_orig + r] = orig_index[r];
@@ -305,7 +310,8 @@ void HostMech::build(const sf_mech_desc *d)
   int o = 0;
   auto take = [&](int n) { const int r = o; o += (n + 1) & ~1; return r; };
   L.misc = take(16);
-  L.y = take(ns); L.C = take(ns); L.gRT = take(ns); L.eh = take(ns); L.cpv = take(ns); L.w = take(ns);
+  L.y = take(ns); L.C = take(ns); L.eh = take(ns); L.cpv = take(ns); L.w = take(ns);
+  L.gm = take(ns); L.gmi = take(ns); L.gk = take(ns);
   L.q = take(nr);
   L.total_rhs = o;
   L.dB = take(ns); L.dcp = take(ns); L.Srho = take(ns); L.ST = take(ns); L.P = take(ns); L.Q = take(ns);

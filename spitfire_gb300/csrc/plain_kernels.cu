@@ -58,13 +58,13 @@ __global__ void __launch_bounds__(128) plain_jac_kernel(const PlainParams p)
   }
   StateCtx s;
   s.T = T; s.logT = log(T); s.invT = 1. / T; s.rho = rho; s.invRho = 1. / rho; s.mmw = mmw; s.invM = 1. / mmw;
-  s.ct = rho / mmw; s.log_port = log(m.pref * s.invT * m.invRu); s.option = 0;
+  s.ct = rho / mmw; s.port = m.pref * s.invT * m.invRu; s.invport = 1. / s.port; s.option = 0;
   double cpmix = 0., cpsens = 0.;
   for (int i = 0; i < ns; ++i) {
     const double invmw = b.d[m.d_invmw + i];
     scr[L.C + i] = scr[L.y + i] * rho * invmw;
     const SpeciesThermo th = species_thermo(m, b, i, T, s.logT, s.invT, true);
-    scr[L.gRT + i] = th.g * s.invT * m.invRu;
+    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu);
     scr[L.eh + i] = iso ? th.h - m.Ru * T * invmw : th.h;
     scr[L.cpv + i] = iso ? th.cp - m.Ru * invmw : th.cp;
     scr[L.dB + i] = th.dB;

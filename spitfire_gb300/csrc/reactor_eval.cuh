@@ -43,7 +43,7 @@ __device__ __forceinline__ SpeciesSums prep_species(const DevMech &m, const Blob
     const double invmw = b.d[m.d_invmw + i];
     scr[L.C + i] = yi * s.rho * invmw;
     const SpeciesThermo th = species_thermo(m, b, i, s.T, s.logT, s.invT, JAC);
-    scr[L.gRT + i] = th.g * s.invT * m.invRu;
+    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu);
     if (want_eh) {
       scr[L.eh + i] = isochoric ? th.h - m.Ru * s.T * invmw : th.h;
       scr[L.cpv + i] = isochoric ? th.cp - m.Ru * invmw : th.cp;
@@ -131,7 +131,8 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   s.mmw = mmw;
   s.invM = 1. / mmw;
   s.ct = rho / mmw;
-  s.log_port = log(m.pref * s.invT * m.invRu);
+  s.port = m.pref * s.invT * m.invRu;
+  s.invport = 1. / s.port;
   s.option = c.option;
   // ---------------- P1-P3
   const SpeciesSums sums = prep_species<G, JAC>(m, b, L, scr, grp, s, isochoric, true);

@@ -44,6 +44,7 @@ struct DevMech {
   int d_netc;    // [net entries] -nu*M (coefficient of q_r in w_i)
   int d_ord;     // [order entries] special orders
   int d_one;     // 1.0
+  int d_smallint;  // [256] the integer k - 128 at index k (stoichiometric coefficients without conversions)
 
   // ---- int section offsets ----
   int i_info;    // [nr]
@@ -80,7 +81,8 @@ constexpr int GATHER_UNROLL = 8;  // items per batch of the device runner; each 
 
 // Per-state scratch layout (doubles), shared by every kernel of one mechanism.
 struct ScratchLayout {
-  int y, C, gRT, dB, eh, cpv, dcp;     // species arrays [ns]
+  int y, C, dB, eh, cpv, dcp;          // species arrays [ns]
+  int gm, gmi, gk;                     // [ns] exp(-g/RT) = gm * 2^gk (gk as integer bits), gmi = 1 / gm
   int w, Srho, ST, P, Q, trow;         // gather destinations [ns]
   int q, dqdrho, dqdT, E;              // reaction arrays [nr]
   int alpha, beta;                     // [n_dense]
