@@ -256,6 +256,15 @@ typedef struct sf_integrate_params {
   int refine_sweeps;                /* refinement sweeps for linear_precision 1 */
   int rates_option;                 /* 0 dense exact (default), 2 sparse exact */
   int max_attempts;                 /* cap on step attempts (accepted + failed) per reactor */
+  /* Open reactors (params->open) with a time-dependent feed temperature: when feed_temperature_table is non-NULL
+   * (DEVICE pointer to feed_points >= 2 values at integration-local times feed_t0 + j feed_dt), the feed
+   * temperature is its piecewise-linear interpolant, held constant beyond the ends, in place of
+   * params->inflow_temperature. As in the reference (reactors.py:279-282, :335-338, :538-592), each right-hand side
+   * takes the feed at its own time and each Jacobian the feed of the most recent right-hand side, or the feed at
+   * feed_jac_t0 before the first one. NULL: the constant params->inflow_temperature. */
+  const double *feed_temperature_table;
+  int feed_points;
+  double feed_t0, feed_dt, feed_jac_t0;
 } sf_integrate_params;
 
 /* Per-reactor outcome codes written to out_status. */
@@ -265,7 +274,7 @@ enum sf_integrate_status {
 };
 
 size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
-/* Integrate n independent closed reactors of the same configuration from q0 (state-major; isobaric reactors
+/* Integrate n independent reactors of the same configuration and feed from q0 (state-major; isobaric reactors
  * may each have their own pressure). One persistent launch works through the batch: each warp takes the next
  * unfinished reactor from a queue, so reactors with 10x more steps do not stall the rest. Outputs: final states
  * out_q, final time out_t, per-reactor counters out_counts[n][4] = steps, Newton iterations, Jacobian setups,

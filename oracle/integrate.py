@@ -42,13 +42,41 @@ class ReactorProblem:
         self.Tidx = 0 if configuration == 'isobaric' else 1
         self.pres = np.array([pressure]) if configuration == 'isobaric' else None
 
-    def rhs(self, q):
+    def rhs(self, q, t=0.):
         return self.og.reactor_rhs_batch(self.P, q[None, :], pressures=self.pres)[0]
 
     def jac(self, q):
         n = q.size
         _, J = self.og.reactor_jac_batch(self.P, q[None, :], 0, pressures=self.pres)
         return J[0].reshape((n, n), order='F')
+
+
+class OpenReactorProblem(ReactorProblem):
+    """Open (mass-exchange) reactor: a feed of temperature `feed_temperature` (a number or a function of time), mass
+    fractions `feed_Y`, density `feed_density` (isochoric) and mixing time `tau`. As in the reference's closures
+    (reactors.py:538-592 with _update_mass_transfer_parameters, :335-338) every right-hand side evaluation refreshes
+    the feed temperature at its own time, and the Jacobian uses the values the most recent right-hand side left
+    (those at t = 0 before the first one, reactors.py:279-282)."""
+
+    def __init__(self, og, configuration, feed_temperature, feed_Y, tau, pressure=101325., heat='adiabatic',
+                 feed_density=0.):
+        import oracle as orc
+        super().__init__(og, configuration, pressure=pressure, heat=heat)
+        self.P.open = 1
+        self.P.tau = tau
+        self.P.inflow_density = feed_density
+        self._yin = np.asarray(feed_Y, dtype=np.float64).copy()
+        self.P.inflow_Y = orc._p(self._yin)
+        self._tf = feed_temperature
+        self.P.inflow_temperature = feed_temperature(0.) if callable(feed_temperature) else feed_temperature
+
+    def rhs(self, q, t=0.):
+        if callable(self._tf):
+            self.P.inflow_temperature = self._tf(t)
+        return super().rhs(q)
+
+
+C = A.sum(axis=1)  # stage times t + c_s dt
 
 
 def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tolerance=1.e-10,
@@ -90,7 +118,7 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
         setup_count += 1
         # ---- ESDIRK64 single step (methods.py:502-612)
         k = np.zeros((6, neq))
-        k[0] = prob.rhs(state)
+        k[0] = prob.rhs(state, t)
         Y = state.copy()
         nl_ok = True
         nl_slow = False
@@ -102,7 +130,7 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
             for it in range(1, max_nonlinear_iter + 1):
                 dx = dgetrs(lu, piv, resid)[0]
                 Y = Y - dx
-                f = prob.rhs(Y)
+                f = prob.rhs(Y, t + C[s] * dt)
                 resid = dt * (GAMMA * f + prior) - (Y - state)
                 nnewton += 1
                 if np.max(np.abs(resid * w)) < nonlinear_tolerance:

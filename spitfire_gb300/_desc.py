@@ -48,7 +48,8 @@ class SfIntegrateParams(C.Structure):
                 ('stop_at_time', C.c_double), ('delta_temperature_ignition', C.c_double),
                 ('minimum_allowable_residual', C.c_double), ('stop_at_steady', C.c_double),
                 ('linear_precision', C.c_int), ('refine_sweeps', C.c_int), ('rates_option', C.c_int),
-                ('max_attempts', C.c_int)]
+                ('max_attempts', C.c_int), ('feed_temperature_table', _dp), ('feed_points', C.c_int),
+                ('feed_t0', C.c_double), ('feed_dt', C.c_double), ('feed_jac_t0', C.c_double)]
 
 
 class SfFlameletBatch(C.Structure):

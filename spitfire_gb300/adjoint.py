@@ -124,9 +124,11 @@ class ReactorAdjoint:
         Bt = torch.tensor(_B, dtype=torch.float64, device=q0.device)
         h = rec[:, :, 1]
         Ts = rec[:, :, 2:].view(n, capacity, 6, self.neq)[..., self.tix]
-        valid = (torch.arange(capacity, device=q0.device)[None, :] < steps[:, None]).double()
+        # slots past a reactor's last step hold whatever the buffer held: select, do not multiply by zero
+        valid = torch.arange(capacity, device=q0.device)[None, :] < steps[:, None]
         g = 1. - torch.sigmoid((Ts - T0[:, None, None] - DT_IGN) / WIDTH)
-        tau = (valid * h * (g * Bt).sum(-1)).sum(1)
+        contrib = h * (g * Bt).sum(-1)
+        tau = torch.where(valid, contrib, torch.zeros_like(contrib)).sum(1)
         return Trajectory(q0=q0, pressures=pressures, rec=rec, steps=steps, status=out['status'], q_end=out['q'],
                           t_end=out['t'], T0=T0, T_end=out['q'][:, self.tix].clone(), tau_s=tau,
                           counts=out['counts'])

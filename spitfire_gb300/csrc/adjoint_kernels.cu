@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
     for (int st = 0; st < p.stages; ++st) {
       const double *qs = p.q + ((size_t)it * p.stages + st) * neq;
       const double *w = p.w + ((size_t)it * p.stages + st) * neq;
-      reactor_eval<G, false>(m, b, L, scr, grp, qs, pres, p.cfg, p.pg, rhs_tmp, noj);
+      reactor_eval<G, false, default_unroll(G), false>(m, b, L, scr, grp, qs, pres, p.cfg, p.pg, rhs_tmp, noj);
       // state quantities (as in reactor_eval)
       const double T = qs[tix];
       double sim = 0., cmix = 0.;

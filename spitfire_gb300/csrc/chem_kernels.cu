@@ -36,6 +36,10 @@ struct KParams {
   double *out_w, *out_S, *out_rhs, *out_J;
   int groups_per_cta;
   double *gscratch;  // thread-per-state kernels: interleaved per-warp scratch in global memory
+  // open reactors: feed
+  int open;
+  double tau, rho_in, Tin;
+  const double *yin;
 };
 
 template <int G>
@@ -128,6 +132,11 @@ __device__ __forceinline__ ReactorCfg cfg_of(const KParams &p)
   cfg.hc = p.hc;
   cfg.eps = p.eps;
   cfg.SoV = p.SoV;
+  cfg.open = p.open;
+  cfg.tau = p.tau;
+  cfg.rho_in = p.rho_in;
+  cfg.Tin = p.Tin;
+  cfg.yin = p.yin;
   return cfg;
 }
 
@@ -471,7 +480,16 @@ static void fill_reactor(KParams &p, const sf_reactor_params *rp)
   if (!rp) throw sf_error(SF_ERR_INVALID_ARGUMENT, "null reactor params");
   if (rp->configuration != 0 && rp->configuration != 1) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad configuration");
   if (rp->heat_transfer < 0 || rp->heat_transfer > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad heat_transfer");
-  if (rp->open) throw sf_error(SF_ERR_UNSUPPORTED, "open (mass-exchange) reactors are not on the GPU path");
+  if (rp->open) {
+    if (!rp->inflow_Y) throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor without feed mass fractions");
+    if (!(rp->tau > 0.)) throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs a positive mixing time");
+    if (!(rp->inflow_temperature > 0.)) throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs a feed temperature");
+  }
+  p.open = rp->open ? 1 : 0;
+  p.tau = rp->tau;
+  p.rho_in = rp->inflow_density;
+  p.Tin = rp->inflow_temperature;
+  p.yin = rp->inflow_Y;
   p.configuration = rp->configuration;
   p.heat = rp->heat_transfer;
   p.pressure = rp->pressure;

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
     const double mcf = p.mc[pt], ncf = p.nc[pt], chi = p.chi[pt];
     if (!JAC) {
       double *out = p.out_rhs + (size_t)pt * ns;
-      reactor_eval<G, false>(m, b, L, scr, grp, st, p.pressure, cfg, p.pg, out, noj);
+      reactor_eval<G, false, default_unroll(G), false>(m, b, L, scr, grp, st, p.pressure, cfg, p.pg, out, noj);
       // enthalpy-flux and variable-cp terms of the temperature equation (flamelet_kernels.cpp:1141-1206)
       double cp = 0.;
       for (int i = lane; i < ns; i += G) cp += scr[L.y + i] * scr[L.cpv + i];
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
       double *blk = vals + (size_t)iz * ns * ns;
       BlockWriter bw{blk, ns, p.cmajor + (size_t)pt * ns, p.scale_offset, p.prefactor};
       double *rhs_tmp = scr + L.total;
-      reactor_eval<G, true>(m, b, L, scr, grp, st, p.pressure, cfg, p.pg, rhs_tmp, bw);
+      reactor_eval<G, true, default_unroll(G), false>(m, b, L, scr, grp, st, p.pressure, cfg, p.pg, rhs_tmp, bw);
       if (p.eflux) {
         // approximate diagonal correction of the enthalpy-flux term (flamelet_kernels.cpp:1350-1381)
         double cp = 0., cps = 0.;

@@ -35,6 +35,14 @@ __constant__ double c_a[6][6] = {
     {5012029. / 34652500., -654441. / 2922500., 174375. / 388108., 0.25, 0., 0.},
     {15267082809. / 155376265600., -71443401. / 120774400., 730878875. / 902184768., 2285395. / 8070912., 0.25, 0.},
     {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25}};
+// stage times c_s = sum_j a_sj, summed left to right as numpy does for methods.py:500 (self.c)
+__constant__ double c_c[6] = {
+    0.,
+    0.25 + 0.25,
+    8611. / 62500. + -1743. / 31250. + 0.25,
+    5012029. / 34652500. + -654441. / 2922500. + 174375. / 388108. + 0.25,
+    15267082809. / 155376265600. + -71443401. / 120774400. + 730878875. / 902184768. + 2285395. / 8070912. + 0.25,
+    82889. / 524892. + 0. + 15625. / 83664. + 69875. / 102672. + -2260. / 8211. + 0.25};
 __constant__ double c_b[6] = {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25};
 __constant__ double c_bh[6] = {4586570599. / 29645900160., 0., 178811875. / 945068544., 814220225. / 1159782912.,
                                -3700637. / 11593932., 61727. / 225920.};
@@ -71,12 +79,36 @@ struct IterMatrix {
   }
 };
 
+// Feed temperature of an open reactor at integration-local time t: the table's 4-point (cubic) Lagrange interpolant,
+// else the constant. At a spacing of the first time step the interpolation error, O(h^4 T''''), is far below the
+// rounding of the temperature, so the right-hand side sees the feed function itself.
+__device__ __forceinline__ double feed_temperature_at(const IntParams &p, double t)
+{
+  const sf_integrate_params &ip = p.ip;
+  const double *tab = ip.feed_temperature_table;
+  if (!tab) return p.cfg.Tin;
+  const double u = (t - ip.feed_t0) / ip.feed_dt;
+  const int last = ip.feed_points - 1;
+  if (!(u > 0.)) return tab[0];
+  if (u >= (double)last) return tab[last];
+  int i = (int)u;
+  // stencil i-1 .. i+2, shifted inside the table at its ends
+  const int i0 = i < 1 ? 0 : (i + 2 > last ? last - 3 : i - 1);
+  const double x = u - (double)i0;  // position within the stencil, nodes at 0, 1, 2, 3
+  const double x0 = x, x1 = x - 1., x2 = x - 2., x3 = x - 3.;
+  const double w0 = -x1 * x2 * x3 * (1. / 6.), w1 = x0 * x2 * x3 * 0.5, w2 = -x0 * x1 * x3 * 0.5,
+               w3 = x0 * x1 * x2 * (1. / 6.);
+  if (last < 3) return tab[i] + (u - (double)i) * (tab[i + 1] - tab[i]);
+  return w0 * tab[i0] + w1 * tab[i0 + 1] + w2 * tab[i0 + 2] + w3 * tab[i0 + 3];
+}
+
 __device__ __forceinline__ double warp_max(double v)
 {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
+template <bool OPEN>
 __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -118,6 +150,10 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
     for (int i = lane; i < neq; i += 32) y[i] = p.q0[(size_t)r * neq + i];
     __syncwarp();
     const double T0 = y[Tidx];
+    // reactor options with the feed temperature of the current evaluation; t_rhs: time of the most recent
+    // right-hand side, whose feed the next Jacobian uses
+    ReactorCfg cf = p.cfg;
+    double t_rhs = ip.feed_jac_t0;
     double t = 0., dt = ip.first_time_step;
     bool setup = true;
     int count = 0, nsteps = 0, nnewton = 0, njac = 0, nfail = 0, status = 0, attempts = 0;
@@ -130,7 +166,8 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
       if (coerce && t + dt > ip.stop_at_time) dt = ip.stop_at_time - t;
       if (setup) {
         IterMatrix im{A, neq, dt * kGamma};
-        reactor_eval<32, true, kIntegratorUnroll>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, f, im);
+        if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs);
+        reactor_eval<32, true, kIntegratorUnroll, OPEN>(m, b, L, scr, grp, y, pres, cf, p.pg, f, im);
         __syncwarp();
         if (p.prec == 1) {
           for (int e = lane; e < neq * neq; e += 32) LU32[e] = (float)A[e];
@@ -158,12 +195,14 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
         for (int i = lane; i < neq; i += 32) slot[2 + i] = y[i];
       }
       // ---------------- one ESDIRK64 step (methods.py:502-612)
-      reactor_eval<32, false, kIntegratorUnroll>(m, b, L, scr, grp, y, pres, p.cfg, p.pg, k, noj);
+      if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs = t);
+      reactor_eval<32, false, kIntegratorUnroll, OPEN>(m, b, L, scr, grp, y, pres, cf, p.pg, k, noj);
       for (int i = lane; i < neq; i += 32) Y[i] = y[i];
       __syncwarp();
       bool nl_ok = true;
       for (int s = 1; s < 6; ++s) {
         const double *kprev = k + (s - 1) * neq;
+        if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs = t + c_c[s] * dt);
         for (int i = lane; i < neq; i += 32) {
           double pr = 0.;
           for (int j = s - 1; j >= 0; --j) pr += c_a[s][j] * k[j * neq + i];  // a_s,s-1 k_s-1 + ... + a_s1 k_1
@@ -199,7 +238,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
           }
           for (int i = lane; i < neq; i += 32) Y[i] -= x[i];
           __syncwarp();
-          reactor_eval<32, false, kIntegratorUnroll>(m, b, L, scr, grp, Y, pres, p.cfg, p.pg, f, noj);
+          reactor_eval<32, false, kIntegratorUnroll, OPEN>(m, b, L, scr, grp, Y, pres, cf, p.pg, f, noj);
           double nrm = 0.;
           for (int i = lane; i < neq; i += 32) {
             res[i] = dt * (kGamma * f[i] + prior[i]) - (Y[i] - y[i]);
@@ -372,8 +411,14 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
   try {
     if (!mech || !rp || !ip || n < 0 || (n > 0 && (!q0 || !out_q || !out_t || !out_counts || !out_status)))
       throw sf_error(SF_ERR_INVALID_ARGUMENT, "sf_integrate_batch: bad argument");
-    if (rp->open) throw sf_error(SF_ERR_UNSUPPORTED, "open reactors are not on the GPU path");
     if (rp->configuration != 0 && rp->configuration != 1) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad configuration");
+    if (rp->heat_transfer < 0 || rp->heat_transfer > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad heat_transfer");
+    if (rp->open) {
+      if (!rp->inflow_Y || !(rp->tau > 0.))
+        throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs feed mass fractions and a positive mixing time");
+      if (ip->feed_temperature_table ? (ip->feed_points < 2 || !(ip->feed_dt > 0.)) : !(rp->inflow_temperature > 0.))
+        throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs a feed temperature (constant or table)");
+    }
     if (ip->linear_precision != 0 && ip->linear_precision != 1)
       throw sf_error(SF_ERR_INVALID_ARGUMENT, "linear_precision must be 0 or 1");
     if (ip->rates_option < 0 || ip->rates_option > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad rates option");
@@ -401,7 +446,13 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.cfg.hc = rp->h_convection;
     p.cfg.eps = rp->eps_radiation;
     p.cfg.SoV = rp->surface_area_to_volume;
+    p.cfg.open = rp->open ? 1 : 0;
+    p.cfg.tau = rp->tau;
+    p.cfg.rho_in = rp->inflow_density;
+    p.cfg.Tin = rp->inflow_temperature;
+    p.cfg.yin = rp->inflow_Y;
     p.ip = *ip;
+    if (!rp->open) p.ip.feed_temperature_table = nullptr;
     if (p.ip.maximum_time_step_count <= 0) p.ip.maximum_time_step_count = 2147483647;
     p.n = n;
     p.neq = rp->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
@@ -422,10 +473,11 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.per_warp = sh.per_warp;
     p.warps = sh.warps;
     p.gscratch = sh.scratch_bytes ? reinterpret_cast<double *>(static_cast<char *>(workspace) + 256) : nullptr;
-    CUDA_THROW(cudaFuncSetAttribute(integrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+    auto kern = p.cfg.open ? integrate_kernel<true> : integrate_kernel<false>;
+    CUDA_THROW(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_THROW(cudaMemsetAsync(workspace, 0, 256, st));
-    integrate_kernel<<<sh.grid, 32 * sh.warps, sh.smem, st>>>(p);
+    kern<<<sh.grid, 32 * sh.warps, sh.smem, st>>>(p);
     CUDA_THROW(cudaGetLastError());
     return SF_OK;
   } catch (sf_error &e) {

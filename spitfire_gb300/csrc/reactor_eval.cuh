@@ -20,6 +20,9 @@ struct ReactorCfg {
   int heat;           // 0 adiabatic, 1 isothermal, 2 diathermal
   int option;         // rates-sensitivity option
   double Tc, Tr, hc, eps, SoV;
+  int open;           // mass exchange with a feed of temperature Tin, mass fractions yin[ns] (device), density
+  double tau, rho_in, Tin;  // rho_in (isochoric), over the mixing time tau
+  const double *yin;
 };
 
 struct Progs {
@@ -91,14 +94,16 @@ __device__ __forceinline__ double2 reactions_and_gathers(const DevMech &m, const
 
 // Reactor right-hand side (and, with JAC, the analytical Jacobian) of the state qs (neq values, any memory space).
 // rhs receives neq values; jset(row, col, value) receives every Jacobian entry exactly once.
-// U: gather batch (loads in flight per lane); smaller batches use fewer registers.
-template <int G, bool JAC, int U = default_unroll(G), class JSet, class S>
+// U: gather batch (loads in flight per lane); smaller batches use fewer registers. OPEN = false compiles the feed
+// terms of open reactors out (c.open is then ignored).
+template <int G, bool JAC, int U = default_unroll(G), bool OPEN = true, class JSet, class S>
 __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayout &L, S scr,
                              const Group<G> &grp, const double *qs, double pres, const ReactorCfg &c,
                              const Progs &pg, double *rhs, JSet &jset)
 {
   const int ns = m.ns, lane = grp.lane;
   const bool isochoric = c.configuration == 1;
+  const bool open_ = OPEN && c.open;
   const int neq = isochoric ? ns + 1 : ns;
   // ---------------- P0
   double T, rho = 0.;
@@ -140,6 +145,25 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   const double EA = E.x, EB = E.y;
   const double cmix = isochoric ? sums.cpmix - m.Ru / mmw : sums.cpmix;  // cv or cp
   const double cpsens = sums.cpsens;
+  // feed of an open reactor (isochoric_reactor_kernels.cpp:39-154, isobaric_reactor_kernels.cpp:31-168):
+  // fe = sum_i (e_i(Tin) - e_i(T)) yin_i (enthalpies when isobaric), fc = sum_i yin_i cv_i(T) (cp_i)
+  double fe = 0., fc = 0.;
+  if (open_) {
+    const double Tin = c.Tin, lTin = log(Tin), iTin = 1. / Tin;
+    for (int i = lane; i < ns; i += G) {
+      const SpeciesThermo th = species_thermo(m, b, i, Tin, lTin, iTin, false);
+      const double ein = isochoric ? th.h - m.Ru * Tin * b.d[m.d_invmw + i] : th.h;
+      const double yi = c.yin[i];
+      fe += (ein - scr[L.eh + i]) * yi;
+      fc += yi * scr[L.cpv + i];
+    }
+    fe = grp.sum(fe);
+    fc = grp.sum(fc);
+  }
+  // mass-exchange factor of the species and energy equations: rho_in / (tau rho) isochoric, 1 / tau isobaric
+  const double itau = open_ ? 1. / c.tau : 0.;
+  const double mfac = open_ ? (isochoric ? itau * c.rho_in / rho : itau) : 0.;
+  const double mrT = open_ ? fe / cmix * mfac : 0.;  // feed term of the temperature equation
 
   // ---------------- P4: right-hand side and rho/T columns
   double swe = 0., sre = 0., ste = 0., swc = 0.;
@@ -165,10 +189,11 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   if (c.heat == 2)
     qheat = c.SoV / (rho * cmix) * (c.hc * (c.Tc - T) + c.eps * 5.67e-8 * (c.Tr * c.Tr * c.Tr * c.Tr - T * T * T * T));
   const int tix = isochoric ? 1 : 0;  // index of T in the state
-  for (int i = lane; i < ns - 1; i += G) rhs[tix + 1 + i] = scr[L.w + i] * invRho;
+  for (int i = lane; i < ns - 1; i += G)
+    rhs[tix + 1 + i] = scr[L.w + i] * invRho + (open_ ? (c.yin[i] - scr[L.y + i]) * mfac : 0.);
   if (lane == 0) {
-    if (isochoric) rhs[0] = 0.;
-    rhs[tix] = c.heat == 1 ? 0. : rhsT + qheat;
+    if (isochoric) rhs[0] = open_ ? (c.rho_in - rho) * itau : 0.;
+    rhs[tix] = c.heat == 1 ? 0. : (open_ ? rhsT + qheat + mrT : rhsT + qheat);
   }
   if (!JAC) {
     grp.sync();
@@ -180,7 +205,8 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   const double cpv_last = scr[L.cpv + ns - 1];
   if (isochoric) {
     for (int i = lane; i < ns - 1; i += G) {
-      jset(2 + i, 0, invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]));
+      const double mr = open_ ? (c.yin[i] - scr[L.y + i]) * mfac : 0.;
+      jset(2 + i, 0, invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]) - mr * invRho);
       jset(2 + i, 1, invRho * scr[L.ST + i]);
     }
   } else {
@@ -197,10 +223,16 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   for (int k = lane; k < ns; k += G) scr[L.trow + k] = 0.;
   grp.sync();
 
-  // ---------------- P5: Y block (species rows/columns) and T-row sums
+  // ---------------- P5: Y block (species rows/columns) and T-row sums; an open reactor's feed adds -mfac on the
+  // diagonal (rho_in / (tau rho) isochoric, 1 / tau isobaric)
   {
     const int off = isochoric ? 2 : 1;
-    auto yblock = [&](int row, int col, double v) { jset(off + row, off + col, v); };
+    const bool diag = open_;
+    const double dyy = -mfac;
+    auto yblock = [&](int row, int col, double v) {
+      if (diag && row == col) v += dyy;
+      jset(off + row, off + col, v);
+    };
     run_program<G, U>(pg.j, lane, b.d, scr, yblock);
   }
   grp.sync();
@@ -211,12 +243,17 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
     for (int k = lane; k < ns - 1; k += G) {
       const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
       double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
+      if (open_) v += -iC * mrT * (scr[L.cpv + k] - cpv_last);
       if (c.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
       jset(1, 2 + k, v * iso_heat);
     }
-    for (int k = lane; k < neq; k += G) jset(0, k, 0.);
+    for (int k = lane; k < neq; k += G) jset(0, k, (k == 0 && open_) ? -itau : 0.);
     if (lane == 0) {
       double j10 = JTrho, j11 = JTT;
+      if (open_) {
+        j10 += -mrT * invRho;
+        j11 += -iC * (itau * invRho * c.rho_in * fc + cpsens * mrT);
+      }
       if (c.heat == 2) {
         j10 += -qheat / rho;
         j11 += -iC * cpsens * qheat - c.SoV * iRC * (c.hc + 4. * c.eps * 5.67e-8 * T * T * T);
@@ -227,6 +264,7 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   } else {
     const double roT = rho / T, nrm = -rho * mmw;
     double pjr = JTrho, pjt = JTT;
+    if (open_) pjt += -iC * (cpsens * mrT + itau * fc);
     if (c.heat == 2) {
       pjr += -qheat / rho;
       pjt += -iC * cpsens * qheat - c.SoV * iRC * (c.hc + 4. * c.eps * 5.67e-8 * T * T * T);
@@ -236,6 +274,7 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
     for (int k = lane; k < ns - 1; k += G) {
       const double ts = scr[L.trow + k] + b.d[m.d_u + k] * EA + EB;
       double v = -iC * ts - rhsT * (scr[L.cpv + k] - cpv_last) * iC;
+      if (open_) v += -mrT * (scr[L.cpv + k] - cpv_last) * iC;
       if (c.heat == 2) v += iC * qheat * (cpv_last - scr[L.cpv + k]);
       jset(0, 1 + k, v * iso_heat + nrm * b.d[m.d_u + k] * pjr);
     }

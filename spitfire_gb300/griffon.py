@@ -238,15 +238,19 @@ class PyCombustionKernels(GriffonSetters):
         prod_rates_sens[:] = self._np1(S[0])
 
     def _params(self, configuration, p_or_rho, Tin, Yin, tau, Tc, Tr, hc, eps, SoV, heat, open_):
+        yptr = None
         if open_:
-            raise N.NativeError('open reactors are not on the GPU path')
+            # the feed mass fractions live on the device for the call (kept until the next call replaces them;
+            # the reference-shaped methods read their results back, which orders the two)
+            self._feed_Y = self._dev(np.asarray(Yin, dtype=np.float64).reshape(-1))
+            yptr = self._feed_Y.data_ptr()
         if configuration == 'isobaric':
-            return reactor_params('isobaric', int(heat), False, pressure=p_or_rho, inflow_temperature=Tin, tau=tau,
-                                  fluid_temperature=Tc, surface_temperature=Tr, h_convection=hc, eps_radiation=eps,
-                                  surface_area_to_volume=SoV)
-        return reactor_params('isochoric', int(heat), False, inflow_density=p_or_rho, inflow_temperature=Tin, tau=tau,
-                              fluid_temperature=Tc, surface_temperature=Tr, h_convection=hc, eps_radiation=eps,
-                              surface_area_to_volume=SoV)
+            return reactor_params('isobaric', int(heat), bool(open_), pressure=p_or_rho, inflow_temperature=Tin,
+                                  inflow_Y_ptr=yptr, tau=tau, fluid_temperature=Tc, surface_temperature=Tr,
+                                  h_convection=hc, eps_radiation=eps, surface_area_to_volume=SoV)
+        return reactor_params('isochoric', int(heat), bool(open_), inflow_density=p_or_rho, inflow_temperature=Tin,
+                              inflow_Y_ptr=yptr, tau=tau, fluid_temperature=Tc, surface_temperature=Tr,
+                              h_convection=hc, eps_radiation=eps, surface_area_to_volume=SoV)
 
     def reactor_rhs_isobaric(self, state, pressure, Tin, Yin, tau, Tc, Tr, hc, eps, SoV, heat, open_, out):
         P = self._params('isobaric', pressure, Tin, Yin, tau, Tc, Tr, hc, eps, SoV, heat, open_)

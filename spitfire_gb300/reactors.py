@@ -1,14 +1,15 @@
 """Homogeneous reactors on the GPU: batched adaptive ESDIRK64 integration and a drop-in ``HomogeneousReactor``.
 
-``BatchIntegrator`` integrates thousands of closed reactors of one mechanism and configuration in a single
-persistent launch (``sf_integrate_batch``), with the reference's defaults (reactors.py:429-611): first time step
-1e-6, maximum 1e6, PI target error 1e-10, Newton tolerance 1e-12 with weights 1/[1e3 on T], at least 40 steps,
-Jacobian every step. Optionally the launch is captured once in a CUDA graph and replayed.
+``BatchIntegrator`` integrates thousands of reactors of one mechanism, configuration and feed in a single persistent
+launch (``sf_integrate_batch``), with the reference's defaults (reactors.py:429-611): first time step 1e-6, maximum
+1e6, PI target error 1e-10, Newton tolerance 1e-12 with weights 1/[1e3 on T], at least 40 steps, Jacobian every
+step. Closed or open (mass exchange with a feed whose temperature may vary in time), adiabatic, isothermal or
+diathermal. Optionally the launch is captured once in a CUDA graph and replayed; ``run_recorded`` returns every
+accepted step.
 
 ``HomogeneousReactor`` keeps the constructor and the integrate / compute_ignition_delay / integrate_to_steady /
-integrate_to_time methods of ``spitfire.chemistry.reactors.HomogeneousReactor`` for closed reactors; it runs the
-batched integrator with one reactor and returns the first and last states (the GPU path does not record
-trajectories).
+integrate_to_time methods of ``spitfire.chemistry.reactors.HomogeneousReactor`` and returns the same output library
+(every accepted step, or the first and last when ``save_first_and_last_only``).
 """
 
 import ctypes as C
@@ -21,6 +22,10 @@ from ._desc import SfIntegrateParams, reactor_params
 STATUS_NAMES = {0: 'running', 1: 'done', 2: 'ignited', 3: 'steady', 4: 'max_steps', 5: 'nan', 6: 'no_ignition',
                 7: 'record_full'}
 
+# feed temperature tables: points per unit of the first time step over the horizon, and the bounds on their number
+FEED_TABLE_MIN_POINTS = 1024
+FEED_TABLE_MAX_POINTS = 1 << 21
+
 
 def _torch():
     import torch
@@ -28,23 +33,75 @@ def _torch():
 
 
 class BatchIntegrator:
+    """Batched ESDIRK64 integration of reactors that share a mechanism, configuration, heat transfer and feed.
+
+    heat_transfer 'diathermal' takes convection_temperature, radiation_temperature, convection_coefficient,
+    radiative_emissivity and surface_area_to_volume (constants). mass_transfer 'open' takes mixing_tau, the feed
+    mass fractions feed_mass_fractions (ns values), feed_density (isochoric) and feed_temperature: a number, or a
+    function of time evaluated on a table that the device interpolates linearly (reactors.py:335-338 evaluates it at
+    each right-hand side; the table spacing is the first time step, at most FEED_TABLE_MAX_POINTS points)."""
+
     def __init__(self, mech, configuration='isobaric', heat_transfer='adiabatic', pressure=101325.,
-                 linear_precision=0, refine_sweeps=2, rates_option=0):
+                 linear_precision=0, refine_sweeps=2, rates_option=0, mass_transfer='closed', mixing_tau=None,
+                 feed_temperature=None, feed_mass_fractions=None, feed_density=None, convection_temperature=None,
+                 radiation_temperature=None, convection_coefficient=None, radiative_emissivity=None,
+                 surface_area_to_volume=None):
         if configuration not in ('isobaric', 'isochoric'):
             raise ValueError('configuration must be isobaric or isochoric')
+        if mass_transfer not in ('closed', 'open'):
+            raise ValueError('mass_transfer must be closed or open')
         self.mech = mech
         self.g = mech.griffon
         self.configuration = configuration
-        self.params = reactor_params(configuration, heat_transfer, pressure=pressure)
+        self.open = mass_transfer == 'open'
+        kw = {}
+        if heat_transfer == 'diathermal':
+            for name, v in (('convection_temperature', convection_temperature),
+                            ('radiation_temperature', radiation_temperature),
+                            ('convection_coefficient', convection_coefficient),
+                            ('radiative_emissivity', radiative_emissivity),
+                            ('surface_area_to_volume', surface_area_to_volume)):
+                if v is None:
+                    raise ValueError(f'diathermal reactors need {name}')
+                if callable(v):
+                    raise NotImplementedError(f'a time-dependent {name} is not on the GPU path')
+            kw = dict(fluid_temperature=convection_temperature, surface_temperature=radiation_temperature,
+                      h_convection=convection_coefficient, eps_radiation=radiative_emissivity,
+                      surface_area_to_volume=surface_area_to_volume)
+        self._feed_T = None
+        self._feed_Y = None
+        if self.open:
+            if mixing_tau is None or feed_temperature is None or feed_mass_fractions is None:
+                raise ValueError('open reactors need mixing_tau, feed_temperature and feed_mass_fractions')
+            if configuration == 'isochoric' and feed_density is None:
+                raise ValueError('open isochoric reactors need feed_density')
+            for name, v in (('mixing_tau', mixing_tau), ('feed_mass_fractions', feed_mass_fractions),
+                            ('feed_density', feed_density)):
+                if callable(v):
+                    raise NotImplementedError(f'a time-dependent {name} is not on the GPU path')
+            self._feed_Y = self.g._dev(np.asarray(feed_mass_fractions, dtype=np.float64).reshape(-1))
+            if self._feed_Y.numel() != mech.n_species:
+                raise ValueError('feed_mass_fractions needs one value per species')
+            self._feed_T = feed_temperature
+            kw.update(inflow_temperature=300. if callable(feed_temperature) else float(feed_temperature),
+                      inflow_density=float(feed_density or 0.), tau=float(mixing_tau),
+                      inflow_Y_ptr=self._feed_Y.data_ptr())
+        self.params = reactor_params(configuration, heat_transfer, self.open, pressure=pressure, **kw)
         self.linear_precision = linear_precision
         self.refine_sweeps = refine_sweeps
         self.rates_option = rates_option
         self._graph = None
+        self._table = None
 
     def controls(self, stop_at_time=None, delta_temperature_ignition=None, stop_at_steady=None,
                  first_time_step=1.e-6, max_time_step=1.e6, transient_tolerance=1.e-10, nonlinear_tolerance=1.e-12,
                  minimum_time_step_count=40, maximum_time_step_count=None, max_nonlinear_iter=20,
-                 maximum_steps_per_jacobian=1, minimum_allowable_residual=1.e-12, max_attempts=500000):
+                 maximum_steps_per_jacobian=1, minimum_allowable_residual=1.e-12, max_attempts=500000,
+                 time_offset=0., first_jacobian_feed_time=0., feed_horizon=1.):
+        """Integration controls. time_offset: the reactors' current time (a feed function is evaluated at
+        time_offset + integration time). first_jacobian_feed_time: the absolute time whose feed the first Jacobian
+        takes (0 for a new reference reactor). feed_horizon: integration time a feed table covers when stop_at_time
+        is not given."""
         ip = SfIntegrateParams()
         ip.first_time_step = first_time_step
         ip.max_time_step = max_time_step
@@ -62,6 +119,25 @@ class BatchIntegrator:
         ip.refine_sweeps = self.refine_sweeps
         ip.rates_option = self.rates_option
         ip.max_attempts = max_attempts
+        ip.feed_jac_t0 = float(first_jacobian_feed_time) - float(time_offset)
+        if self.open and callable(self._feed_T):
+            horizon = stop_at_time if stop_at_time is not None else feed_horizon
+            t_lo = min(0., ip.feed_jac_t0)
+            n = int(min(FEED_TABLE_MAX_POINTS,
+                        max(FEED_TABLE_MIN_POINTS, np.ceil((horizon - t_lo) / first_time_step) + 1)))
+            tl = np.linspace(t_lo, horizon, n)
+            ta = tl + float(time_offset)
+            try:
+                vals = np.asarray(self._feed_T(ta), dtype=np.float64)
+                if vals.shape != ta.shape:
+                    raise ValueError
+            except Exception:
+                vals = np.array([float(self._feed_T(x)) for x in ta])
+            self._table = self.g._dev(vals)
+            ip.feed_temperature_table = C.cast(C.c_void_p(self._table.data_ptr()), C.POINTER(C.c_double))
+            ip.feed_points = n
+            ip.feed_t0 = float(tl[0])
+            ip.feed_dt = float(tl[1] - tl[0])
         return ip
 
     def allocate(self, n):
@@ -77,13 +153,20 @@ class BatchIntegrator:
     def workspace_bytes(self, n):
         return int(N.load().sf_integrate_workspace_size(self.g.handle, C.byref(self.params), int(n)))
 
-    def launch(self, q0, pressures, out, ip):
+    def launch(self, q0, pressures, out, ip, record=None):
         L = N.load()
         n = q0.shape[0]
-        N.check(L.sf_integrate_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0),
-                                     N.ptr(pressures), N.ptr(out['q']), N.ptr(out['t']), N.ptr(out['counts']),
-                                     N.ptr(out['status']), N.ptr(out['ws']), out['ws'].numel() * 4,
-                                     N.stream_handle()))
+        if record is None:
+            N.check(L.sf_integrate_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0),
+                                         N.ptr(pressures), N.ptr(out['q']), N.ptr(out['t']), N.ptr(out['counts']),
+                                         N.ptr(out['status']), N.ptr(out['ws']), out['ws'].numel() * 4,
+                                         N.stream_handle()))
+        else:
+            N.check(L.sf_integrate_record_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0),
+                                                N.ptr(pressures), N.ptr(out['q']), N.ptr(out['t']),
+                                                N.ptr(out['counts']), N.ptr(out['status']), N.ptr(out['ws']),
+                                                out['ws'].numel() * 4, N.ptr(record), record.shape[1],
+                                                N.stream_handle()))
 
     def run(self, q0, pressures=None, graph=False, **controls):
         """Integrate every row of q0 (isobaric [T, Y_0..Y_{ns-2}] or isochoric [rho, T, Y...]).
@@ -108,7 +191,40 @@ class BatchIntegrator:
         with torch.cuda.graph(g):
             self.launch(q0, pr, out, ip)
         g.replay()
-        self._graph = (g, q0, pr, out, ip)
+        self._graph = (g, q0, pr, out, ip, self._table)
+        return out
+
+    def run_recorded(self, q0, pressures=None, capacity=1024, **controls):
+        """run() that also returns every accepted step: 'times' [n, steps + 1] and 'states' [n, steps + 1, neq]
+        (host arrays, padded past each reactor's own step count with its final time and state), 'steps' [n].
+        The record grows until every reactor fits."""
+        torch = _torch()
+        q0 = self.g._dev(q0)
+        pr = self.g._dev(pressures) if pressures is not None else None
+        ip = self.controls(**controls)
+        n, neq = q0.shape
+        out = self.allocate(n)
+        while True:
+            rec = torch.empty((n, capacity, 2 + 6 * neq), dtype=torch.float64, device=q0.device)
+            self.launch(q0, pr, out, ip, record=rec)
+            if not bool((out['status'] == 7).any()):
+                break
+            del rec
+            capacity *= 2
+        steps = out['counts'][:, 0].cpu().numpy()
+        smax = int(steps.max()) if n else 0
+        r = rec[:, :smax].cpu().numpy()
+        tf = out['t'].cpu().numpy()
+        qf = out['q'].cpu().numpy()
+        times = np.empty((n, smax + 1))
+        states = np.empty((n, smax + 1, neq))
+        for i in range(n):
+            k = int(steps[i])
+            times[i, :k] = r[i, :k, 0]
+            states[i, :k] = r[i, :k, 2:2 + neq]
+            times[i, k:] = tf[i]
+            states[i, k:] = qf[i]
+        out.update(times=times, states=states, steps=steps)
         return out
 
     def replay(self):
@@ -119,22 +235,67 @@ class BatchIntegrator:
         return self._graph[3]
 
 
+# surface-to-volume ratio of a reactor shape from its characteristic length a or its volume v (the geometry of each
+# solid; the reference's table is reactors.py:85-97)
+_SOV = {'cube': (lambda a: 6. / a, lambda v: 6. / np.cbrt(v)),
+        'sphere': (lambda a: 3. / a, lambda v: 3. / np.cbrt(3. * v / (4. * np.pi))),
+        'capsule': (lambda a: 12. / (5. * a), lambda v: 12. / (5. * np.cbrt(3. * v / (10. * np.pi)))),
+        'tetrahedron': (lambda a: 6. * np.sqrt(6.) / a, lambda v: 6. * np.sqrt(6.) / np.cbrt(12. * v / np.sqrt(2.))),
+        'octahedron': (lambda a: 3. * np.sqrt(6.) / a, lambda v: 3. * np.sqrt(6.) / np.cbrt(3. * v / np.sqrt(2.))),
+        'icosahedron': (lambda a: 12. * np.sqrt(3.) / ((3. + np.sqrt(5.)) * a),
+                        lambda v: 12. * np.sqrt(3.) / ((3. + np.sqrt(5.)) *
+                                                       np.cbrt(12. * v / 5. / (3. + np.sqrt(5.)))))}
+
+
+def _surface_to_volume(shape_dimension_dict):
+    d = shape_dimension_dict
+    if d is None or 'shape' not in d:
+        raise ValueError('diathermal reactors need shape_dimension_dict with a shape key')
+    if d['shape'] not in _SOV:
+        raise ValueError(f'unknown reactor shape {d["shape"]!r}; supported: {sorted(_SOV)}')
+    if ('char. length' in d) == ('volume' in d):
+        raise ValueError('shape_dimension_dict needs exactly one of the char. length or volume keys')
+    l2s, v2s = _SOV[d['shape']]
+    return float(l2s(d['char. length'])) if 'char. length' in d else float(v2s(d['volume']))
+
+
 class HomogeneousReactor:
-    """Drop-in for spitfire.chemistry.reactors.HomogeneousReactor (closed reactors; reactors.py:27-794)."""
+    """Drop-in for spitfire.chemistry.reactors.HomogeneousReactor (reactors.py:27-794): closed or open (mass
+    exchange with a feed), adiabatic, isothermal or diathermal, isobaric or isochoric. Time-dependent parameters are
+    supported for the feed temperature (tabulated for the device); the other parameters are constants."""
 
     def __init__(self, mech_spec, initial_mixture, configuration, heat_transfer, mass_transfer,
                  convection_temperature=None, radiation_temperature=None, convection_coefficient=None,
                  radiative_emissivity=None, shape_dimension_dict=None, mixing_tau=None, feed_temperature=None,
                  feed_mass_fractions=None, feed_density=None, rates_sensitivity_type='dense',
                  sensitivity_transform_type='exact', initial_time=0.):
-        if mass_transfer != 'closed':
-            raise NotImplementedError('open reactors are not on the GPU path')
-        if heat_transfer not in ('adiabatic', 'isothermal'):
-            raise NotImplementedError('the GPU integrator covers adiabatic and isothermal reactors')
+        configuration = configuration.lower()
+        heat_transfer = heat_transfer.lower()
+        mass_transfer = mass_transfer.lower()
+        if configuration not in ('isobaric', 'isochoric'):
+            raise ValueError(f'bad configuration {configuration!r}; use isobaric or isochoric')
+        if heat_transfer not in ('adiabatic', 'isothermal', 'diathermal'):
+            raise ValueError(f'bad heat transfer {heat_transfer!r}')
+        if mass_transfer not in ('closed', 'open'):
+            raise ValueError(f'bad mass transfer {mass_transfer!r}')
         self._mechanism = mech_spec
         self._configuration = configuration
         self._heat_transfer = heat_transfer
+        self._mass_transfer = mass_transfer
         self._rates_sensitivity_option = {'dense': 0, 'no-TBAF': 1, 'sparse': 2}[rates_sensitivity_type]
+        if sensitivity_transform_type != 'exact':
+            raise ValueError('sensitivity_transform_type must be exact')
+        self._options = dict(heat_transfer=heat_transfer, mass_transfer=mass_transfer)
+        if heat_transfer == 'diathermal':
+            self._options.update(convection_temperature=convection_temperature,
+                                 radiation_temperature=radiation_temperature,
+                                 convection_coefficient=convection_coefficient,
+                                 radiative_emissivity=radiative_emissivity,
+                                 surface_area_to_volume=_surface_to_volume(shape_dimension_dict))
+        if mass_transfer == 'open':
+            self._options.update(mixing_tau=mixing_tau, feed_temperature=feed_temperature,
+                                 feed_mass_fractions=feed_mass_fractions,
+                                 feed_density=feed_density if configuration == 'isochoric' else None)
         self._initial_pressure = initial_mixture.P
         self._initial_temperature = initial_mixture.T
         self._initial_mass_fractions = np.array(initial_mixture.Y)
@@ -148,7 +309,9 @@ class HomogeneousReactor:
             self._initial_state = np.hstack([[initial_mixture.density, initial_mixture.T],
                                              self._initial_mass_fractions[:-1]])
         self._current_state = self._initial_state.copy()
+        self._initial_time = float(initial_time)
         self._current_time = float(initial_time)
+        self._integrations = 0
         self._last_info = None
 
     @property
@@ -160,12 +323,37 @@ class HomogeneousReactor:
         return self._current_state.copy()
 
     @property
+    def initial_time(self):
+        return self._initial_time
+
+    @property
     def current_time(self):
         return self._current_time
 
     @property
+    def initial_temperature(self):
+        return self._initial_temperature
+
+    @property
     def current_temperature(self):
         return self._current_state[self._temperature_index]
+
+    @property
+    def initial_pressure(self):
+        return self._initial_pressure
+
+    @property
+    def initial_mass_fractions(self):
+        return self._initial_mass_fractions.copy()
+
+    @property
+    def current_mass_fractions(self):
+        y = self._current_state[self._temperature_index + 1:]
+        return np.hstack([y, 1. - y.sum()])
+
+    @property
+    def n_species(self):
+        return self._mechanism.n_species
 
     @property
     def n_equations(self):
@@ -175,10 +363,23 @@ class HomogeneousReactor:
     def last_counts(self):
         return self._last_info
 
-    def _integrate(self, **controls):
-        bi = BatchIntegrator(self._mechanism, self._configuration, self._heat_transfer,
-                             pressure=self._initial_pressure, rates_option=self._rates_sensitivity_option)
-        out = bi.run(self._current_state[None, :], **controls)
+    @classmethod
+    def get_supported_reactor_shapes(cls):
+        return _SOV.keys()
+
+    def _integrate(self, save_first_and_last_only=False, **controls):
+        bi = BatchIntegrator(self._mechanism, self._configuration, pressure=self._initial_pressure,
+                             rates_option=self._rates_sensitivity_option, **self._options)
+        # a new reference reactor's first Jacobian takes the feed at t = 0 (reactors.py:279-282); a continued one
+        # the feed of its last right-hand side, at the current time
+        controls['time_offset'] = self._current_time
+        controls['first_jacobian_feed_time'] = 0. if self._integrations == 0 else self._current_time
+        q0 = self._current_state[None, :]
+        t0 = self._current_time
+        if save_first_and_last_only:
+            out = bi.run(q0, **controls)
+        else:
+            out = bi.run_recorded(q0, **controls)
         st = int(out['status'][0])
         if st == 6:
             raise ValueError('From compute_ignition_delay(): residual < minimum allowable value, suggesting that '
@@ -186,33 +387,45 @@ class HomogeneousReactor:
         q = out['q'][0].cpu().numpy()
         self._last_info = dict(zip(['steps', 'newton_iters', 'jac_setups', 'failed_steps'],
                                    out['counts'][0].cpu().numpy().tolist()), status=STATUS_NAMES.get(st, st))
-        t_end = float(out['t'][0]) + self._current_time
-        t0 = self._current_time
+        t_end = float(out['t'][0]) + t0
+        if save_first_and_last_only:
+            times = np.array([t_end])
+            states = q[None, :]
+        else:
+            k = int(out['steps'][0])
+            times = out['times'][0, :k + 1] + t0
+            states = out['states'][0, :k + 1]
         self._current_state = q
         self._current_time = t_end
+        self._integrations += 1
         from .library import Dimension, Library
-        lib = Library(Dimension('time', np.array([t0, t_end])))
-        states = np.vstack([self._initial_state if t0 == 0. else q, q])
+        lib = Library(Dimension('time', times))
         names = self._mechanism.species_names
         Tidx = self._temperature_index
-        lib['temperature'] = states[:, Tidx]
+        lib['temperature'] = states[:, Tidx].copy()
         if self._configuration == 'isochoric':
-            lib['density'] = states[:, 0]
+            lib['density'] = states[:, 0].copy()
         else:
-            lib['pressure'] = np.full(2, self._initial_pressure)
-        last = np.ones(2)
+            lib['pressure'] = np.full(times.size, self._initial_pressure)
+        last = np.ones(times.size)
         for i, s in enumerate(names[:-1]):
-            lib['mass fraction ' + s] = states[:, Tidx + 1 + i]
+            lib['mass fraction ' + s] = states[:, Tidx + 1 + i].copy()
             last -= states[:, Tidx + 1 + i]
         lib['mass fraction ' + names[-1]] = last
         return lib
 
-    def integrate(self, stop_at_time=None, stop_at_steady=None, first_time_step=1.e-6, max_time_step=1.e6,
-                  minimum_time_step_count=40, transient_tolerance=1.e-10, maximum_steps_per_jacobian=1,
-                  nonlinear_solve_tolerance=1.e-12, **kwargs):
-        return self._integrate(stop_at_time=stop_at_time, stop_at_steady=stop_at_steady,
-                               first_time_step=first_time_step, max_time_step=max_time_step,
-                               minimum_time_step_count=minimum_time_step_count,
+    def integrate(self, stop_at_time=None, stop_at_steady=None, stop_criteria=None, first_time_step=1.e-6,
+                  max_time_step=1.e6, minimum_time_step_count=40, transient_tolerance=1.e-10, write_log=False,
+                  log_rate=100, maximum_steps_per_jacobian=1, nonlinear_solve_tolerance=1.e-12,
+                  linear_solver='lapack', plot=None, save_first_and_last_only=False, **kwargs):
+        """reactors.py:429-678. A stop_at_time of the reference is an absolute time; stop_criteria callables are
+        not on the GPU path (integrate_to_steady and compute_ignition_delay are)."""
+        if stop_criteria is not None:
+            raise NotImplementedError('stop_criteria callables are not on the GPU path')
+        return self._integrate(save_first_and_last_only=save_first_and_last_only,
+                               stop_at_time=None if stop_at_time is None else stop_at_time - self._current_time,
+                               stop_at_steady=stop_at_steady, first_time_step=first_time_step,
+                               max_time_step=max_time_step, minimum_time_step_count=minimum_time_step_count,
                                transient_tolerance=transient_tolerance,
                                maximum_steps_per_jacobian=maximum_steps_per_jacobian,
                                nonlinear_tolerance=nonlinear_solve_tolerance)
@@ -228,13 +441,16 @@ class HomogeneousReactor:
         if self._heat_transfer == 'isothermal':
             raise ValueError('compute_ignition_delay() called on an isothermal reactor! This is not currently '
                              'supported!')
-        lib = self._integrate(delta_temperature_ignition=delta_temperature_ignition,
+        lib = self._integrate(save_first_and_last_only=not return_solution,
+                              delta_temperature_ignition=delta_temperature_ignition,
                               minimum_allowable_residual=minimum_allowable_residual,
                               first_time_step=kwargs.get('first_time_step', 1.e-6),
                               max_time_step=kwargs.get('max_time_step', 1.e6),
                               minimum_time_step_count=kwargs.get('minimum_time_step_count', 40),
                               transient_tolerance=kwargs.get('transient_tolerance', 1.e-10),
                               nonlinear_tolerance=kwargs.get('nonlinear_solve_tolerance', 1.e-12),
-                              stop_at_time=kwargs.get('stop_at_time'))
+                              maximum_steps_per_jacobian=kwargs.get('maximum_steps_per_jacobian', 1),
+                              stop_at_time=None if kwargs.get('stop_at_time') is None
+                              else kwargs['stop_at_time'] - self._current_time)
         tau = self._current_time
         return (tau, lib) if return_solution else tau

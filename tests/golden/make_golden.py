@@ -9,12 +9,16 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
                        HomogeneousReactor.compute_ignition_delay (reference odesolve + ESDIRK64 + Newton + PI)
   h2_mech_data.json    the Cantera-converted mech_data embedded in tests/tabulation/adiabatic_slfm/gold.pkl
   closed_reactor_gold.npz  the reference's stored closed-reactor trajectories (tests/reactor/closed_reactors/gold.pkl)
+  open_kernels_<mech>.npz  seeded states with a feed and the reference Griffon's open-reactor (mass exchange)
+                       right-hand sides and Jacobians, isochoric and isobaric, adiabatic / isothermal / diathermal
+  open_reactor_gold.npz    the reference's stored open-reactor trajectory under an oscillating feed temperature
+                       (tests/reactor/oscillating_feed_temperature/gold.pkl)
   flamelet_ref.npz     reference Flamelet (flamelet.py) residuals, BTDDOD Jacobians (plain, scaled, with eigenvalue
                        bounds), block-Thomas solves and matvecs, and steady Newton / psitc solutions with iteration
                        counts, for an H2 and a GRI-3.0 flamelet started from a Burke-Schumann profile
   adiabatic_slfm_gold.npz  temperature and mass fractions of tests/tabulation/adiabatic_slfm/gold.pkl
 
-Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets]
+Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open]
 """
 import json
 import os
@@ -75,6 +79,52 @@ def kernels():
         np.savez_compressed(os.path.join(HERE, f'kernels_{name}.npz'), T=T, p=p, Y=Y, rho=rho, w=w, S=S, qiv=qiv,
                             qib=qib, jac_rhs_iv=riv, Jiv=Jiv, rhs_iv=riv_rhs, jac_rhs_ib=rib, Jib=Jib, rhs_ib=rib_rhs)
         print('kernels', name, n)
+
+
+OPEN_HEAT = {'adiabatic': 0, 'isothermal': 1, 'diathermal': 2}
+# convection / radiation parameters of the diathermal cases: Tc, Tr, h, eps, surface-to-volume
+OPEN_DIATHERMAL = (600., 900., 50., 0.3, 20.)
+
+
+def open_kernels():
+    import ref_harness as rh
+    for fname, phase, name, n in [('h2-burke.yaml', 'h2-burke', 'h2-burke', 12),
+                                  ('methane-gri30.yaml', 'methane-gri30', 'methane-gri30', 4)]:
+        ref = rh.ReferenceMechanism(os.path.join(MECHS, fname), phase)
+        g = ref.griffon
+        ns = ref.n_species
+        T, p, Y, rho = seeded_states(ref, n, 4343)
+        rng = np.random.default_rng(4344)
+        Tin = rng.uniform(300., 1500., n)
+        Yin = rng.dirichlet(0.5 * np.ones(ns), n)
+        tau = np.exp(rng.uniform(np.log(1.e-6), np.log(1.e-2), n))
+        rhoin = rho * rng.uniform(0.5, 2., n)
+        qiv = np.hstack([rho[:, None], T[:, None], Y[:, :-1]])
+        qib = np.hstack([T[:, None], Y[:, :-1]])
+        arrs = dict(T=T, p=p, Y=Y, rho=rho, Tin=Tin, Yin=Yin, tau=tau, rhoin=rhoin, qiv=qiv, qib=qib)
+        Tc, Tr, hc, eps, sov = OPEN_DIATHERMAL
+        for heat, ho in OPEN_HEAT.items():
+            riv, Jiv = np.zeros((n, ns + 1)), np.zeros((n, (ns + 1) ** 2))
+            rib, Jib = np.zeros((n, ns)), np.zeros((n, ns * ns))
+            riv_r, rib_r = np.zeros((n, ns + 1)), np.zeros((n, ns))
+            for i in range(n):
+                g.reactor_rhs_isochoric(qiv[i], rhoin[i], Tin[i], Yin[i], tau[i], Tc, Tr, hc, eps, sov, ho, True,
+                                        riv_r[i])
+                g.reactor_jac_isochoric(qiv[i], rhoin[i], Tin[i], Yin[i], tau[i], Tc, Tr, hc, eps, sov, ho, True, 0,
+                                        riv[i], Jiv[i])
+                g.reactor_rhs_isobaric(qib[i], p[i], Tin[i], Yin[i], tau[i], Tc, Tr, hc, eps, sov, ho, True,
+                                       rib_r[i])
+                g.reactor_jac_isobaric(qib[i], p[i], Tin[i], Yin[i], tau[i], Tc, Tr, hc, eps, sov, ho, True, 0, 0,
+                                       rib[i], Jib[i])
+            arrs.update({f'{heat}_rhs_iv': riv_r, f'{heat}_jac_rhs_iv': riv, f'{heat}_Jiv': Jiv,
+                         f'{heat}_rhs_ib': rib_r, f'{heat}_jac_rhs_ib': rib, f'{heat}_Jib': Jib})
+        np.savez_compressed(os.path.join(HERE, f'open_kernels_{name}.npz'), **arrs)
+        print('open kernels', name, n)
+    t, T, Y = pickle.load(open(os.path.join(REF, 'tests', 'reactor', 'oscillating_feed_temperature', 'gold.pkl'),
+                               'rb'))
+    np.savez_compressed(os.path.join(HERE, 'open_reactor_gold.npz'), t=np.asarray(t), T=np.asarray(T),
+                        Y=np.asarray(Y))
+    print('open reactor gold', np.asarray(t).shape)
 
 
 IGNITION_CASES = [
@@ -268,3 +318,5 @@ if __name__ == '__main__':
         kernels()
     if 'ignition' in what:
         ignition()
+    if 'open' in what:
+        open_kernels()

@@ -131,3 +131,99 @@ def test_autotuned_shapes_do_not_change_results(cuda):
         assert abs(out['t'][i].item() - r['t']) / r['t'] <= 1e-6
     for k in AT.KNOBS:
         AT.set_tuning(spec, k, 0)
+
+
+def _h2_air_mix(spec, T):
+    air = spec.stream(stp_air=True)
+    fuel = spec.stream('X', 'H2:1')
+    mix = spec.mix_for_equivalence_ratio(1.0, fuel, air)
+    mix.TP = T, 101325.
+    return mix
+
+
+@pytest.mark.parametrize('key', ['cp_adiabatic', 'cp_isothermal', 'cv_adiabatic', 'cv_isothermal'])
+def test_drop_in_reactor_trajectories_match_closed_gold(cuda, key):
+    """tests/reactor/closed_reactors: HomogeneousReactor(...).integrate_to_steady() for the four closed reactors,
+    every accepted step against the reference's stored trajectory under its own test's tolerances (rtol 1e-4,
+    atol 1e-8 on t, T and Y) and step for step."""
+    from spitfire_gb300.reactors import HomogeneousReactor
+    g = np.load(os.path.join(GOLD, 'closed_reactor_gold.npz'))
+    spec, og = pair('h2-burke')
+    conf = 'isobaric' if key.startswith('cp') else 'isochoric'
+    heat = key.split('_')[1]
+    r = HomogeneousReactor(spec, _h2_air_mix(spec, 1200.), conf, heat, 'closed')
+    out = r.integrate_to_steady()
+    t, T = out.time_values, out['temperature']
+    Y = np.array([out['mass fraction ' + s] for s in spec.species_names])
+    assert t.size == g[key + '_t'].size, (t.size, g[key + '_t'].size)
+    np.testing.assert_allclose(t, g[key + '_t'], rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(T, g[key + '_T'], rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(Y, g[key + '_Y'], rtol=1e-4, atol=1e-8)
+
+
+def test_open_reactor_oscillating_feed_matches_gold(cuda):
+    """tests/reactor/oscillating_feed_temperature: an open isobaric H2/air reactor (mixing time 1e-5 s) whose feed
+    temperature is 800 + 400 sin(2 pi 10 t), integrated to 0.1 s through the drop-in reactor; every step against
+    the reference's stored trajectory (rtol 1e-3, atol 1e-8, the reference test's tolerances) and the step count
+    against the oracle's."""
+    import integrate as I
+    from spitfire_gb300.reactors import HomogeneousReactor
+    from test_oracle_golden import oscillating_feed_case
+    g = np.load(os.path.join(GOLD, 'open_reactor_gold.npz'))
+    spec, og = pair('h2-burke')
+    mix, feed_T = oscillating_feed_case(spec)
+    feed = spec.copy_stream(mix)
+    r = HomogeneousReactor(spec, mix, configuration='isobaric', heat_transfer='adiabatic', mass_transfer='open',
+                           mixing_tau=1.e-5, feed_temperature=feed_T, feed_mass_fractions=feed.Y)
+    out = r.integrate_to_time(0.1, transient_tolerance=1.e-10, write_log=False, log_rate=200)
+    t, T = out.time_values, out['temperature']
+    Y = np.array([out['mass fraction ' + s] for s in spec.species_names])
+    np.testing.assert_allclose(t, g['t'], rtol=1e-3, atol=1e-8)
+    np.testing.assert_allclose(T, g['T'], rtol=1e-3, atol=1e-8)
+    np.testing.assert_allclose(Y, g['Y'], rtol=1e-3, atol=1e-8)
+    Y0 = np.array(mix.Y)
+    ro = I.integrate(I.OpenReactorProblem(og, 'isobaric', feed_T, Y0, 1.e-5), np.hstack([[mix.T], Y0[:-1]]),
+                     stop_at_time=0.1)
+    assert abs(r.last_counts['steps'] - ro['steps']) <= 2, (r.last_counts, ro['steps'])
+
+
+@pytest.mark.parametrize('configuration', ['isobaric', 'isochoric'])
+@pytest.mark.parametrize('heat', ['adiabatic', 'diathermal'])
+def test_open_reactor_batch_matches_oracle(cuda, configuration, heat):
+    """A batch of open GRI-3.0 reactors with a constant feed (and, diathermal, convection and radiation) against
+    the oracle integrator reactor by reactor: status and accepted steps equal, final state within 1e-6."""
+    import integrate as I
+    import oracle as orc
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec, og = pair('methane-gri30')
+    n = 6
+    d = W.ignition_batch(spec, n, seed=91, T_range=(1100., 1400.))
+    ns = spec.n_species
+    yin = np.array(d['q0'][0, 1:].tolist() + [1. - d['q0'][0, 1:].sum()])
+    Tin, tau = 900., 2.e-3
+    q0 = d['q0']
+    if configuration == 'isochoric':
+        mw = spec.molecular_weights
+        Yf = np.hstack([q0[:, 1:], 1. - q0[:, 1:].sum(1, keepdims=True)])
+        rho = 101325. / (8314.46261815324 * q0[:, 0] * (Yf / mw).sum(1))
+        q0 = np.hstack([rho[:, None], q0])
+    rho_in = 0.4
+    dia = dict(convection_temperature=500., radiation_temperature=600., convection_coefficient=20.,
+               radiative_emissivity=0.5, surface_area_to_volume=30.) if heat == 'diathermal' else {}
+    bi = BatchIntegrator(spec, configuration, heat, pressure=101325., mass_transfer='open', mixing_tau=tau,
+                         feed_temperature=Tin, feed_mass_fractions=yin, feed_density=rho_in, **dia)
+    out = bi.run(q0, stop_at_time=5.e-3)
+    qg, st, cnt = out['q'].cpu().numpy(), out['status'].cpu().numpy(), out['counts'].cpu().numpy()
+    for i in range(n):
+        prob = I.OpenReactorProblem(og, configuration, Tin, yin, tau, pressure=101325.,
+                                    heat='diathermal' if dia else 'adiabatic', feed_density=rho_in)
+        if dia:
+            prob.P.fluid_temperature, prob.P.surface_temperature = 500., 600.
+            prob.P.h_convection, prob.P.eps_radiation, prob.P.surface_area_to_volume = 20., 0.5, 30.
+        r = I.integrate(prob, q0[i], stop_at_time=5.e-3)
+        assert st[i] == r['status'], i
+        assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
+        assert np.max(np.abs(qg[i] - r['state']) / np.maximum(np.abs(r['state']), 1e-3)) <= 1e-6, i
+    assert spec.griffon.device_status() == 0
+    del orc, ns

@@ -224,3 +224,42 @@ def test_thread_per_state_grid_stride(cuda, name):
         _tps_check(spec, og, d, ('adiabatic',), rates=name == 'methane-gri30')
     finally:
         _tps_off(spec)
+
+
+@pytest.mark.parametrize('name', ['h2-burke', 'methane-gri30', 'unit-rev_troe4_withN_withNTB', 'unit-methane-lu30'])
+@pytest.mark.parametrize('configuration', ['isochoric', 'isobaric'])
+@pytest.mark.parametrize('heat', ['adiabatic', 'isothermal', 'diathermal'])
+@pytest.mark.parametrize('group', [0, 1])
+def test_open_reactor_rhs_jac(cuda, name, configuration, heat, group):
+    """Open (mass-exchange) reactors: feed temperature, mass fractions (a device array), mixing time and feed density,
+    with the lane-group and thread-per-state kernels."""
+    import oracle as orc
+    import torch
+    from spitfire_gb300 import autotune as AT
+    spec, og = pair(name)
+    g = spec.griffon
+    d = random_states(spec, 70, 31)
+    q = W.isochoric_state(d) if configuration == 'isochoric' else W.isobaric_state(d)
+    neq = q.shape[1]
+    rng = np.random.default_rng(32)
+    yin = rng.dirichlet(0.5 * np.ones(spec.n_species))
+    yin_d = torch.tensor(yin, dtype=torch.float64, device='cuda')
+    kw = dict(pressure=101325., inflow_density=0.7, inflow_temperature=650., tau=3.e-4, fluid_temperature=600.,
+              surface_temperature=900., h_convection=50., eps_radiation=0.3, surface_area_to_volume=20.)
+    P = reactor_params(configuration, heat, True, inflow_Y_ptr=yin_d.data_ptr(), **kw)
+    Po = reactor_params(configuration, heat, True, **kw)
+    Po.inflow_Y = orc._p(yin)
+    pres = d['p'] if configuration == 'isobaric' else None
+    try:
+        if group:
+            AT.set_tuning(spec, 'group_rhs', 1)
+            AT.set_tuning(spec, 'group_jac', 1)
+        rhs = gpu_np(g.reactor_rhs_batch(P, q, pressures=pres))
+        assert rownorm_err(rhs, og.reactor_rhs_batch(Po, q, pressures=pres)) <= TOL
+        r2, J = g.reactor_jac_batch(P, q, 0, pressures=pres)
+        ro2, Jo = og.reactor_jac_batch(Po, q, 0, pressures=pres)
+        assert rownorm_err(gpu_np(r2), ro2) <= TOL
+        assert rownorm_err(colmajor(gpu_np(J), neq), colmajor(Jo, neq)) <= TOL
+        assert g.device_status() == 0
+    finally:
+        _tps_off(spec)

@@ -155,3 +155,62 @@ def test_oracle_rate_parameter_sensitivity_matches_finite_differences():
             vals.append(g2.rate_param_sens_batch(d['T'], d['rho'], d['Y'])[0][:, r])
         fd = (vals[0] - vals[1]) / 2e-6
         assert np.max(np.abs(fd - s[:, r]) / np.abs(s[:, r])) < 1e-7, (kinds[r], r)
+
+
+OPEN_DIATHERMAL = (600., 900., 50., 0.3, 20.)  # Tc, Tr, h, eps, surface-to-volume (tests/golden/make_golden.py)
+
+
+@pytest.mark.parametrize('name', ['h2-burke', 'methane-gri30'])
+def test_oracle_open_reactor_kernels_match_reference(name):
+    """Open (mass-exchange) reactor right-hand sides and Jacobians, isochoric and isobaric, each heat-transfer
+    option, with a per-state feed (temperature, mass fractions, residence time, density)."""
+    g = np.load(os.path.join(GOLD, f'open_kernels_{name}.npz'))
+    spec, og = pair(name)
+    ns = spec.n_species
+    Tc, Tr, hc, eps, sov = OPEN_DIATHERMAL
+    for heat, ho in (('adiabatic', 0), ('isothermal', 1), ('diathermal', 2)):
+        for i in range(g['T'].size):
+            feed = (g['Tin'][i], g['Yin'][i], g['tau'][i], Tc, Tr, hc, eps, sov, ho, True)
+            r = np.zeros(ns + 1)
+            rj, J = np.zeros(ns + 1), np.zeros((ns + 1) ** 2)
+            og.reactor_rhs_isochoric(g['qiv'][i], g['rhoin'][i], *feed, r)
+            og.reactor_jac_isochoric(g['qiv'][i], g['rhoin'][i], *feed, 0, rj, J)
+            assert rownorm_err(r, g[f'{heat}_rhs_iv'][i]) <= 1e-13
+            assert rownorm_err(rj, g[f'{heat}_jac_rhs_iv'][i]) <= 1e-13
+            assert rownorm_err(colmajor(J, ns + 1), colmajor(g[f'{heat}_Jiv'][i], ns + 1)) <= 1e-13
+            r = np.zeros(ns)
+            rj, J = np.zeros(ns), np.zeros(ns * ns)
+            og.reactor_rhs_isobaric(g['qib'][i], g['p'][i], *feed, r)
+            og.reactor_jac_isobaric(g['qib'][i], g['p'][i], *feed, 0, 0, rj, J)
+            assert rownorm_err(r, g[f'{heat}_rhs_ib'][i]) <= 1e-13
+            assert rownorm_err(rj, g[f'{heat}_jac_rhs_ib'][i]) <= 1e-13
+            assert rownorm_err(colmajor(J, ns), colmajor(g[f'{heat}_Jib'][i], ns)) <= 1e-13
+
+
+def oscillating_feed_case(spec):
+    """tests/reactor/oscillating_feed_temperature/rebless.py: h2-burke, stoichiometric H2/air (air = O2:N2 1:3.74
+    at 300 K) at 800 K and 1 atm, isobaric adiabatic open reactor with mixing time 1e-5 s, feed = the initial
+    mixture with temperature 800 + 400 sin(2 pi 10 t), integrated to t = 0.1 s."""
+    air = spec.stream(stp_air=True)
+    fuel = spec.stream('X', 'H2:1')
+    mix = spec.mix_for_equivalence_ratio(1.0, fuel, air)
+    mix.TP = 800., 101325.
+    return mix, (lambda t: 800. + 400. * np.sin(2. * np.pi * 10. * t))
+
+
+def test_oracle_open_reactor_trajectory_matches_gold():
+    """The reference's oscillating-feed gold (1720 steps) under the reference test's own tolerances
+    (rtol 1e-3, atol 1e-8 on t, T and Y; tests/reactor/oscillating_feed_temperature/test.py)."""
+    import integrate as I
+    g = np.load(os.path.join(GOLD, 'open_reactor_gold.npz'))
+    spec, og = pair('h2-burke')
+    mix, feed_T = oscillating_feed_case(spec)
+    Y0 = np.array(mix.Y)
+    prob = I.OpenReactorProblem(og, 'isobaric', feed_T, Y0, 1.e-5, pressure=101325.)
+    q0 = np.hstack([[mix.T], Y0[:-1]])
+    r = I.integrate(prob, q0, stop_at_time=0.1, save_each_step=True)
+    assert r['times'].size == g['t'].size
+    np.testing.assert_allclose(r['times'], g['t'], rtol=1e-3, atol=1e-8)
+    np.testing.assert_allclose(r['states'][:, 0], g['T'], rtol=1e-3, atol=1e-8)
+    Y = np.vstack([r['states'][:, 1:].T, 1. - r['states'][:, 1:].sum(1)])
+    np.testing.assert_allclose(Y, g['Y'], rtol=1e-3, atol=1e-8)
