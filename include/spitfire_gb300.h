@@ -332,12 +332,18 @@ typedef struct sf_flamelet_batch {
   const double *diffterm;   /* DEVICE [n_flamelets] diffusion term of each flamelet for the eigenvalue bound of
                                sf_flamelet_jac_batch, or NULL to use its scalar diffterm argument for all */
   const int *active;        /* DEVICE [n_flamelets] or NULL: flamelets with active[f] == 0 are left untouched */
+  /* Nonadiabatic flamelets (flamelet_kernels.cpp:1121-1138, :1290-1320): DEVICE [points] convection temperature and
+   * coefficient, radiation temperature and emissivity per interior point, all NULL for adiabatic flamelets. With
+   * use_scaled_heat_loss the coefficients are divided by (max T - T_conv) and (max T^4 - T_rad^4), max T over each
+   * flamelet's interior points. */
+  const double *T_convection, *h_convection, *T_radiation, *h_radiation;
+  int use_scaled_heat_loss;
 } sf_flamelet_batch;
 
-/* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218, adiabatic path). */
+/* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218). */
 int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, double *out_rhs,
                           void *stream);
-/* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, adiabatic path, rates options 0/1/2, exact transform).
+/* BTDDOD Jacobian values (flamelet_kernels.cpp:1220-1409, rates options 0/1/2, exact transform).
  * If scale_and_offset, J <- prefactor*J - I on the diagonal blocks (flamelet_kernels.cpp:1395-1408). If
  * out_expeig is non-NULL it receives, for every row of a point, max(max Re(lambda) - d, 0) over the eigenvalues
  * lambda of that point's diagonal block without the diffusion diagonal (block - diag(cmajor)), d = fb->diffterm[f]

@@ -20,8 +20,13 @@ import oracle as orc
 
 
 class FlameletOperator:
-    def __init__(self, og, z, chi, oxy, fuel, pressure=101325., include_enthalpy_flux=True, include_variable_cp=True):
+    """heat_loss: None (adiabatic) or dict(T_conv, T_rad, h_conv, h_rad, scaled) over the interior points, the
+    reference Flamelet's _T_conv, _T_rad, _h_conv, _h_rad and scale_heat_loss_by_temp_range."""
+
+    def __init__(self, og, z, chi, oxy, fuel, pressure=101325., include_enthalpy_flux=True, include_variable_cp=True,
+                 heat_loss=None):
         self.og = og
+        self.heat_loss = heat_loss
         self.z = np.asarray(z, dtype=np.float64)
         self.chi = np.asarray(chi, dtype=np.float64)
         self.dz = self.z[1:] - self.z[:-1]
@@ -42,20 +47,29 @@ class FlameletOperator:
         self.scales[::self.ns] = 1.e3
         self.max_dissipation_rate = float(np.max(self.chi))
 
+    def _heat(self):
+        h = self.heat_loss
+        if h is None:
+            n = self.null
+            return True, n, n, n, n, False
+        return (False, np.asarray(h['T_conv'], dtype=np.float64), np.asarray(h['T_rad'], dtype=np.float64),
+                np.asarray(h['h_conv'], dtype=np.float64), np.asarray(h['h_rad'], dtype=np.float64),
+                bool(h.get('scaled', False)))
+
     def rhs(self, state, eflux=None, vcp=None):
         out = np.zeros(self.nzi * self.ns)
-        n = self.null
-        self.og.flamelet_rhs(state, self.pressure, self.oxy, self.fuel, True, n, n, n, n, self.nzi, self.cmajor,
-                             self.csub, self.csup, self.mc, self.nc, self.chi,
-                             self.eflux if eflux is None else eflux, self.vcp if vcp is None else vcp, False, out)
+        adiabatic, Tc, Tr, hc, hr, scaled = self._heat()
+        self.og.flamelet_rhs(state, self.pressure, self.oxy, self.fuel, adiabatic, Tc, Tr, hc, hr, self.nzi,
+                             self.cmajor, self.csub, self.csup, self.mc, self.nc, self.chi,
+                             self.eflux if eflux is None else eflux, self.vcp if vcp is None else vcp, scaled, out)
         return out
 
     def jac(self, state, eflux=None, scale_and_offset=False, prefactor=0.):
-        n = self.null
-        return self.og.flamelet_jacobian_values(state, self.pressure, self.oxy, self.fuel, True, n, n, n, n,
+        adiabatic, Tc, Tr, hc, hr, scaled = self._heat()
+        return self.og.flamelet_jacobian_values(state, self.pressure, self.oxy, self.fuel, adiabatic, Tc, Tr, hc, hr,
                                                 self.nzi, self.cmajor, self.csub, self.csup, self.mc, self.nc,
                                                 self.chi, scale_and_offset, prefactor, 0,
-                                                self.eflux if eflux is None else eflux, False)
+                                                self.eflux if eflux is None else eflux, scaled)
 
     def blocks(self, values):
         """[nzi, row, col] diagonal blocks of a BTDDOD value array."""

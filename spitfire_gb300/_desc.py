@@ -57,7 +57,8 @@ class SfFlameletBatch(C.Structure):
                 ('pressure', C.c_double), ('oxy_state', _dp), ('fuel_state', _dp),
                 ('cmajor', _dp), ('csub', _dp), ('csup', _dp), ('mcoeff', _dp), ('ncoeff', _dp), ('chi', _dp),
                 ('include_enthalpy_flux', C.c_int), ('include_variable_cp', C.c_int), ('diffterm', _dp),
-                ('active', _ip)]
+                ('active', _ip), ('T_convection', _dp), ('h_convection', _dp), ('T_radiation', _dp),
+                ('h_radiation', _dp), ('use_scaled_heat_loss', C.c_int)]
 
 
 def reactor_params(configuration='isobaric', heat_transfer='adiabatic', open_=False, pressure=101325.,

@@ -1,4 +1,4 @@
-// Flamelet kernels: the adiabatic flamelet right-hand side and its block-tridiagonal ("BTDDOD": block diagonal,
+// Flamelet kernels: the flamelet right-hand side (adiabatic or with heat loss) and its block-tridiagonal ("BTDDOD": block diagonal,
 // diagonal off-diagonals) Jacobian for a batch of flamelets with different grids, and the block-Thomas algebra.
 //
 // Reference: src/spitfire/griffon/src/flamelet_kernels.cpp:31-90 (stencils, COO indices), :1039-1218
@@ -37,6 +37,9 @@ struct FlmParams {
   double prefactor;
   double *eflux_store;  // if set: the enthalpy-flux diagonal correction is stored here (per point) instead
   const int *active;    // device [nf] or null: flamelets with active[f] == 0 are skipped
+  // nonadiabatic flamelets: convection / radiation temperature and coefficient per interior point (null: adiabatic)
+  const double *Tconv, *hconv, *Trad, *hrad;
+  int scaled_heat_loss;
   int groups_per_cta;
 };
 
@@ -83,6 +86,40 @@ struct BlockWriter {
   }
 };
 
+// Heat loss of a nonadiabatic flamelet point (flamelet_kernels.cpp:1121-1138, :1290-1320): the isobaric reactor's
+// diathermal terms with unit surface-to-volume ratio and this point's convection (Tc, hc) and radiation (Tr, hr)
+// parameters, q = hc (Tc - T) + hr sigma (Tr^4 - T^4) entering dT/dt as q / (rho cp). With use_scaled_heat_loss the
+// coefficients are divided by (max T - Tc) and (max T^4 - Tr^4), max T over the flamelet's interior points (held
+// constant in the Jacobian, as the reference does). The reference adds the Y-column terms in a loop that runs two
+// columns past the end of its primitive Jacobian (flamelet_kernels.cpp:1316-1319); here they stop at the last Y
+// column.
+template <int G>
+__device__ __forceinline__ void heat_loss_cfg(const FlmParams &p, const Group<G> &grp, int pt, int z0, int nzi,
+                                              ReactorCfg &cfg)
+{
+  if (!p.Tconv) {
+    cfg.heat = 0;
+    return;
+  }
+  const double Tc = p.Tconv[pt], Tr = p.Trad[pt];
+  double hc = p.hconv[pt], hr = p.hrad[pt];
+  if (p.scaled_heat_loss) {
+    double mx = -1.;
+    for (int j = grp.lane; j < nzi; j += G) mx = fmax(mx, p.state[(size_t)(z0 + j) * p.m.ns]);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(grp.mask, mx, o, G));
+    const double Tr4 = Tr * Tr * Tr * Tr;
+    hc = hc / (mx - Tc);
+    hr = hr / (mx * mx * mx * mx - Tr4);
+  }
+  cfg.heat = 2;
+  cfg.Tc = Tc;
+  cfg.hc = hc;
+  cfg.Tr = Tr;
+  cfg.eps = hr;
+  cfg.SoV = 1.;
+}
+
 template <int G, bool JAC>
 __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
 {
@@ -108,6 +145,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
     if (p.active && !p.active[f]) continue;
     const int z0 = p.offz[f], nzi = p.offz[f + 1] - z0;
     const int iz = pt - z0;
+    heat_loss_cfg<G>(p, grp, pt, z0, nzi, cfg);
     const double *st = p.state + (size_t)pt * ns;
     const double *oxy = p.oxy + (size_t)f * ns;
     const double *fuel = p.fuel + (size_t)f * ns;
@@ -670,6 +708,15 @@ void fill(FlmParams &p, const sf_flamelet_batch *fb)
   p.mc = fb->mcoeff;
   p.nc = fb->ncoeff;
   p.chi = fb->chi;
+  if (fb->T_convection || fb->h_convection || fb->T_radiation || fb->h_radiation) {
+    if (!fb->T_convection || !fb->h_convection || !fb->T_radiation || !fb->h_radiation)
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "nonadiabatic flamelets need all four heat-loss arrays");
+    p.Tconv = fb->T_convection;
+    p.hconv = fb->h_convection;
+    p.Trad = fb->T_radiation;
+    p.hrad = fb->h_radiation;
+    p.scaled_heat_loss = fb->use_scaled_heat_loss ? 1 : 0;
+  }
   p.eflux = fb->include_enthalpy_flux;
   p.vcp = fb->include_variable_cp;
   p.active = fb->active;

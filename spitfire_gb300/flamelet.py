@@ -1,7 +1,7 @@
-"""Steady flamelets on the GPU: Spitfire's ``FlameletSpec``/``Flamelet`` for the adiabatic path, batched.
+"""Steady flamelets on the GPU: Spitfire's ``FlameletSpec``/``Flamelet``, adiabatic or with heat loss, batched.
 
-``FlameletBatch`` holds any number of adiabatic flamelets of one mechanism, each with its own mixture-fraction grid
-and dissipation-rate profile, and evaluates all of them with one launch per operation: the flamelet residual
+``FlameletBatch`` holds any number of flamelets of one mechanism, each with its own mixture-fraction grid,
+dissipation-rate profile and heat-loss parameters, and evaluates all of them with one launch per operation: the flamelet residual
 (``sf_flamelet_rhs_batch``), the block-tridiagonal Jacobian (``sf_flamelet_jac_batch``), the block-Thomas
 factorization and solve (``sf_btddod_*``). The steady solvers restate the reference's control flow per flamelet
 (spitfire/chemistry/flamelet.py): ``steady_solve_newton`` (:1352-1485; chord Newton on -J with a refresh after
@@ -56,16 +56,28 @@ def compute_dissipation_rate(mixture_fraction, max_dissipation_rate, form='Peter
 
 
 class FlameletSpec:
-    """The specification arguments of spitfire's FlameletSpec used on the adiabatic path (flamelet.py:35-237)."""
+    """The specification arguments of spitfire's FlameletSpec (flamelet.py:35-237): grid, dissipation rate,
+    streams, initial condition and, for heat_transfer='nonadiabatic', the convection / radiation parameters
+    (numbers or arrays over the interior points) and the heat-loss scaling options."""
 
     def __init__(self, mech_spec=None, initial_condition=None, oxy_stream=None, fuel_stream=None, grid=None,
                  grid_points=None, grid_type='clustered', grid_cluster_intensity=4.,
                  grid_cluster_point='stoichiometric', max_dissipation_rate=None, stoich_dissipation_rate=None,
                  dissipation_rate=None, dissipation_rate_form='Peters', heat_transfer='adiabatic',
+                 convection_temperature=None, radiation_temperature=None, convection_coefficient=None,
+                 radiative_emissivity=None, scale_heat_loss_by_temp_range=False,
+                 scale_convection_by_dissipation=False, use_linear_ref_temp_profile=False,
                  rates_sensitivity_type='dense', sensitivity_transform_type='exact', include_enthalpy_flux=True,
                  include_variable_cp=True, **ignored):
-        if heat_transfer != 'adiabatic':
-            raise NotImplementedError('the GPU flamelet path covers adiabatic flamelets')
+        if heat_transfer not in ('adiabatic', 'nonadiabatic'):
+            raise ValueError(f'bad heat_transfer {heat_transfer!r}; use adiabatic or nonadiabatic')
+        self.convection_temperature = convection_temperature
+        self.radiation_temperature = radiation_temperature
+        self.convection_coefficient = convection_coefficient
+        self.radiative_emissivity = radiative_emissivity
+        self.scale_heat_loss_by_temp_range = scale_heat_loss_by_temp_range
+        self.scale_convection_by_dissipation = scale_convection_by_dissipation
+        self.use_linear_ref_temp_profile = use_linear_ref_temp_profile
         self.mech_spec = mech_spec
         self.initial_condition = initial_condition
         self.oxy_stream = oxy_stream
@@ -130,6 +142,33 @@ class FlameletSetup:
         self.include_enthalpy_flux = fs.include_enthalpy_flux
         self.include_variable_cp = fs.include_variable_cp
         self.rates_option = {'dense': 0, 'no-TBAF': 1, 'sparse': 2}[fs.rates_sensitivity_type]
+        # heat loss (flamelet.py:479-519): per interior point convection / radiation temperature and coefficient
+        self.heat_transfer = fs.heat_transfer
+        self.scale_heat_loss_by_temp_range = bool(fs.scale_heat_loss_by_temp_range)
+        self.T_conv = self.T_rad = self.h_conv = self.h_rad = None
+        if self.heat_transfer == 'nonadiabatic':
+            def per_point(v, name):
+                if v is None:
+                    raise ValueError(f'Flamelet specifications: Nonadiabatic heat transfer was selected but no {name} '
+                                     f'argument was given.')
+                a = np.asarray(v, dtype=np.float64)
+                if a.ndim == 0:
+                    return float(a) + np.zeros(self.nzi)
+                if a.shape != (self.nzi,):
+                    raise ValueError(f'{name} needs one value per interior grid point ({self.nzi})')
+                return a.copy()
+            self.h_conv = per_point(fs.convection_coefficient, 'convection_coefficient')
+            self.h_rad = per_point(fs.radiative_emissivity, 'radiative_emissivity')
+            if fs.use_linear_ref_temp_profile:
+                self.T_conv = fs.oxy_stream.T + self.z[1:-1] * (fs.fuel_stream.T - fs.oxy_stream.T)
+                self.T_rad = self.T_conv.copy()
+            else:
+                self.T_rad = per_point(fs.radiation_temperature, 'radiation_temperature')
+                self.T_conv = per_point(fs.convection_temperature, 'convection_temperature')
+            if fs.scale_convection_by_dissipation:
+                factor = np.max(self.x) / (1. - self.z_st) / self.z_st
+                self.h_conv = self.h_conv * factor
+                self.h_rad = self.h_rad * factor
         ic = fs.initial_condition
         if isinstance(ic, np.ndarray):
             if ic.size != self.nzi * ns:
@@ -187,7 +226,7 @@ def burke_schumann_state(m, oxy, fuel, z, pressure):
 
 
 class FlameletBatch:
-    """GPU evaluation of a batch of adiabatic flamelets (one mechanism, common pressure)."""
+    """GPU evaluation of a batch of flamelets (one mechanism, common pressure), adiabatic or with heat loss."""
 
     def __init__(self, setups):
         torch = _torch()
@@ -256,6 +295,26 @@ class FlameletBatch:
             setattr(fb, name, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
         fb.include_enthalpy_flux = int(self.setups[0].include_enthalpy_flux)
         fb.include_variable_cp = int(self.setups[0].include_variable_cp)
+        # heat loss: per-point arrays when any flamelet is nonadiabatic (adiabatic members get zero coefficients,
+        # which add exact zeros)
+        nonad = [s for s in self.setups if s.heat_transfer == 'nonadiabatic']
+        self.t_heat = None
+        if nonad:
+            scaled = {s.scale_heat_loss_by_temp_range for s in nonad}
+            if len(scaled) > 1:
+                raise ValueError('the nonadiabatic flamelets of a batch share scale_heat_loss_by_temp_range')
+            arrs = {k: [] for k in ('T_convection', 'h_convection', 'T_radiation', 'h_radiation')}
+            for s in self.setups:
+                if s.heat_transfer == 'nonadiabatic':
+                    vals = (s.T_conv, s.h_conv, s.T_rad, s.h_rad)
+                else:
+                    vals = (np.zeros(s.nzi), np.zeros(s.nzi), np.zeros(s.nzi), np.zeros(s.nzi))
+                for k, v in zip(arrs, vals):
+                    arrs[k].append(v)
+            self.t_heat = {k: T(v) for k, v in arrs.items()}
+            for k, t in self.t_heat.items():
+                setattr(fb, k, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
+            fb.use_scaled_heat_loss = int(scaled.pop())
         self.fb = fb
         self.nvals = int(offv[-1])
         self.values = torch.empty(self.nvals, dtype=torch.float64, device=dev)
@@ -533,11 +592,12 @@ class FlameletBatch:
 
 
 class Flamelet:
-    """Drop-in for spitfire.chemistry.flamelet.Flamelet on the adiabatic path (one flamelet, GPU kernels)."""
+    """Drop-in for spitfire.chemistry.flamelet.Flamelet's steady path (one flamelet, GPU kernels)."""
 
     def __init__(self, flamelet_specs=None, **kwargs):
         fs = FlameletSpec(**flamelet_specs) if isinstance(flamelet_specs, dict) else \
             (flamelet_specs if flamelet_specs is not None else FlameletSpec(**kwargs))
+        self._fs = fs
         self._setup = FlameletSetup(fs)
         self._batch = None
         self._current_state = self._setup.initial_state.copy()
@@ -550,6 +610,14 @@ class Flamelet:
     @property
     def mechanism(self):
         return self._setup.mech
+
+    @property
+    def oxy_stream(self):
+        return self._fs.oxy_stream
+
+    @property
+    def fuel_stream(self):
+        return self._fs.fuel_stream
 
     @property
     def mixfrac_grid(self):

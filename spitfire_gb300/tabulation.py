@@ -1,4 +1,5 @@
-"""Adiabatic steady laminar flamelet (SLFM) libraries on the GPU flamelet solvers.
+"""Steady laminar flamelet (SLFM) libraries on the GPU flamelet solvers: adiabatic, and nonadiabatic with an
+enthalpy-defect dimension from quasisteady heat loss.
 
 ``build_adiabatic_slfm_library`` keeps the interface and behaviour of spitfire/chemistry/tabulation.py:229-336:
 a sequential continuation in the dissipation rate, each flamelet started from the previous converged profile,
@@ -7,6 +8,14 @@ solved with compute_steady_state (Newton, then pseudo-transient continuation), s
 (mixture_fraction, dissipation_rate_stoich or _max). The first flamelet starts from the Burke-Schumann profile:
 the reference starts it from Cantera's HP equilibrium, which is not available here; both starts converge to the
 burning steady solution the solver tolerance defines.
+
+``build_nonadiabatic_defect_steady_slfm_library`` keeps the interface of tabulation.py:786-845: for every burning
+dissipation rate of the adiabatic library, a continuation in the convection coefficient of a heat-loss flamelet
+(linear reference temperature profile, no radiation) until extinction (tabulation.py:408-519), the solutions
+subsampled every h_stoich_spacing of stoichiometric enthalpy, then interpolated onto n_defect_st uniformly spaced
+stoichiometric enthalpy defects (tabulation.py:594-665) and returned over (mixture_fraction,
+dissipation_rate_stoich, enthalpy_defect_stoich). The continuations of all dissipation rates advance together,
+each step one batched steady solve.
 
 ``solve_steady_flamelets`` solves any number of independent flamelets (own grids, dissipation rates, initial
 profiles) at once, every solver iteration one batched launch per operation over all of them.
@@ -21,6 +30,7 @@ from .library import Dimension, Library
 
 _mixture_fraction_name = 'mixture_fraction'
 _dissipation_rate_name = 'dissipation_rate'
+_enthalpy_defect_name = 'enthalpy_defect'
 _stoich_suffix = '_stoich'
 
 
@@ -116,3 +126,166 @@ def build_adiabatic_slfm_library(flamelet_specs, diss_rate_values=np.logspace(-3
     if verbose:
         print(f'library built in {perf_counter() - t00:6.2f} s')
     return lib
+
+
+# ------------------------------------------------------------------------------------------------------ heat loss
+def _mixture_enthalpy(m, T, Y):
+    """Mass-specific mixture enthalpy of states T[...] and Y[..., ns] (the quantity Cantera's enthalpy_mass gives
+    analysis.compute_specific_enthalpy, from the same NASA7 polynomials)."""
+    T = np.asarray(T, dtype=np.float64)
+    hs, _ = m.species_h_cp_host_vec(T.ravel())
+    return (hs * np.asarray(Y).reshape(-1, m.n_species)).sum(1).reshape(T.shape)
+
+
+def _enthalpy_of_props(m, props):
+    names = m.species_names
+    Y = np.stack([props['mass fraction ' + n] for n in names], axis=-1)
+    return _mixture_enthalpy(m, props['temperature'], Y)
+
+
+def _expand_defect_steady(flamelet_specs, table, chis, h_stoich_spacing, verbose):
+    """Quasisteady heat-loss continuation of every dissipation rate (tabulation.py:408-519), all advanced together:
+    convection coefficient h += dh from 0 with dh = 0.1, dh *= min(max(sqrt(0.1 / diff), 0.1), 2) after each solve
+    (diff: largest relative change of the interior state), until the maximum of the interior state drops below
+    max(T_oxy, T_fuel) + 10 (extinction) or h reaches 1e10. Returns the unstructured table {(chi_st, g_st): data}."""
+    m = flamelet_specs.mech_spec
+    fs = _spec_copy(flamelet_specs, heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=False,
+                    scale_convection_by_dissipation=False, use_linear_ref_temp_profile=True,
+                    radiative_emissivity=0., convection_coefficient=0., dissipation_rate=None,
+                    max_dissipation_rate=None)
+    t_ext = max(flamelet_specs.oxy_stream.T, flamelet_specs.fuel_stream.T) + 10.
+    k = len(chis)
+    hval = np.zeros(k)
+    dh = np.full(k, 0.1)
+    diff_target = 0.1
+    hval_max = 1.e10
+    state = [table[c]['adiabatic_state'].copy() for c in chis]
+    state_old = [x.copy() for x in state]
+    running = np.ones(k, dtype=bool)
+    hvalues = [[0.] for _ in chis]
+    solutions = [[{q: v for q, v in table[c].items() if q != 'adiabatic_state'}] for c in chis]
+    z = None
+    setup0 = None
+    it = 0
+    while running.any():
+        it += 1
+        idx = np.flatnonzero(running)
+        hval[idx] += dh[idx]
+        setups = [FlameletSetup(_spec_copy(fs, stoich_dissipation_rate=float(chis[i]),
+                                           convection_coefficient=float(hval[i]), initial_condition=state[i]))
+                  for i in idx]
+        setup0 = setups[0]
+        z = setup0.z
+        states, methods = solve_steady_flamelets(setups)
+        for j, i in enumerate(idx):
+            if states[j] is None:
+                raise RuntimeError(f'steady heat-loss flamelet solve failed at chi_st = {chis[i]}, h = {hval[i]}')
+            cur = states[j]
+            diff = np.max(np.abs(cur - state_old[i]) / (np.abs(cur) + 1.e-4))
+            extinguished = np.max(cur) < t_ext
+            state[i] = cur
+            state_old[i] = cur.copy()
+            dh[i] *= np.min([np.max([np.sqrt(diff_target / diff), 0.1]), 2.])
+            hvalues[i].append(hval[i])
+            solutions[i].append(_library_of(setups[j], cur))
+            if extinguished or hval[i] >= hval_max:
+                running[i] = False
+        if verbose:
+            print(f'  heat-loss step {it:4d}: {int(running.sum())} of {k} flamelets still burning', flush=True)
+    z_st = m.stoich_mixture_fraction(flamelet_specs.fuel_stream, flamelet_specs.oxy_stream)
+    out = {}
+    for i, chi in enumerate(chis):
+        sols = solutions[i]
+        h_tz = np.stack([_enthalpy_of_props(m, sol) for sol in sols], axis=1)  # [nz, nt]
+        h_ad = h_tz[:, 0]
+        nt = h_tz.shape[1]
+        indices = [0]
+        last_hst = np.interp(z_st, z, h_ad)
+        for t in range(nt - 1):
+            this_hst = np.interp(z_st, z, h_tz[:, t])
+            if last_hst - this_hst > h_stoich_spacing:
+                indices.append(t)
+                last_hst = this_hst
+        for t in indices:
+            defect = h_tz[:, t] - h_ad
+            gst = float(np.interp(z_st, z, defect))
+            data = {'enthalpy_defect': defect.copy(), 'enthalpy_cons': h_ad.copy(), 'enthalpy': h_tz[:, t].copy(),
+                    _mixture_fraction_name: z.copy()}
+            for q, v in sols[t].items():
+                data[q] = np.asarray(v).copy()
+            out[(chi, gst)] = data
+    return out
+
+
+def _structure_defect(unstructured, n_defect_st, extend=False):
+    """tabulation.py:594-665: every quantity of every dissipation rate interpolated onto n_defect_st uniformly spaced
+    stoichiometric defects between the smallest and largest of all flamelets (piecewise linear, constant beyond a
+    flamelet's own range; enthalpy and enthalpy_defect extrapolated linearly when extend). Returns (table, sorted
+    dissipation rates, defects in decreasing order)."""
+    gs = np.array([g for (_, g) in unstructured])
+    gmin, gmax = float(gs.min()), float(gs.max())
+    space = np.linspace(gmin, gmax, n_defect_st)
+    if extend:
+        sp = abs(space[1] - space[0])
+        space = np.linspace(gmin - 2 * sp, gmax, n_defect_st + 2)
+    chis = sorted({c for (c, _) in unstructured})
+    table = {}
+    for chi in chis:
+        gl = np.array(sorted(g for (c, g) in unstructured if c == chi))
+        first = unstructured[(chi, gl[0])]
+        for q in first:
+            Y = np.stack([unstructured[(chi, g)][q] for g in gl], axis=0)  # [ng, nz]
+            for gs_ in space:
+                if extend and q in ('enthalpy', 'enthalpy_defect') and gl.size > 1 and not gl[0] <= gs_ <= gl[-1]:
+                    lo = 0 if gs_ < gl[0] else gl.size - 2
+                    w = (gs_ - gl[lo]) / (gl[lo + 1] - gl[lo])
+                    val = Y[lo] + w * (Y[lo + 1] - Y[lo])
+                elif gl.size == 1:
+                    val = Y[0].copy()
+                else:
+                    val = np.array([np.interp(gs_, gl, Y[:, iz]) for iz in range(Y.shape[1])])
+                table.setdefault((chi, gs_), {})[q] = val
+                if q in ('density', 'temperature') and np.any(val < 1.e-14):
+                    raise ValueError(f'{q} < 1.e-14 detected!')
+    return table, np.array(chis), space[::-1]
+
+
+def build_nonadiabatic_defect_steady_slfm_library(flamelet_specs, diss_rate_values=np.logspace(-3, 2, 16),
+                                                  diss_rate_ref='stoichiometric', verbose=True,
+                                                  solver_verbose=False, h_stoich_spacing=10.e3, num_procs=1,
+                                                  integration_args=None, n_defect_st=32, extend_defect_dim=False,
+                                                  diss_rate_log_scaled=True):
+    """SLFM library with an enthalpy-defect dimension from quasisteady heat loss (tabulation.py:786-845); see the
+    module docstring. num_procs and integration_args are accepted for interface compatibility: the continuations
+    already run together on the device, and no time integration is involved."""
+    if isinstance(flamelet_specs, dict):
+        flamelet_specs = FlameletSpec(**flamelet_specs)
+    m = flamelet_specs.mech_spec
+    t00 = perf_counter()
+    table, z, x_values = build_adiabatic_slfm_library(flamelet_specs, diss_rate_values, diss_rate_ref,
+                                                      verbose, solver_verbose, _return_intermediates=True)
+    if verbose:
+        print('expanding (steady) enthalpy defect dimension ...', flush=True)
+    unstructured = _expand_defect_steady(flamelet_specs, table, list(x_values), h_stoich_spacing, verbose)
+    st, xs, gs = _structure_defect(unstructured, n_defect_st, extend_defect_dim)
+    key0 = next(iter(st))
+    lib = Library(Dimension(_mixture_fraction_name, st[key0][_mixture_fraction_name]),
+                  Dimension(_dissipation_rate_name + _stoich_suffix, xs, diss_rate_log_scaled),
+                  Dimension(_enthalpy_defect_name + _stoich_suffix, gs))
+    lib.extra_attributes['mech_spec'] = m
+    for q in st[key0]:
+        vals = lib.get_empty_dataset()
+        for ix, x in enumerate(xs):
+            for ig, g in enumerate(gs):
+                vals[:, ix, ig] = st[(x, g)][q]
+        lib[q] = vals
+    if verbose:
+        print(f'library built in {perf_counter() - t00:6.2f} s')
+    return lib
+
+
+def build_nonadiabatic_defect_transient_slfm_library(*args, **kwargs):
+    """tabulation.py:727-784 expands the defect dimension by transient flamelet integration
+    (Flamelet.integrate_for_heat_loss), which is not on the GPU path; the steady variant is."""
+    raise NotImplementedError('transient flamelet integration is not on the GPU path; use '
+                              'build_nonadiabatic_defect_steady_slfm_library')

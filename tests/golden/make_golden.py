@@ -17,8 +17,13 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
                        bounds), block-Thomas solves and matvecs, and steady Newton / psitc solutions with iteration
                        counts, for an H2 and a GRI-3.0 flamelet started from a Burke-Schumann profile
   adiabatic_slfm_gold.npz  temperature and mass fractions of tests/tabulation/adiabatic_slfm/gold.pkl
+  flamelet_nonad_ref.npz   reference Flamelet residuals and BTDDOD Jacobians with heat loss (convection and
+                       radiation per point; unscaled, and scaled by the temperature range with the linear reference
+                       temperature profile) for the flamelet cases
+  nonadiabatic_steady_slfm_gold.npz  dimensions, temperature, mass fractions and enthalpy defect of
+                       tests/tabulation/nonadiabatic_defect_steady_slfm/gold.pkl
 
-Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open]
+Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
 """
 import json
 import os
@@ -289,6 +294,66 @@ def flamelets():
     np.savez_compressed(os.path.join(HERE, 'flamelet_ref.npz'), **out)
 
 
+def nonadiabatic():
+    import ref_harness as rh
+    from flamelet_cases import FLAMELET_CASES, flamelet_case_setup
+    from spitfire_gb300.flamelet import burke_schumann_state, clustered_grid
+    ns_ref = rh.load_reference()
+    out = {}
+    for case in FLAMELET_CASES:
+        name, fname, phase = case[:3]
+        ref = rh.ReferenceMechanism(os.path.join(MECHS, fname), phase)
+        spec = ref.spec
+        oxy, fuel, kw = flamelet_case_setup(spec, case)
+        zst = spec.stoich_mixture_fraction(fuel, oxy)
+        z, _ = clustered_grid(kw['grid_points'], zst, 4.)
+        ic = burke_schumann_state(spec, oxy, fuel, z, 101325.)
+        rng = np.random.default_rng(case[-1] + 100)
+        st = np.abs(ic * (1. + 0.02 * rng.standard_normal(ic.size)))
+        nzi = z.size - 2
+        variants = {
+            # per-point convection / radiation parameters, unscaled
+            'plain': dict(heat_transfer='nonadiabatic', convection_temperature=rng.uniform(300., 600., nzi),
+                          radiation_temperature=rng.uniform(300., 900., nzi),
+                          convection_coefficient=rng.uniform(1.e3, 1.e5, nzi),
+                          radiative_emissivity=rng.uniform(0.1, 0.9, nzi)),
+            # the transient defect builder's options (tabulation.py:341-348)
+            'scaled': dict(heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                           scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                           convection_coefficient=1.e7, radiative_emissivity=0.5),
+        }
+        pre = name + '_'
+        out[pre + 'state'] = st
+        for vname, hk in variants.items():
+            F = ns_ref.flamelet.Flamelet(ns_ref.flamelet.FlameletSpec(mech_spec=ref, initial_condition=ic,
+                                                                      **dict(kw, **hk)))
+            v = pre + vname + '_'
+            out[v + 'T_conv'] = np.asarray(F._T_conv)
+            out[v + 'T_rad'] = np.asarray(F._T_rad)
+            out[v + 'h_conv'] = np.asarray(F._h_conv)
+            out[v + 'h_rad'] = np.asarray(F._h_rad)
+            for q in ('convection_temperature', 'radiation_temperature', 'convection_coefficient',
+                      'radiative_emissivity'):
+                if q in hk:
+                    out[v + 'arg_' + q] = np.asarray(hk[q])
+            out[v + 'rhs'] = F._nonadiabatic_rhs(0., st)
+            out[v + 'jac'] = F._nonadiabatic_jac(st)
+        print('nonadiabatic flamelet kernels', name, nzi)
+    np.savez_compressed(os.path.join(HERE, 'flamelet_nonad_ref.npz'), **out)
+    d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'nonadiabatic_defect_steady_slfm', 'gold.pkl'), 'rb')).load()
+    st = d._st
+    arrs = {}
+    for i in range(len(st['dim_ordering'])):
+        n = st['dim_ordering'][i]
+        arrs['dim%d_name' % i] = np.array(n)
+        arrs['dim%d_values' % i] = np.asarray(st['dimensions'][n]['values'])
+    for k, v in st['properties'].items():
+        if k in ('temperature', 'enthalpy_defect', 'enthalpy', 'pressure') or k.startswith('mass fraction'):
+            arrs['prop:' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'nonadiabatic_steady_slfm_gold.npz'), **arrs)
+    print('nonadiabatic steady slfm gold', np.asarray(st['properties']['temperature']).shape)
+
+
 def slfm_gold():
     d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'adiabatic_slfm', 'gold.pkl'), 'rb')).load()
     st = d._st
@@ -320,3 +385,5 @@ if __name__ == '__main__':
         ignition()
     if 'open' in what:
         open_kernels()
+    if 'nonadiabatic' in what:
+        nonadiabatic()

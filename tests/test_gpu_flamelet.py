@@ -240,3 +240,86 @@ def test_adiabatic_slfm_library_matches_reference_gold(cuda):
         l2 = Library.load_from_file(p)
         for k in keys:
             assert np.array_equal(l2[k[5:]], lib[k[5:]])
+
+
+@pytest.mark.parametrize('name', CASES)
+@pytest.mark.parametrize('variant', ['plain', 'scaled'])
+def test_nonadiabatic_flamelet_rhs_and_jacobian(cuda, name, variant):
+    """Heat loss on the GPU: a batch of the reference's nonadiabatic flamelet (tests/golden/flamelet_nonad_ref.npz),
+    an adiabatic flamelet and a nonadiabatic flamelet on another grid; residuals and Jacobians against the reference
+    and the oracle at the same bars."""
+    import flamelet_steady as FS
+    from spitfire_gb300.flamelet import FlameletBatch, FlameletSetup, FlameletSpec
+    g = np.load(FC.GOLD + '/flamelet_nonad_ref.npz')
+    d = FC.golden()
+    spec, og = pair(FC.BUNDLED[name])
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case(name))
+    v = f'{name}_{variant}_'
+    if variant == 'plain':
+        hk = dict(heat_transfer='nonadiabatic', convection_temperature=g[v + 'arg_convection_temperature'],
+                  radiation_temperature=g[v + 'arg_radiation_temperature'],
+                  convection_coefficient=g[v + 'arg_convection_coefficient'],
+                  radiative_emissivity=g[v + 'arg_radiative_emissivity'])
+        hk2 = dict(heat_transfer='nonadiabatic', convection_temperature=400., radiation_temperature=500.,
+                   convection_coefficient=3.e4, radiative_emissivity=0.4)
+    else:
+        hk = dict(heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                  scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                  convection_coefficient=1.e7, radiative_emissivity=0.5)
+        hk2 = dict(hk, convection_coefficient=3.e6)
+    st0 = g[name + '_state']
+    s0 = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition=st0, **dict(kw, **hk)))
+    s1 = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition='Burke-Schumann',
+                                    **dict(kw, grid_points=13, stoich_dissipation_rate=3.)))
+    s2 = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition='Burke-Schumann',
+                                    **dict(kw, grid_points=19, stoich_dissipation_rate=0.5, **hk2)))
+    rng = np.random.default_rng(7)
+    for s in (s1, s2):
+        s.initial_state = np.abs(s.initial_state * (1. + 0.02 * rng.standard_normal(s.initial_state.size)))
+    setups = [s0, s1, s2]
+    b = FlameletBatch(setups)
+    ops = [FS.FlameletOperator(og, s.z, s.x, s.state_oxy, s.state_fuel,
+                               heat_loss=None if s.heat_transfer == 'adiabatic' else
+                               dict(T_conv=s.T_conv, T_rad=s.T_rad, h_conv=s.h_conv, h_rad=s.h_rad,
+                                    scaled=s.scale_heat_loss_by_temp_range)) for s in setups]
+    ns = b.ns
+    st = b.initial_state()
+    r = _split(b, b.rhs(st))
+    assert FC.vec_err(r[0], g[v + 'rhs'], ns) < 1e-10
+    J = _split(b, b.jacobian(st).clone(), 'v')
+    assert FC.btddod_row_err(J[0], g[v + 'jac'], s0.nzi, ns) < 1e-10
+    for f, s in enumerate(setups):
+        assert FC.vec_err(r[f], ops[f].rhs(s.initial_state), ns) < 1e-10, f
+        assert FC.btddod_row_err(J[f], ops[f].jac(s.initial_state), s.nzi, ns) < 1e-10, f
+    assert spec.griffon.device_status() == 0
+    del d
+
+
+def test_nonadiabatic_steady_slfm_library_matches_reference_gold(cuda):
+    """tests/tabulation/nonadiabatic_defect_steady_slfm of the reference (h2-burke, air 1200 K / H2 300 K, 34
+    points, chi_st = logspace(0, 1, 4), 32 stoichiometric enthalpy defects) through the drop-in
+    build_nonadiabatic_defect_steady_slfm_library; the reference test's bars (rtol 2e-4, atol 1e-4) on temperature,
+    pressure, every mass fraction, the enthalpy and the enthalpy defect, and the library dimensions. As in the
+    reference test (rebless.py), the enthalpy is recomputed from the library's states afterwards."""
+    import os
+    from spitfire_gb300.analysis import compute_specific_enthalpy
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    from spitfire_gb300.tabulation import build_nonadiabatic_defect_steady_slfm_library
+    g = np.load(os.path.join(FC.GOLD, 'nonadiabatic_steady_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    lib = build_nonadiabatic_defect_steady_slfm_library(
+        dict(mech_spec=m, oxy_stream=air, fuel_stream=fuel, grid_points=34), verbose=False,
+        diss_rate_values=np.logspace(0, 1, 4), diss_rate_log_scaled=True,
+        integration_args={'transient_tolerance': 1e-10}, num_procs=1)
+    lib = compute_specific_enthalpy(m, lib)
+    assert lib.dim_names == ['mixture_fraction', 'dissipation_rate_stoich', 'enthalpy_defect_stoich']
+    np.testing.assert_allclose(lib.dims[0].values, g['dim0_values'], rtol=1e-14)
+    np.testing.assert_allclose(lib.dims[1].values, g['dim1_values'], rtol=1e-12)
+    np.testing.assert_allclose(lib.dims[2].values, g['dim2_values'], rtol=2e-4, atol=1e-4)
+    keys = [k for k in g.files if k.startswith('prop:')]
+    assert len(keys) == 4 + m.n_species
+    for k in keys:
+        np.testing.assert_allclose(lib[k[5:]], g[k], rtol=2e-4, atol=1e-4, err_msg=k)

@@ -148,3 +148,53 @@ def test_oracle_slfm_continuation_matches_reference_gold():
         ic = st
     np.testing.assert_allclose(s.z, d['dim0_values'], rtol=1e-14)
     np.testing.assert_allclose(chis, d['dim1_values'], rtol=1e-12)
+
+
+def _nonad_op(name, variant):
+    import flamelet_steady as FS
+    d = FC.golden()
+    g = np.load(FC.GOLD + '/flamelet_nonad_ref.npz')
+    spec, og = pair(FC.BUNDLED[name])
+    v = f'{name}_{variant}_'
+    heat = dict(T_conv=g[v + 'T_conv'], T_rad=g[v + 'T_rad'], h_conv=g[v + 'h_conv'], h_rad=g[v + 'h_rad'],
+                scaled=variant == 'scaled')
+    op = FS.FlameletOperator(og, d[name + '_z'], d[name + '_chi'], d[name + '_oxy'], d[name + '_fuel'],
+                             heat_loss=heat)
+    return g, v, op, spec
+
+
+@pytest.mark.parametrize('name', CASES)
+@pytest.mark.parametrize('variant', ['plain', 'scaled'])
+def test_oracle_nonadiabatic_flamelet_kernels_match_reference(name, variant):
+    """Heat-loss terms (convection and radiation per point; and scaled by the temperature range with the linear
+    reference temperature profile and dissipation-scaled coefficients) against the reference Flamelet's
+    _nonadiabatic_rhs / _nonadiabatic_jac (tests/golden/flamelet_nonad_ref.npz)."""
+    g, v, op, spec = _nonad_op(name, variant)
+    st = g[name + '_state']
+    ns = op.ns
+    assert FC.vec_err(op.rhs(st), g[v + 'rhs'], ns) < 1e-12
+    assert FC.btddod_row_err(op.jac(st), g[v + 'jac'], op.nzi, ns) < 1e-12
+
+
+@pytest.mark.parametrize('name', CASES)
+@pytest.mark.parametrize('variant', ['plain', 'scaled'])
+def test_nonadiabatic_setup_matches_reference(name, variant):
+    """FlameletSetup's heat-loss arrays (flamelet.py:479-519) equal the reference Flamelet's."""
+    from spitfire_gb300.flamelet import FlameletSetup, FlameletSpec
+    g = np.load(FC.GOLD + '/flamelet_nonad_ref.npz')
+    spec, _ = pair(FC.BUNDLED[name])
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case(name))
+    v = f'{name}_{variant}_'
+    if variant == 'plain':
+        hk = dict(heat_transfer='nonadiabatic', convection_temperature=g[v + 'arg_convection_temperature'],
+                  radiation_temperature=g[v + 'arg_radiation_temperature'],
+                  convection_coefficient=g[v + 'arg_convection_coefficient'],
+                  radiative_emissivity=g[v + 'arg_radiative_emissivity'])
+    else:
+        hk = dict(heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                  scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                  convection_coefficient=1.e7, radiative_emissivity=0.5)
+    s = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition='Burke-Schumann', **dict(kw, **hk)))
+    for a, k in ((s.T_conv, 'T_conv'), (s.T_rad, 'T_rad'), (s.h_conv, 'h_conv'), (s.h_rad, 'h_rad')):
+        assert np.allclose(a, g[v + k], rtol=1e-13, atol=0.), k
+    assert s.scale_heat_loss_by_temp_range == (variant == 'scaled')
