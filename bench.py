@@ -55,8 +55,8 @@ N_ADJOINT = 2048
 # (python -m spitfire_gb300.profile_cases jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA) and
 # warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states).
 FP64_PER_STATE = {
-    32: {'kernel': 'chem_kernel<32, MODE_JAC>', 'flops': 105050., 'warp_instr': 4189.},
-    1: {'kernel': 'chem_kernel_tps<MODE_JAC>', 'flops': 96855., 'warp_instr': 2150.},
+    32: {'kernel': 'chem_kernel<32, MODE_JAC>', 'flops': 86953., 'warp_instr': 2816.},
+    1: {'kernel': 'chem_kernel_tps<MODE_JAC>', 'flops': 79842., 'warp_instr': 1733.},
 }
 
 

@@ -209,6 +209,13 @@ __device__ __forceinline__ double scale_pow2(double x, long long K)
   return x * f1 * f2;
 }
 
+// A small integer (a stoichiometric coefficient or a sum of them) as a double: from the blob's table when within
+// -32..31 (a shared-memory load), else converted.
+__device__ __forceinline__ double small_int(const double *table, int k)
+{
+  return (unsigned)(k + 32) < 64u ? table[k + 32] : (double)k;
+}
+
 // ------------------------------------------------------------------------------------------ reaction phase
 // Per-state quantities every reaction needs.
 struct StateCtx {
@@ -467,8 +474,9 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
   scr[L.q + r] = Rnet * Ctbaf;
   if (!JAC) return;
 
-  const double *smallint = b.d + m.d_smallint + 128;
-  const double sum_reac_nu = smallint[(sums >> 16) & 0xFF], sum_prod_nu = smallint[(sums >> 24) & 0xFF];
+  const double *smallint = b.d + m.d_smallint;
+  const double sum_reac_nu = small_int(smallint, (sums >> 16) & 0xFF),
+               sum_prod_nu = small_int(smallint, (sums >> 24) & 0xFF);
   double dRdrho, dRdT;
   if (orders) {
     double sumo = 0.;
@@ -483,7 +491,7 @@ __device__ __forceinline__ void eval_reaction(const DevMech &m, Blob b, const Sc
       const int n0 = b.i[m.i_net_off + r], n1 = b.i[m.i_net_off + r + 1];
       for (int j = n0; j < n1; ++j) {
         const int e = b.i[m.i_net + j];
-        dKc -= smallint[(e >> 16) - 128] * scr[L.dB + (e & 0xFFFF)];
+        dKc -= small_int(smallint, (e >> 16) - 128) * scr[L.dB + (e & 0xFFFF)];
       }
     }
     dRdrho = (Rf * sum_reac_nu - Rr * sum_prod_nu) * s.invRho;

@@ -16,7 +16,12 @@
 
 namespace sfgb {
 
-enum Mode { MODE_RATES = 0, MODE_SENS = 1, MODE_RHS = 2, MODE_JAC = 3 };
+// MODE_RHS_OPEN / MODE_JAC_OPEN: the reactor modes of open (mass-exchange) reactors, compiled with the feed terms;
+// the closed modes compile them out.
+enum Mode { MODE_RATES = 0, MODE_SENS = 1, MODE_RHS = 2, MODE_JAC = 3, MODE_RHS_OPEN = 4, MODE_JAC_OPEN = 5 };
+
+__host__ __device__ constexpr int base_mode(int mode) { return mode >= MODE_RHS_OPEN ? mode - 2 : mode; }
+__host__ __device__ constexpr bool jac_mode(int mode) { return base_mode(mode) == MODE_JAC || mode == MODE_SENS; }
 
 struct KParams {
   DevMech m;
@@ -68,15 +73,17 @@ template <int G, int MODE, class S>
 __device__ __forceinline__ void eval_state(const KParams &p, const DevMech &m, const Blob &b, const ScratchLayout &L,
                                            S scr, const Group<G> &grp, const Progs &pg, const ReactorCfg &cfg, int st)
 {
-  constexpr bool JAC = (MODE == MODE_JAC || MODE == MODE_SENS);
+  constexpr bool JAC = jac_mode(MODE);
+  constexpr bool OPEN = MODE >= MODE_RHS_OPEN;
   const int lane = grp.lane;
   const int ns = m.ns;
   const int neq = p.configuration == 1 ? ns + 1 : ns;
-  if (MODE == MODE_RHS || MODE == MODE_JAC) {
+  if (base_mode(MODE) == MODE_RHS || base_mode(MODE) == MODE_JAC) {
     const double *qs = p.q + (size_t)st * neq;
     const double pres = p.configuration == 1 ? 0. : (p.pressures ? p.pressures[st] : p.pressure);
     GlobalJ gj{JAC ? p.out_J + (size_t)st * neq * neq : nullptr, neq};
-    reactor_eval<G, JAC>(m, b, L, scr, grp, qs, pres, cfg, pg, p.out_rhs + (size_t)st * neq, gj);
+    reactor_eval<G, JAC, default_unroll(G), OPEN>(m, b, L, scr, grp, qs, pres, cfg, pg, p.out_rhs + (size_t)st * neq,
+                                                  gj);
     return;
   }
   // ---------------- production rates / sensitivities at (T, rho, Y)
@@ -150,7 +157,7 @@ __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
   const Blob b = blob_at(m, smem);
   const ScratchLayout &L = p.L;
   const int gid = threadIdx.x / G;
-  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? L.total : L.total_rhs;
+  const int scr_doubles = jac_mode(MODE) ? L.total : L.total_rhs;
   double *scr = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)gid * scr_doubles;
   const Group<G> grp;
   const Progs pg{p.prog_w, p.prog_full, p.prog_j};
@@ -174,7 +181,7 @@ __global__ void __launch_bounds__(128) chem_kernel_tps(const KParams p)
   const int lane = threadIdx.x & 31;
   const int wg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int nwg = gridDim.x * (blockDim.x >> 5);
-  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? L.total : L.total_rhs;
+  const int scr_doubles = jac_mode(MODE) ? L.total : L.total_rhs;
   const ScrStrided scr{p.gscratch + (size_t)wg * scr_doubles * 32 + lane};
   const Group<1> grp;
   const Progs pg{p.prog_w, p.prog_full, p.prog_j};
@@ -229,7 +236,7 @@ int launch_tps(HostMech &hm, KParams &p, cudaStream_t st)
   p.prog_full = progs.progs[1];
   p.prog_j = (MODE == MODE_SENS) ? progs.progs[3] : progs.progs[2];
   if (p.n == 0) return SF_OK;
-  const size_t per_warp = (size_t)32 * ((MODE == MODE_JAC || MODE == MODE_SENS) ? hm.sl.total : hm.sl.total_rhs) * 8;
+  const size_t per_warp = (size_t)32 * (jac_mode(MODE) ? hm.sl.total : hm.sl.total_rhs) * 8;
   const int warps_avail = (int)std::min<size_t>(hm.tps_scratch_bytes / per_warp, (size_t)1 << 30);
   if (warps_avail < kTpsThreads / 32)
     throw sf_error(SF_ERR_UNSUPPORTED, "thread-per-state scratch not allocated (set the lanes-per-state knob to 1)");
@@ -256,7 +263,7 @@ int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
   p.prog_w = progs.progs[0];
   p.prog_full = progs.progs[1];
   p.prog_j = (MODE == MODE_SENS) ? progs.progs[3] : progs.progs[2];
-  const int scr_doubles = (MODE == MODE_JAC || MODE == MODE_SENS) ? hm.sl.total : hm.sl.total_rhs;
+  const int scr_doubles = jac_mode(MODE) ? hm.sl.total : hm.sl.total_rhs;
   int dev;
   CUDA_THROW(cudaGetDevice(&dev));
   int smem_max, nsm;
@@ -294,8 +301,8 @@ int chem_launch(HostMech &hm, int mode, KParams &p, cudaStream_t st, int G)
   switch (mode) {
   case MODE_RATES: return launch_mode<MODE_RATES>(hm, p, st, G);
   case MODE_SENS: return launch_mode<MODE_SENS>(hm, p, st, G);
-  case MODE_RHS: return launch_mode<MODE_RHS>(hm, p, st, G);
-  default: return launch_mode<MODE_JAC>(hm, p, st, G);
+  case MODE_RHS: return p.open ? launch_mode<MODE_RHS_OPEN>(hm, p, st, G) : launch_mode<MODE_RHS>(hm, p, st, G);
+  default: return p.open ? launch_mode<MODE_JAC_OPEN>(hm, p, st, G) : launch_mode<MODE_JAC>(hm, p, st, G);
   }
 }
 

@@ -238,8 +238,8 @@ void HostMech::build(const sf_mech_desc *d)
   m.d_ord = dsec(nord);
   m.d_one = dsec(1);
   D[m.d_one] = 1.;
-  m.d_smallint = dsec(256);
-  for (int k = 0; k < 256; ++k) D[m.d_smallint + k] = k - 128;
+  m.d_smallint = dsec(64);
+  for (int k = 0; k < 64; ++k) D[m.d_smallint + k] = k - 32;
   m.i_info = isec(nr);
   m.i_orig = isec(nr);
   for (int r = 0; r < nr; ++r) I[m.i_orig + r] = orig_index[r];

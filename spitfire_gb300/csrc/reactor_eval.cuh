@@ -189,8 +189,11 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   if (c.heat == 2)
     qheat = c.SoV / (rho * cmix) * (c.hc * (c.Tc - T) + c.eps * 5.67e-8 * (c.Tr * c.Tr * c.Tr * c.Tr - T * T * T * T));
   const int tix = isochoric ? 1 : 0;  // index of T in the state
-  for (int i = lane; i < ns - 1; i += G)
-    rhs[tix + 1 + i] = scr[L.w + i] * invRho + (open_ ? (c.yin[i] - scr[L.y + i]) * mfac : 0.);
+  for (int i = lane; i < ns - 1; i += G) {
+    double v = scr[L.w + i] * invRho;
+    if (open_) v += (c.yin[i] - scr[L.y + i]) * mfac;
+    rhs[tix + 1 + i] = v;
+  }
   if (lane == 0) {
     if (isochoric) rhs[0] = open_ ? (c.rho_in - rho) * itau : 0.;
     rhs[tix] = c.heat == 1 ? 0. : (open_ ? rhsT + qheat + mrT : rhsT + qheat);
@@ -205,8 +208,9 @@ __device__ void reactor_eval(const DevMech &m, const Blob &b, const ScratchLayou
   const double cpv_last = scr[L.cpv + ns - 1];
   if (isochoric) {
     for (int i = lane; i < ns - 1; i += G) {
-      const double mr = open_ ? (c.yin[i] - scr[L.y + i]) * mfac : 0.;
-      jset(2 + i, 0, invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]) - mr * invRho);
+      double v = invRho * (scr[L.Srho + i] - invRho * scr[L.w + i]);
+      if (open_) v -= (c.yin[i] - scr[L.y + i]) * mfac * invRho;
+      jset(2 + i, 0, v);
       jset(2 + i, 1, invRho * scr[L.ST + i]);
     }
   } else {

@@ -44,7 +44,8 @@ struct DevMech {
   int d_netc;    // [net entries] -nu*M (coefficient of q_r in w_i)
   int d_ord;     // [order entries] special orders
   int d_one;     // 1.0
-  int d_smallint;  // [256] the integer k - 128 at index k (stoichiometric coefficients without conversions)
+  int d_smallint;  // [64] the integer k - 32 at index k (stoichiometric coefficients without conversions); kept
+                   // small because every kernel stages the blob into shared memory
 
   // ---- int section offsets ----
   int i_info;    // [nr]
