@@ -52,11 +52,13 @@ N_REACTORS = 8192
 N_FLAMELETS = 64
 N_ADJOINT = 2048
 # Per GRI state of each Jacobian kernel the autotuner can choose, from ncu on the profiling cases
-# (python -m spitfire_gb300.profile_cases jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA) and
-# warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states).
+# (python -m spitfire_gb300.profile_cases jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA),
+# warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states) and DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum / states; the 8192-state case of the lane-group kernel keeps part of
+# its Jacobians in L2 at the end, so its figure is a lower bound).
 FP64_PER_STATE = {
-    32: {'kernel': 'chem_kernel<32, MODE_JAC>', 'flops': 86953., 'warp_instr': 2816.},
-    1: {'kernel': 'chem_kernel_tps<MODE_JAC>', 'flops': 79842., 'warp_instr': 1733.},
+    32: {'kernel': 'chem_kernel<32, MODE_JAC>', 'flops': 86953., 'warp_instr': 2816., 'dram_bytes': 18725.},
+    1: {'kernel': 'chem_kernel_tps<MODE_JAC>', 'flops': 79842., 'warp_instr': 1733., 'dram_bytes': 124314.},
 }
 
 
@@ -586,7 +588,7 @@ def main():
     tuned = AT.tune_chemistry(spec, qh, kinds=('jac',))
     group = tuned['group_jac'][0]
     kern = FP64_PER_STATE.get(group, {'kernel': f'chem_kernel<{group}, MODE_JAC>', 'flops': None,
-                                      'warp_instr': None})
+                                      'warp_instr': None, 'dram_bytes': None})
 
     def step():
         g.reactor_jac_batch(P, q, 0, out_rhs=rhs, out_jac=J)
@@ -666,7 +668,10 @@ def main():
     else:
         roof['achieved'] = None
         roof['frac'] = None
-    roof['traffic'] = None
+    # DRAM bytes of one launch: the ncu figure per state times the states of a launch
+    roof['traffic'] = kern['dram_bytes'] * N_STATES if kern.get('dram_bytes') else None
+    roof['traffic_source'] = 'ncu dram__bytes_read.sum + dram__bytes_write.sum per state on the profiling case ' \
+                             '(python -m spitfire_gb300.profile_cases jac_tps | jac), scaled to the launch'
     issue = C.c_double()
     N.check(N.load().sf_fp64_issue_probe(4000, 32, C.byref(issue), N.ptr(sink), N.stream_handle()))
     if kern['warp_instr']:
