@@ -617,10 +617,9 @@ def main():
     J_h = torch.empty((N_STATES, neq * neq), dtype=torch.float64).pin_memory()
 
     def e2e_step():
-        q.copy_(qpin, non_blocking=True)
-        g.reactor_jac_batch(P, q, 0, out_rhs=rhs, out_jac=J)
-        rhs_h.copy_(rhs, non_blocking=True)
-        J_h.copy_(J, non_blocking=True)
+        # the host-buffer entry point (sf_reactor_jac_host_batch): states in, results out, the copies back of one
+        # chunk overlapping the next chunk's kernel
+        g.reactor_jac_host_batch(P, qpin, rhs_h, J_h)
 
     for _ in range(2):
         e2e_step()
@@ -634,7 +633,9 @@ def main():
     e1.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
     e2e = {'value': world * N_STATES / (e2e_ms * 1e-3), 'unit': 'states/s', 'ms_per_step': e2e_ms,
-           'h2d_bytes_per_step': qpin.numel() * 8, 'd2h_bytes_per_step': (rhs_h.numel() + J_h.numel()) * 8}
+           'h2d_bytes_per_step': qpin.numel() * 8, 'd2h_bytes_per_step': (rhs_h.numel() + J_h.numel()) * 8,
+           'api': 'PyCombustionKernels.reactor_jac_host_batch -> sf_reactor_jac_host_batch (pinned host buffers; '
+                  'chunks of one resident wave, device-to-host copies overlapping the next chunk)'}
 
     # ---------------- comparison point: the plain single-state GPU form on the same states
     ws = torch.empty(N.load().sf_reactor_jac_plain_workspace_size(g.handle, N_STATES) // 8 + 1,

@@ -180,6 +180,19 @@ typedef struct sf_reactor_params {
   double surface_area_to_volume;
 } sf_reactor_params;
 
+/* Reactor right-hand sides and Jacobians of n states held in HOST memory, as the reference's
+ * reactor_jac_isochoric / reactor_jac_isobaric take them (griffon.pyx:807-866): the states (and optional per-state
+ * pressures) are copied in on `stream`, the Jacobians computed in chunks of chunk_states states (<= 0: one wave of
+ * the thread-per-state kernel's resident warps when the autotuner selected it, else half the batch), and each
+ * chunk's results copied back on a second stream while the next chunk computes. `stream` is ordered after the last
+ * copy. Pinned host buffers let the copies run asynchronously. workspace: DEVICE, at least
+ * sf_reactor_jac_host_workspace_size bytes. */
+size_t sf_reactor_jac_host_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
+int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *params, int rates_option, int n,
+                              const double *q_host, const double *pressures_host, double *out_rhs_host,
+                              double *out_jac_host, int chunk_states, void *workspace, size_t workspace_bytes,
+                              void *stream);
+
 /* Right-hand side of n reactors (state-major q, out_rhs). If pressures is non-NULL (isobaric) it gives one
  * pressure per state and overrides params->pressure.
  * Replaces reactor_rhs_isobaric / reactor_rhs_isochoric (isobaric_reactor_kernels.cpp:170-219,

@@ -37,6 +37,10 @@ def _declare(L):
     L.sf_rates_sens_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _ip, _vp, _vp, _vp]
     L.sf_reactor_rhs_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp]
     L.sf_reactor_jac_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _vp]
+    L.sf_reactor_jac_host_workspace_size.argtypes = [_vp, C.POINTER(SfReactorParams), _ip]
+    L.sf_reactor_jac_host_workspace_size.restype = C.c_size_t
+    L.sf_reactor_jac_host_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _ip, _vp,
+                                            C.c_size_t, _vp]
     L.sf_reactor_jac_plain_workspace_size.argtypes = [_vp, _ip]
     L.sf_reactor_jac_plain_workspace_size.restype = C.c_size_t
     L.sf_reactor_jac_plain_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp, _vp,
@@ -68,7 +72,8 @@ def _declare(L):
 # Entry points declared in include/spitfire_gb300.h (the C-ABI test checks the library exports all of them).
 EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 'sf_mech_info', 'sf_device_status',
             'sf_thermo_batch', 'sf_production_rates_batch', 'sf_rates_sens_batch', 'sf_reactor_rhs_batch',
-            'sf_reactor_jac_batch', 'sf_reactor_jac_plain_workspace_size', 'sf_reactor_jac_plain_batch',
+            'sf_reactor_jac_batch', 'sf_reactor_jac_host_workspace_size', 'sf_reactor_jac_host_batch',
+            'sf_reactor_jac_plain_workspace_size', 'sf_reactor_jac_plain_batch',
             'sf_reactor_jac_plain_batch_static',
             'sf_newton_lu_batch', 'sf_newton_solve_batch', 'sf_integrate_workspace_size', 'sf_integrate_batch',
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',

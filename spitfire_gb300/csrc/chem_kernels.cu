@@ -542,6 +542,84 @@ int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int r
   });
 }
 
+size_t sf_reactor_jac_host_workspace_size(const sf_mech *mech, const sf_reactor_params *rp, int n)
+{
+  if (!mech || !rp || n < 0) return 0;
+  const size_t neq = (size_t)mech->m.dm.ns + (rp->configuration == 1 ? 1 : 0);
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8) + up(n * neq * neq * 8);
+}
+
+int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n,
+                              const double *q_host, const double *pressures_host, double *out_rhs_host,
+                              double *out_jac_host, int chunk_states, void *workspace, size_t workspace_bytes,
+                              void *stream)
+{
+  return guard([&]() -> int {
+    if (!mech || !rp || n < 0 || (n > 0 && (!q_host || !out_rhs_host || !out_jac_host)))
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    if (rates_option < 0 || rates_option > 2) throw sf_error(SF_ERR_INVALID_ARGUMENT, "rates option must be 0, 1 or 2");
+    if (n == 0) return SF_OK;
+    if (!workspace || workspace_bytes < sf_reactor_jac_host_workspace_size(mech, rp, n))
+      throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_reactor_jac_host_workspace_size reports");
+    HostMech &hm = const_cast<HostMech &>(mech->m);
+    const size_t neq = (size_t)hm.dm.ns + (rp->configuration == 1 ? 1 : 0);
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char *w = static_cast<char *>(workspace);
+    double *q = reinterpret_cast<double *>(w);
+    double *pr = reinterpret_cast<double *>(w + up(n * neq * 8));
+    double *rhs = reinterpret_cast<double *>(w + up(n * neq * 8) + up((size_t)n * 8));
+    double *J = reinterpret_cast<double *>(w + up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int G = group_of(hm, SF_TUNE_GROUP_JAC);
+    // chunk: by default the states one wave of the thread-per-state kernel covers (its resident warps), else half
+    int chunk = chunk_states;
+    if (chunk <= 0) {
+      if (G == 1 && hm.tps_scratch_bytes) {
+        const size_t per_warp = (size_t)32 * hm.sl.total * 8;
+        chunk = (int)std::min<size_t>((size_t)n, hm.tps_scratch_bytes / per_warp * 32);
+      } else {
+        chunk = (n + 1) / 2;
+      }
+    }
+    chunk = std::max(1, std::min(chunk, n));
+    const int nchunks = (n + chunk - 1) / chunk;
+    if (!hm.copy_stream) CUDA_THROW(cudaStreamCreateWithFlags(&hm.copy_stream, cudaStreamNonBlocking));
+    while ((int)hm.events.size() < nchunks + 1) {
+      cudaEvent_t e;
+      CUDA_THROW(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      hm.events.push_back(e);
+    }
+    // inputs, then per chunk: the Jacobians on the caller's stream and their copies back on the copy stream, so that
+    // a chunk's copies overlap the next chunk's kernel
+    CUDA_THROW(cudaMemcpyAsync(q, q_host, n * neq * 8, cudaMemcpyHostToDevice, st));
+    if (pressures_host) CUDA_THROW(cudaMemcpyAsync(pr, pressures_host, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    for (int c = 0; c < nchunks; ++c) {
+      const size_t a = (size_t)c * chunk;
+      const int m = (int)std::min<size_t>(chunk, n - a);
+      KParams p{};
+      fill_reactor(p, rp);
+      p.n = m;
+      p.q = q + a * neq;
+      p.pressures = pressures_host ? pr + a : nullptr;
+      p.option = rates_option;
+      p.out_rhs = rhs + a * neq;
+      p.out_J = J + a * neq * neq;
+      const int rc = chem_launch(hm, MODE_JAC, p, st, G);
+      if (rc != SF_OK) return (int)rc;
+      CUDA_THROW(cudaEventRecord(hm.events[c], st));
+      CUDA_THROW(cudaStreamWaitEvent(hm.copy_stream, hm.events[c], 0));
+      CUDA_THROW(cudaMemcpyAsync(out_rhs_host + a * neq, rhs + a * neq, (size_t)m * neq * 8, cudaMemcpyDeviceToHost,
+                                 hm.copy_stream));
+      CUDA_THROW(cudaMemcpyAsync(out_jac_host + a * neq * neq, J + a * neq * neq, (size_t)m * neq * neq * 8,
+                                 cudaMemcpyDeviceToHost, hm.copy_stream));
+    }
+    CUDA_THROW(cudaEventRecord(hm.events[nchunks], hm.copy_stream));
+    CUDA_THROW(cudaStreamWaitEvent(st, hm.events[nchunks], 0));
+    return SF_OK;
+  });
+}
+
 int sf_device_status(const sf_mech *mech, int clear)
 {
   if (!mech || !mech->m.d_status) return -1;

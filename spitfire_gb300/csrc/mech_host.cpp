@@ -29,6 +29,8 @@ HostMech::~HostMech()
   if (d_blob) cudaFree(d_blob);
   if (d_status) cudaFree(d_status);
   if (tps_scratch) cudaFree(tps_scratch);
+  for (cudaEvent_t e : events) cudaEventDestroy(e);
+  if (copy_stream) cudaStreamDestroy(copy_stream);
 }
 
 void HostMech::build(const sf_mech_desc *d)

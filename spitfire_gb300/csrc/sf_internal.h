@@ -49,6 +49,8 @@ struct HostMech {
   int tune[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // launch shapes chosen by the autotuner (sf_tune_knob), 0 = default
   double *tps_scratch = nullptr;           // interleaved scratch of the thread-per-state kernels
   size_t tps_scratch_bytes = 0;
+  cudaStream_t copy_stream = nullptr;      // host-buffer entry points: device-to-host copies overlapping compute
+  std::vector<cudaEvent_t> events;         // their chunk-completion events (created on first use)
 
   struct Programs {
     DevProgram progs[4]{};  // 0: w only, 1: w/S_rho/S_T/P/Q, 2: Y block + T row, 3: all species rows (sens)

@@ -161,6 +161,24 @@ class PyCombustionKernels(GriffonSetters):
                                               N.ptr(pr), N.ptr(out_rhs), N.ptr(out_jac), N.stream_handle()))
         return out_rhs, out_jac
 
+    def reactor_jac_host_batch(self, params, q, out_rhs, out_jac, rates_option=0, pressures=None, chunk_states=0):
+        """RHS and Jacobian of states in HOST memory into host outputs (sf_reactor_jac_host_batch): q [n, neq],
+        out_rhs [n, neq], out_jac [n, neq*neq] (torch CPU tensors, pinned for asynchronous copies, or numpy arrays);
+        the copies back overlap the computation of the next chunk. Returns on the current stream without waiting."""
+        torch = _torch()
+        import ctypes as C
+        n = q.shape[0]
+        L = N.load()
+        need = int(L.sf_reactor_jac_host_workspace_size(self.handle, C.byref(params), n))
+        ws = getattr(self, '_host_ws', None)
+        if ws is None or ws.numel() * 8 < need:
+            self._host_ws = ws = torch.empty(need // 8 + 1, dtype=torch.float64, device='cuda')
+        hp = lambda a: (a.data_ptr() if hasattr(a, 'data_ptr') else a.ctypes.data) if a is not None else None
+        N.check(L.sf_reactor_jac_host_batch(self.handle, C.byref(params), int(rates_option), n, hp(q), hp(pressures),
+                                            hp(out_rhs), hp(out_jac), int(chunk_states), N.ptr(ws), ws.numel() * 8,
+                                            N.stream_handle()))
+        return out_rhs, out_jac
+
     def reactor_jac_plain_batch(self, params, q, pressures=None, workspace=None):
         """Plain single-state GPU form (one thread per state), the comparison point of the batched kernel."""
         torch = _torch()

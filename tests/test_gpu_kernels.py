@@ -263,3 +263,37 @@ def test_open_reactor_rhs_jac(cuda, name, configuration, heat, group):
         assert g.device_status() == 0
     finally:
         _tps_off(spec)
+
+
+@pytest.mark.parametrize('group', [0, 1])
+def test_host_buffer_jacobians_match_device_path(cuda, group):
+    """sf_reactor_jac_host_batch (host states in, host results out, chunked with overlapped copies) gives the
+    device entry point's results bit for bit, for pinned and pageable buffers and several chunk sizes."""
+    import torch
+    from spitfire_gb300 import autotune as AT
+    spec, og = pair('methane-gri30')
+    g = spec.griffon
+    n = 3000
+    d = W.gri_states(spec, n, seed=41)
+    qh = W.isochoric_state(d)
+    neq = qh.shape[1]
+    P = reactor_params('isochoric')
+    try:
+        if group:
+            AT.set_tuning(spec, 'group_jac', 1)
+        r_ref, J_ref = g.reactor_jac_batch(P, qh, 0)
+        r_ref, J_ref = gpu_np(r_ref), gpu_np(J_ref)
+        for chunk in (0, 1000, 777, n):
+            qp = torch.from_numpy(qh).pin_memory()
+            rh = torch.empty((n, neq), dtype=torch.float64).pin_memory()
+            Jh = torch.empty((n, neq * neq), dtype=torch.float64).pin_memory()
+            g.reactor_jac_host_batch(P, qp, rh, Jh, chunk_states=chunk)
+            torch.cuda.synchronize()
+            assert np.array_equal(rh.numpy(), r_ref) and np.array_equal(Jh.numpy(), J_ref), chunk
+        rn, Jn = np.zeros((n, neq)), np.zeros((n, neq * neq))
+        g.reactor_jac_host_batch(P, np.ascontiguousarray(qh), rn, Jn, chunk_states=1234)
+        torch.cuda.synchronize()
+        assert np.array_equal(rn, r_ref) and np.array_equal(Jn, J_ref)
+        assert g.device_status() == 0
+    finally:
+        _tps_off(spec)
