@@ -6,6 +6,8 @@ Cases (GRI-3.0 unless stated; each ends by checking the device error word):
   jac        isochoric RHS + Jacobian of 8192 states (chem_kernel MODE_JAC), 3 launches
   jac_tps    the same with the thread-per-state kernel (chem_kernel_tps MODE_JAC) at 2 resident 4-warp blocks per
              SM, on 38912 states (one warp batch per resident warp), 2 launches
+  rates_rhs  production rates (chem_kernel_tps MODE_RATES) and the isochoric right-hand side (MODE_RHS) of 38912
+             states, thread per state at 2 resident 4-warp blocks per SM, 2 launches each
   integrate  256 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s (integrate_kernel)
   flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
              block-Thomas factorization, solve and matvec
@@ -49,6 +51,31 @@ def case_jac_tps():
     P = reactor_params('isochoric')
     for _ in range(2):
         spec.griffon.reactor_jac_batch(P, q, 0)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_rates_rhs():
+    import torch
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    AT.set_tuning(spec, 'tps_ctas', 2)
+    AT.set_tuning(spec, 'group_rates', 1)
+    AT.set_tuning(spec, 'group_rhs', 1)
+    n = torch.cuda.get_device_properties(0).multi_processor_count * 2 * 4 * 32
+    d = W.gri_states(spec, n)
+    g = spec.griffon
+    q = torch.tensor(W.isochoric_state(d), device='cuda')
+    T = torch.tensor(d['T'], device='cuda')
+    rho = torch.tensor(d['rho'], device='cuda')
+    Y = torch.tensor(d['Y'], device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(2):
+        g.production_rates_batch(T, rho, Y)
+    for _ in range(2):
+        g.reactor_rhs_batch(P, q)
     torch.cuda.synchronize()
     return spec
 
@@ -105,7 +132,7 @@ def case_fp64issue():
     return None
 
 
-CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
+CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
          'fp64issue': case_fp64issue}
 
 
