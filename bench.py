@@ -297,6 +297,10 @@ def bench_newton(q, rhs, J, gamma_h, stream):
     return out
 
 
+# integrator memory placement knob: Griffon scratch and iteration matrix in shared memory or L2-resident global slots
+PLACEMENT = {0: 'shared', 1: 'global scratch', 2: 'global scratch + matrix'}
+
+
 def bench_ignition(spec, rank, stream, cpu):
     import numpy as np
     import torch
@@ -326,9 +330,8 @@ def bench_ignition(spec, rank, stream, cpu):
            'status_counts': {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
            'steps': {'min': int(steps.min()), 'median': float(np.median(steps)), 'max': int(steps.max())},
            'device_status': spec.griffon.device_status(),
-           'autotune': {'chosen': {'scratch': 'global' if best[0] else 'shared', 'warps_per_block': best[1]},
-                        'candidates_ms_1024_reactors': {f'{"global" if k[0] else "shared"}/{k[1]}w': v
-                                                        for k, v in cand.items()}}}
+           'autotune': {'chosen': {'placement': PLACEMENT[best[0]], 'warps_per_block': best[1]},
+                        'candidates_ms_1024_reactors': {f'{PLACEMENT[k[0]]}/{k[1]}w': v for k, v in cand.items()}}}
     # FP32-LU + FP64-refinement integrator on the first 512 reactors against the FP64 run
     o32 = BatchIntegrator(spec, 'isobaric', linear_precision=1, refine_sweeps=2).run(
         d['q0'][:512], pressures=d['p'][:512], **kw)

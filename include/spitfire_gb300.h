@@ -125,7 +125,8 @@ int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *cou
  *     mechanism allocates when the knob is set);
  *   SF_TUNE_INTEGRATE_WARPS: warps (reactors) per block of sf_integrate_batch, 1..8 (0: as many as fit);
  *   SF_TUNE_INTEGRATE_SCRATCH: 1 keeps each integrating warp's Griffon scratch in global memory (L2-resident)
- *     instead of shared memory, so that more warps fit per SM (0: shared memory);
+ *     instead of shared memory, so that more warps fit per SM; 2 also its iteration matrix and FP32 factors
+ *     (0: shared memory);
  *   SF_TUNE_TPS_CTAS: resident 4-warp blocks per SM of the thread-per-state kernels, 1..16 (0: as many as fit);
  *     fewer keep more of their interleaved scratch in L2.
  * The integrator knobs do not change results; the lane-group width changes the order of per-species sums, so those

@@ -4,8 +4,9 @@ For one mechanism on the current device it times the candidate shapes on a sampl
 CUDA events and applies the fastest through ``sf_mech_set_tuning``:
   * lanes per state (8, 16, 32, or 1: the thread-per-state kernels, with their resident blocks per SM) of the
     production-rate, right-hand-side and Jacobian kernels;
-  * for the persistent ESDIRK64 integrator: where each warp keeps its Griffon scratch (shared memory, or an
-    L2-resident global slot, which leaves room for more warps per SM) and how many warps (reactors) share a block.
+  * for the persistent ESDIRK64 integrator: where each warp keeps its Griffon scratch and iteration matrix (shared
+    memory, or L2-resident global slots, which leave room for more warps per SM) and how many warps (reactors)
+    share a block.
 The knobs change launch shapes only. The integrator's candidates produce bit-identical results; the lane-group
 width changes the order of the per-species sums, so those candidates agree to rounding (the tuner checks both).
 Choices are cached per (mechanism, device) in spitfire_gb300/_tuning (created on first use).
@@ -131,14 +132,15 @@ def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kind
 
 
 def tune_integrator(integrator, q0, pressures=None, reps=1, **controls):
-    """Choose the integrator's scratch placement and warps per block on a sample batch (q0 rows). Returns
-    (best (scratch, warps), {(scratch, warps): ms})."""
+    """Choose the integrator's memory placement and warps per block on a sample batch (q0 rows): scratch 0 (all in
+    shared memory), 1 (Griffon scratch in an L2-resident global slot per warp) or 2 (the iteration matrix there
+    too). Returns (best (scratch, warps), {(scratch, warps): ms})."""
     torch = _torch()
     mech = integrator.mech
     times = {}
     ref = None
     saved = (get_tuning(mech, 'integrate_scratch'), get_tuning(mech, 'integrate_warps'))
-    for scratch in (0, 1):
+    for scratch in (0, 1, 2):
         set_tuning(mech, 'integrate_scratch', scratch)
         set_tuning(mech, 'integrate_warps', 0)
         fit = _fitting_warps(integrator)
@@ -168,9 +170,11 @@ def _fitting_warps(integrator):
     # per-warp doubles as the integrator lays them out (integrate_kernels.cu per_warp_doubles)
     lay = h.scratch_layout()
     neq = integrator.mech.n_species + (1 if integrator.configuration == 'isochoric' else 0)
-    gs = get_tuning(integrator.mech, 'integrate_scratch') == 1
-    per = neq * neq + 12 * neq + (0 if gs else lay['total']) + \
-        ((neq * neq + 1) // 2 + neq if integrator.linear_precision == 1 else 0) + (neq + 1) // 2 + 2
+    place = get_tuning(integrator.mech, 'integrate_scratch')
+    gs, gm = place >= 1, place == 2
+    n2 = neq * neq
+    per = (0 if gm else n2) + 12 * neq + (0 if gs else lay['total']) + \
+        (((0 if gm else (n2 + 1) // 2) + neq) if integrator.linear_precision == 1 else 0) + (neq + 1) // 2 + 2
     return int(max(1, min(8, (smem - lay['blob_bytes'] - 64) // (per * 8))))
 
 

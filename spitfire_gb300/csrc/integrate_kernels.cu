@@ -65,6 +65,8 @@ struct IntParams {
   double *rec;      // optional trajectory record: [n][rec_cap][2 + 6 neq] = (t_n, dt_n, stage values Y_1..Y_6)
   int rec_cap;
   double *gscratch; // if set: Griffon scratch of every resident warp in global memory ([grid * warps][L.total])
+  double *gmat;     // if set: iteration matrix (and FP32 factors) of every resident warp in global memory
+  size_t mat_doubles;
   int warps;
 };
 
@@ -123,8 +125,10 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   const int neq = p.neq;
   const sf_integrate_params &ip = p.ip;
   double *base = reinterpret_cast<double *>(smem + m.blob_bytes) + (size_t)warp * p.per_warp;
-  double *A = base;                                       // neq*neq
-  double *y = A + neq * neq;                              // current state
+  const size_t slot = (size_t)blockIdx.x * p.warps + warp;  // this warp's global slots
+  // iteration matrix: in shared memory, or with the FP32 factors in this warp's global slot (L2-resident)
+  double *A = p.gmat ? p.gmat + slot * p.mat_doubles : base;  // neq*neq
+  double *y = p.gmat ? base : A + neq * neq;              // current state
   double *Y = y + neq;                                    // stage iterate
   double *res = Y + neq;                                  // Newton residual / step update
   double *f = res + neq;                                  // RHS at the iterate
@@ -132,11 +136,13 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   double *x = prior + neq;                                // linear-solve work vector
   double *k = x + neq;                                    // 6 stage derivatives
   // Griffon scratch: in shared memory, or in this warp's slot of the global scratch array (L2-resident)
-  double *scr = p.gscratch ? p.gscratch + ((size_t)blockIdx.x * p.warps + warp) * L.total : k + 6 * neq;
+  double *scr = p.gscratch ? p.gscratch + slot * L.total : k + 6 * neq;
   double *after = p.gscratch ? k + 6 * neq : scr + L.total;
-  float *LU32 = reinterpret_cast<float *>(after);         // FP32 factors (precision 1)
-  float *xf = reinterpret_cast<float *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 : 0));  // 2*neq floats
-  int *piv = reinterpret_cast<int *>(after + (p.prec == 1 ? (neq * neq + 1) / 2 + neq : 0));
+  const int lu32_doubles = (p.prec == 1 && !p.gmat) ? (neq * neq + 1) / 2 : 0;
+  // FP32 factors (precision 1)
+  float *LU32 = p.gmat ? reinterpret_cast<float *>(A + neq * neq) : reinterpret_cast<float *>(after);
+  float *xf = reinterpret_cast<float *>(after + lu32_doubles);  // 2*neq floats
+  int *piv = reinterpret_cast<int *>(after + (p.prec == 1 ? lu32_doubles + neq : 0));
   float *rf = xf + neq;
   const int Tidx = p.cfg.configuration == 1 ? 1 : 0;
   NoJ noj;
@@ -349,15 +355,24 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   }
 }
 
-size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scratch)
+// Shared memory per warp. global_scratch: the Griffon scratch lives in a global slot; global_matrix: the iteration
+// matrix and the FP32 factors too, leaving the vectors and pivots in shared memory.
+size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scratch, bool global_matrix)
 {
-  return (size_t)neq * neq + 12 * (size_t)neq + (global_scratch ? 0 : hm.sl.total) +
-         (prec == 1 ? ((size_t)neq * neq + 1) / 2 + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2;
+  const size_t n2 = (size_t)neq * neq;
+  return (global_matrix ? 0 : n2) + 12 * (size_t)neq + (global_scratch ? 0 : hm.sl.total) +
+         (prec == 1 ? (global_matrix ? 0 : (n2 + 1) / 2) + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2;
+}
+
+size_t matrix_doubles(int neq, int prec)
+{
+  const size_t n2 = (size_t)neq * neq;
+  return n2 + (prec == 1 ? (n2 + 1) / 2 : 0);
 }
 
 struct IntShape {
   int warps, grid;
-  size_t per_warp, smem, scratch_bytes;
+  size_t per_warp, smem, scratch_bytes, mat_bytes;
 };
 
 // Warps per block and grid of the persistent launch (autotuned knobs, else as many warps as fit)
@@ -368,8 +383,8 @@ IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n)
   CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   IntShape s{};
-  const bool gs = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] == 1;
-  s.per_warp = per_warp_doubles(hm, neq, prec, gs);
+  const bool gs = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] >= 1, gm = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] == 2;
+  s.per_warp = per_warp_doubles(hm, neq, prec, gs, gm);
   const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
   int fit = (int)std::min<size_t>(8, avail / (s.per_warp * 8));
   if (fit < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory integrator");
@@ -379,6 +394,7 @@ IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n)
   const int per_sm = std::max(1, (int)((size_t)smem_max / s.smem));
   s.grid = (int)std::max<long long>(1, std::min<long long>((long long)nsm * per_sm, ((long long)n + s.warps - 1) / s.warps));
   s.scratch_bytes = gs ? (size_t)nsm * per_sm * s.warps * hm.sl.total * 8 : 0;
+  s.mat_bytes = gm ? (size_t)nsm * per_sm * s.warps * matrix_doubles(neq, prec) * 8 : 0;
   return s;
 }
 
@@ -397,7 +413,7 @@ size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params 
     const int neq = params->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
     // both linear precisions: the larger of the two scratch needs
     const IntShape a = integrate_shape(hm, neq, 0, n < 1 ? 1 : n), b = integrate_shape(hm, neq, 1, n < 1 ? 1 : n);
-    return 256 + std::max(a.scratch_bytes, b.scratch_bytes);
+    return 256 + std::max(a.scratch_bytes + a.mat_bytes, b.scratch_bytes + b.mat_bytes);
   } catch (...) {
     return 256;
   }
@@ -468,11 +484,14 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.rec = record;
     p.rec_cap = record_cap;
     const IntShape sh = integrate_shape(hm, p.neq, p.prec, n);
-    if (workspace_bytes < 256 + sh.scratch_bytes)
+    if (workspace_bytes < 256 + sh.scratch_bytes + sh.mat_bytes)
       throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_integrate_workspace_size reports");
     p.per_warp = sh.per_warp;
     p.warps = sh.warps;
     p.gscratch = sh.scratch_bytes ? reinterpret_cast<double *>(static_cast<char *>(workspace) + 256) : nullptr;
+    p.gmat = sh.mat_bytes ? reinterpret_cast<double *>(static_cast<char *>(workspace) + 256 + sh.scratch_bytes)
+                          : nullptr;
+    p.mat_doubles = matrix_doubles(p.neq, p.prec);
     auto kern = p.cfg.open ? integrate_kernel<true> : integrate_kernel<false>;
     CUDA_THROW(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
     cudaStream_t st = (cudaStream_t)stream;
