@@ -332,6 +332,21 @@ def bench_ignition(spec, rank, stream, cpu):
            'device_status': spec.griffon.device_status(),
            'autotune': {'chosen': {'placement': PLACEMENT[best[0]], 'warps_per_block': best[1]},
                         'candidates_ms_1024_reactors': {f'{PLACEMENT[k[0]]}/{k[1]}w': v for k, v in cand.items()}}}
+    # comparison point: the plain single-state GPU form (one thread per reactor, same step logic) on the same batch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    outp = bi.run_plain(d['q0'], pressures=d['p'], **kw)
+    e1.record(stream)
+    e1.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    tp = outp['t'].cpu().numpy()
+    same = outp['counts'][:, 0].cpu().numpy() == steps
+    res['plain_gpu_form'] = {'value': world * N_REACTORS / (plain_ms * 1e-3), 'unit': 'ignitions/s', 'ms': plain_ms,
+                             'speedup_batched_over_plain': plain_ms / ms,
+                             'tau_rel_diff_vs_batched_max': float(np.max(np.abs(tp - tau) / tau)),
+                             'steps_equal_fraction': float(same.mean())}
+    del outp
     # FP32-LU + FP64-refinement integrator on the first 512 reactors against the FP64 run
     o32 = BatchIntegrator(spec, 'isobaric', linear_precision=1, refine_sweeps=2).run(
         d['q0'][:512], pressures=d['p'][:512], **kw)

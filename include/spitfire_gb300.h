@@ -298,6 +298,16 @@ int sf_integrate_batch(const sf_mech *mech, const sf_reactor_params *params, con
                        int n, const double *q0, const double *pressures, double *out_q, double *out_t,
                        int *out_counts, int *out_status, void *workspace, size_t workspace_bytes, void *stream);
 
+/* The plain single-state GPU form of sf_integrate_batch, kept as its comparison point: one thread per reactor runs
+ * the same step logic serially over Griffon's plain per-state evaluation (dense derivative scatter, as
+ * sf_reactor_jac_plain_batch) and a serial LU, with all its data in the workspace (DEVICE, at least
+ * sf_integrate_plain_workspace_size bytes). Closed adiabatic reactors. */
+size_t sf_integrate_plain_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
+int sf_integrate_plain_batch(const sf_mech *mech, const sf_reactor_params *params, const sf_integrate_params *iparams,
+                             int n, const double *q0, const double *pressures, double *out_q, double *out_t,
+                             int *out_counts, int *out_status, void *workspace, size_t workspace_bytes,
+                             void *stream);
+
 /* sf_integrate_batch that also records every accepted step for adjoint sensitivities: trajectory is DEVICE
  * [n][capacity_steps][2 + 6*neq] doubles, per step (t_n, dt_n, Y_1..Y_6) with Y_1 = y_n and Y_2..Y_6 the converged
  * ESDIRK64 stage values (in the integrator's order). A reactor that needs more steps than the capacity stops with

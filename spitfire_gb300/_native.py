@@ -52,6 +52,10 @@ def _declare(L):
     L.sf_integrate_workspace_size.restype = C.c_size_t
     L.sf_integrate_batch.argtypes = [_vp, C.POINTER(SfReactorParams), C.POINTER(SfIntegrateParams), _ip, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_integrate_plain_workspace_size.argtypes = [_vp, C.POINTER(SfReactorParams), _ip]
+    L.sf_integrate_plain_workspace_size.restype = C.c_size_t
+    L.sf_integrate_plain_batch.argtypes = [_vp, C.POINTER(SfReactorParams), C.POINTER(SfIntegrateParams), _ip, _vp,
+                                           _vp, _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
     L.sf_integrate_record_batch.argtypes = [_vp, C.POINTER(SfReactorParams), C.POINTER(SfIntegrateParams), _ip,
                                             _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp, _ip, _vp]
     L.sf_rate_param_adjoint_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _vp]
@@ -76,6 +80,7 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_reactor_jac_plain_workspace_size', 'sf_reactor_jac_plain_batch',
             'sf_reactor_jac_plain_batch_static',
             'sf_newton_lu_batch', 'sf_newton_solve_batch', 'sf_integrate_workspace_size', 'sf_integrate_batch',
+            'sf_integrate_plain_workspace_size', 'sf_integrate_plain_batch',
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',
             'sf_btddod_scale_and_add_diagonal_batch', 'sf_fp64_peak_probe', 'sf_integrate_record_batch',

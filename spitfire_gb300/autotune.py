@@ -174,7 +174,7 @@ def _fitting_warps(integrator):
     gs, gm = place >= 1, place == 2
     n2 = neq * neq
     per = (0 if gm else n2) + 12 * neq + (0 if gs else lay['total']) + \
-        (((0 if gm else (n2 + 1) // 2) + neq) if integrator.linear_precision == 1 else 0) + (neq + 1) // 2 + 2
+        (((0 if gm else (n2 + 1) // 2) + neq) if integrator.linear_precision == 1 else 0) + (neq + 1) // 2 + 2 + neq
     return int(max(1, min(8, (smem - lay['blob_bytes'] - 64) // (per * 8))))
 
 

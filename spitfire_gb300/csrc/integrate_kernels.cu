@@ -18,6 +18,7 @@
 #include "reactor_eval.cuh"
 #include "sf_internal.h"
 #include "warp_lu.cuh"
+#include "esdirk64.cuh"
 
 namespace sfgb {
 namespace {
@@ -25,27 +26,6 @@ namespace {
 // Gather batch of the reactor evaluations inside the integrator: unbatched measured fastest there (the warp's scratch
 // is in shared memory or L2, and the integrator kernel has no registers to spare for operands in flight).
 constexpr int kIntegratorUnroll = 1;
-
-constexpr double kGamma = 0.25;
-// ESDIRK64 stage coefficients a_sj (methods.py:464-500)
-__constant__ double c_a[6][6] = {
-    {0., 0., 0., 0., 0., 0.},
-    {0.25, 0.25, 0., 0., 0., 0.},
-    {8611. / 62500., -1743. / 31250., 0.25, 0., 0., 0.},
-    {5012029. / 34652500., -654441. / 2922500., 174375. / 388108., 0.25, 0., 0.},
-    {15267082809. / 155376265600., -71443401. / 120774400., 730878875. / 902184768., 2285395. / 8070912., 0.25, 0.},
-    {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25}};
-// stage times c_s = sum_j a_sj, summed left to right as numpy does for methods.py:500 (self.c)
-__constant__ double c_c[6] = {
-    0.,
-    0.25 + 0.25,
-    8611. / 62500. + -1743. / 31250. + 0.25,
-    5012029. / 34652500. + -654441. / 2922500. + 174375. / 388108. + 0.25,
-    15267082809. / 155376265600. + -71443401. / 120774400. + 730878875. / 902184768. + 2285395. / 8070912. + 0.25,
-    82889. / 524892. + 0. + 15625. / 83664. + 69875. / 102672. + -2260. / 8211. + 0.25};
-__constant__ double c_b[6] = {82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25};
-__constant__ double c_bh[6] = {4586570599. / 29645900160., 0., 178811875. / 945068544., 814220225. / 1159782912.,
-                               -3700637. / 11593932., 61727. / 225920.};
 
 struct IntParams {
   DevMech m;
@@ -142,7 +122,9 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   // FP32 factors (precision 1)
   float *LU32 = p.gmat ? reinterpret_cast<float *>(A + neq * neq) : reinterpret_cast<float *>(after);
   float *xf = reinterpret_cast<float *>(after + lu32_doubles);  // 2*neq floats
+  // row permutation of the factorization, then the reciprocals of U's diagonal (double, or float for precision 1)
   int *piv = reinterpret_cast<int *>(after + (p.prec == 1 ? lu32_doubles + neq : 0));
+  double *dinv = after + (p.prec == 1 ? lu32_doubles + neq : 0) + (neq + 1) / 2 + 1;
   float *rf = xf + neq;
   const int Tidx = p.cfg.configuration == 1 ? 1 : 0;
   NoJ noj;
@@ -178,9 +160,9 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
         if (p.prec == 1) {
           for (int e = lane; e < neq * neq; e += 32) LU32[e] = (float)A[e];
           __syncwarp();
-          warp_lu(LU32, neq, piv);
+          warp_lu_pd(LU32, neq, piv, reinterpret_cast<float *>(dinv));
         } else {
-          warp_lu(A, neq, piv);
+          warp_lu_pd(A, neq, piv, dinv);
         }
         __syncwarp();
         ++njac;
@@ -221,26 +203,24 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
           // dx = A^-1 res
           if (p.prec == 1) {
             // FP32 triangular solves of the FP32 factors, FP64 residual refinement r = res - A x
-            for (int i = lane; i < neq; i += 32) xf[i] = (float)res[i];
-            __syncwarp();
-            warp_lu_solve(LU32, neq, piv, xf);
+            for (int i = lane; i < neq; i += 32) xf[i] = (float)res[piv[i]];
+            warp_lu_solve_pd(LU32, neq, reinterpret_cast<const float *>(dinv), xf);
             for (int i = lane; i < neq; i += 32) x[i] = (double)xf[i];
             __syncwarp();
             for (int sweep = 0; sweep < ip.refine_sweeps; ++sweep) {
               for (int i = lane; i < neq; i += 32) {
-                double rr = res[i];
-                for (int j = 0; j < neq; ++j) rr = fma(-A[j * neq + i], x[j], rr);
+                const int pi = piv[i];  // the residual of row perm[i], in the factors' row order
+                double rr = res[pi];
+                for (int j = 0; j < neq; ++j) rr = fma(-A[j * neq + pi], x[j], rr);
                 rf[i] = (float)rr;
               }
-              __syncwarp();
-              warp_lu_solve(LU32, neq, piv, rf);
+              warp_lu_solve_pd(LU32, neq, reinterpret_cast<const float *>(dinv), rf);
               for (int i = lane; i < neq; i += 32) x[i] += (double)rf[i];
               __syncwarp();
             }
           } else {
-            for (int i = lane; i < neq; i += 32) x[i] = res[i];
-            __syncwarp();
-            warp_lu_solve(A, neq, piv, x);
+            for (int i = lane; i < neq; i += 32) x[i] = res[piv[i]];
+            warp_lu_solve_pd(A, neq, dinv, x);
           }
           for (int i = lane; i < neq; i += 32) Y[i] -= x[i];
           __syncwarp();
@@ -361,7 +341,8 @@ size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scrat
 {
   const size_t n2 = (size_t)neq * neq;
   return (global_matrix ? 0 : n2) + 12 * (size_t)neq + (global_scratch ? 0 : hm.sl.total) +
-         (prec == 1 ? (global_matrix ? 0 : (n2 + 1) / 2) + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2;
+         (prec == 1 ? (global_matrix ? 0 : (n2 + 1) / 2) + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2 +
+         (size_t)neq;  // the last: reciprocals of U's diagonal
 }
 
 size_t matrix_doubles(int neq, int prec)

@@ -8,6 +8,8 @@ Cases (GRI-3.0 unless stated; each ends by checking the device error word):
              SM, on 38912 states (one warp batch per resident warp), 2 launches
   rates_rhs  production rates (chem_kernel_tps MODE_RATES) and the isochoric right-hand side (MODE_RHS) of 38912
              states, thread per state at 2 resident 4-warp blocks per SM, 2 launches each
+  integrate_2048  2048 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s with the
+             autotuner's shape (Griffon scratch in global slots, 6 warps per block)
   integrate  256 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s (integrate_kernel)
   flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
              block-Thomas factorization, solve and matvec
@@ -90,6 +92,19 @@ def case_integrate():
     return spec
 
 
+def case_integrate_2048():
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec = _spec()
+    AT.set_tuning(spec, 'integrate_scratch', 1)
+    AT.set_tuning(spec, 'integrate_warps', 6)
+    d = W.ignition_batch(spec, 2048, seed=1003)
+    BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                          stop_at_time=0.1)
+    return spec
+
+
 def case_flamelet():
     import torch
     from spitfire_gb300 import workloads as W
@@ -132,7 +147,8 @@ def case_fp64issue():
     return None
 
 
-CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs, 'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
+CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs, 'integrate_2048': case_integrate_2048,
+         'integrate': case_integrate, 'flamelet': case_flamelet, 'adjoint': case_adjoint,
          'fp64issue': case_fp64issue}
 
 

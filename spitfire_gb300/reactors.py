@@ -227,6 +227,28 @@ class BatchIntegrator:
         out.update(times=times, states=states, steps=steps)
         return out
 
+    def run_plain(self, q0, pressures=None, **controls):
+        """The plain single-state GPU form (sf_integrate_plain_batch, one thread per reactor, same step logic): the
+        comparison point of run(). Closed adiabatic reactors; returns the dict of run()."""
+        torch = _torch()
+        q0 = self.g._dev(q0)
+        pr = self.g._dev(pressures) if pressures is not None else None
+        ip = self.controls(**controls)
+        n, neq = q0.shape
+        dev = q0.device
+        out = dict(q=torch.empty((n, neq), dtype=torch.float64, device=dev),
+                   t=torch.empty(n, dtype=torch.float64, device=dev),
+                   counts=torch.empty((n, 4), dtype=torch.int32, device=dev),
+                   status=torch.empty(n, dtype=torch.int32, device=dev))
+        L = N.load()
+        nb = int(L.sf_integrate_plain_workspace_size(self.g.handle, C.byref(self.params), n))
+        ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=dev)
+        N.check(L.sf_integrate_plain_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0), N.ptr(pr),
+                                           N.ptr(out['q']), N.ptr(out['t']), N.ptr(out['counts']),
+                                           N.ptr(out['status']), N.ptr(ws), ws.numel() * 8, N.stream_handle()))
+        out['workspace'] = ws
+        return out
+
     def replay(self):
         """Re-run the captured launch (same inputs, same outputs)."""
         if self._graph is None:

@@ -227,3 +227,33 @@ def test_open_reactor_batch_matches_oracle(cuda, configuration, heat):
         assert np.max(np.abs(qg[i] - r['state']) / np.maximum(np.abs(r['state']), 1e-3)) <= 1e-6, i
     assert spec.griffon.device_status() == 0
     del orc, ns
+
+
+def test_plain_integrator_form_matches_reference_and_oracle(cuda):
+    """The plain single-state GPU form of the integrator (one thread per reactor): the reference's H2 ignition delays
+    with their step counts, and GRI reactors of the batched-ignition distribution against the oracle."""
+    import integrate as I
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    for conf in ('isobaric', 'isochoric'):
+        cases = [c for c in CASES if c['mechanism'] == 'h2-burke' and c['configuration'] == conf]
+        spec, og = pair('h2-burke')
+        q0 = np.array([_q0(spec, c) for c in cases])
+        pres = np.array([c['p'] for c in cases])
+        bi = BatchIntegrator(spec, conf, pressure=pres[0])
+        out = bi.run_plain(q0, delta_temperature_ignition=400., **(dict(pressures=pres) if conf == 'isobaric' else {}))
+        tau, cnt, st = out['t'].cpu().numpy(), out['counts'].cpu().numpy(), out['status'].cpu().numpy()
+        for i, c in enumerate(cases):
+            assert st[i] == 2 and cnt[i, 0] == c['steps'], (c, st[i], cnt[i])
+            assert abs(tau[i] - c['tau']) / c['tau'] <= 1e-6, (c, tau[i])
+    spec, og = pair('methane-gri30')
+    d = W.ignition_batch(spec, 4, seed=77, T_range=(1300., 1500.))
+    out = BatchIntegrator(spec, 'isobaric').run_plain(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                                      stop_at_time=0.1)
+    tau, cnt = out['t'].cpu().numpy(), out['counts'].cpu().numpy()
+    for i in range(4):
+        r = I.integrate(I.ReactorProblem(og, 'isobaric', pressure=d['p'][i]), d['q0'][i],
+                        delta_temperature_ignition=400., stop_at_time=0.1)
+        assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
+        assert abs(tau[i] - r['t']) / r['t'] <= 1e-6, (i, tau[i], r['t'])
+    assert spec.griffon.device_status() == 0
