@@ -380,17 +380,22 @@ int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
 
 /* The four block-Thomas functions take `active`: DEVICE int [n_flamelets] or NULL; flamelets with active[f] == 0
  * are left untouched (their values, factors and outputs keep what they held).
- * Block-Thomas factorization of a batch of BTDDOD matrices, in place (btddod_matrix_kernels.cpp:19-80).
- * values: DEVICE, layout per flamelet as above; l_values: DEVICE output of nzi*ns*ns per flamelet at point offset
- * offsets_z[f]*ns*ns (the L_i = diag(sub) D_{i-1}^-1 blocks); pivots: DEVICE int [points][ns], the row
- * permutation of each block's LU factorization (factored row k is row pivots[k] of the block; the reference stores
- * LAPACK swap indices there, which only its own solve reads). ns <= 128 and 3*ns*ns doubles must fit in the
- * shared memory of one block (ns <= 97 on GB300). */
+ * Block-Thomas factorization of a batch of BTDDOD matrices, in place (btddod_matrix_kernels.cpp:19-80), twisted:
+ * with m = nzi/2, blocks 0..m-1 are eliminated downward as the reference does (L_i = diag(sub_{i-1}) D_{i-1}^-1,
+ * D_i <- D_i - L_i diag(sup_{i-1})), blocks nzi-1..m+1 upward (U_i = diag(sup_{i-1}) D_i^-1,
+ * D_{i-1} <- D_{i-1} - U_i diag(sub_{i-1})), and block m takes both updates; the two halves run concurrently, which
+ * halves a flamelet's chain of dependent block steps. With nzi <= 2 this is the reference's order exactly.
+ * values: DEVICE, layout per flamelet as above, overwritten with each block's LU factors; l_values: DEVICE output of
+ * nzi*ns*ns per flamelet at point offset offsets_z[f]*ns*ns (block i: L_i for 1 <= i <= m, U_i for m < i < nzi);
+ * pivots: DEVICE int [points][ns], the row permutation of each block's LU factorization (factored row k is row
+ * pivots[k] of the block; the reference stores LAPACK swap indices there, which only its own solve reads). The
+ * factors are read only by sf_btddod_solve_batch. ns <= 128 and 3*ns*ns doubles must fit in the shared memory of
+ * one block (ns <= 97 on GB300). */
 int sf_btddod_factor_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
                            const int *offsets_z_host, double *values, double *l_values, int *pivots,
                            const int *active, void *stream);
-/* Solve with the factors (btddod_matrix_kernels.cpp:82-119). rhs and out_x are point-major [points][ns]
- * (they must not alias). */
+/* Solve with the factors of sf_btddod_factor_batch (btddod_matrix_kernels.cpp:82-119, its two sweeps run from both
+ * ends toward block m and back). rhs and out_x are point-major [points][ns] (they must not alias). */
 int sf_btddod_solve_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
                           const int *offsets_z_host, const double *values, const double *l_values,
                           const int *pivots, const double *rhs, double *out_x, const int *active, void *stream);

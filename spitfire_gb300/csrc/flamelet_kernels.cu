@@ -264,12 +264,19 @@ __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *
 }
 
 // ------------------------------------------------------------------------------- block-Thomas (BTDDOD) algebra
-// Factorization (btddod_matrix_kernels.cpp:19-80): LU(D_0); for i >= 1: L_i = diag(sub_{i-1}) D_{i-1}^-1 (the
-// reference solves D_{i-1} X = I with dgetrs), D_i <- D_i - L_i diag(sup_{i-1}), LU(D_i). One CTA per flamelet
-// walks its blocks in order; within a block every step is spread over the CTA's threads: the inverse is a
-// right-looking triangular solve over all ns columns at once, the LU a right-looking factorization with two
-// barriers per column. Pivots are stored as the row permutation of each factorization (factored row k is row
-// perm[k] of the block), which the solve applies as one gather.
+// The reference factorization (btddod_matrix_kernels.cpp:19-80) eliminates downward from the first block:
+// LU(D_0); for i >= 1: L_i = diag(sub_{i-1}) D_{i-1}^-1 (the reference solves D_{i-1} X = I with dgetrs),
+// D_i <- D_i - L_i diag(sup_{i-1}), LU(D_i). Its chain of nzi dependent block steps is the critical path of a
+// flamelet, so this factorization is twisted: with m = nzi/2, one CTA eliminates blocks 0..m-1 downward exactly as
+// above, a second CTA eliminates blocks nzi-1..m+1 upward (T_{nzi-1} = D_{nzi-1}; U_i = diag(sup_{i-1}) T_i^-1;
+// T_{i-1} = D_{i-1} - U_i diag(sub_{i-1})), and block m receives both: M = D_m - L_m diag(sup_{m-1})
+// - U_{m+1} diag(sub_m). Same flops, half the chain, and as stable for these block-diagonally dominant matrices.
+// Storage: l_values block i holds L_i for 1 <= i <= m and U_i for m < i < nzi (block 0 unused); values block i
+// the LU factors of the eliminated block. With nzi <= 2 it is the reference's order exactly.
+// Within a block every step is spread over the CTA's threads: the inverse is a triangular solve over all ns
+// columns at once, the LU a right-looking factorization with two barriers per column. Pivots are stored as the
+// row permutation of each factorization (factored row k is row perm[k] of the block), which the solve applies as
+// one gather.
 constexpr int kFactorThreads = 512;  // 16 warps: 9 % faster than 8 on the 64-flamelet batch, 1024 no faster
 
 // In-place LU with partial pivoting of the n x n ROW-major A (shared memory) by the whole CTA (8 warps); perm
@@ -341,19 +348,22 @@ __device__ void cta_lu_perm(double *A, int n, int *perm, double *scratch)
   }
 }
 
-// X <- (LU)^-1 P for the row-major factors of cta_lu_perm (the inverse of the original block), X row-major, all
-// columns at once: warps over rows, lanes over columns. uinv: n doubles of shared scratch for the reciprocals of
-// U's diagonal, computed in parallel up front so that no division sits on the per-row critical path (a
-// multiplication by the reciprocal instead of dtrsm's division: at most one ulp apart).
-__device__ void cta_lu_inverse(const double *LU, const int *perm, int n, double *X, double *uinv)
+// W <- U^-1 L^-1 for the row-major factors of cta_lu_perm; the inverse of the original block is W P, i.e. its
+// column perm[j] is W's column j. W is formed in place, all columns at once: warps over rows, lanes over columns.
+// The unit-lower forward sweep starts from the identity, so row j of W is zero right of the diagonal until the
+// sweep reaches it and step j only touches columns <= j (the updates it skips are exact no-ops: x - l*0). uinv: n
+// doubles of shared scratch for the reciprocals of U's diagonal, computed in parallel up front so that no division
+// sits on the per-row critical path (a multiplication by the reciprocal instead of dtrsm's division: at most one
+// ulp apart).
+__device__ void cta_lu_inverse(const double *LU, int n, double *W, double *uinv)
 {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   for (int k = tid; k < n; k += nt) uinv[k] = 1. / LU[k * n + k];
   for (int k = warp; k < n; k += nw)
-    for (int c = lane; c < n; c += 32) X[k * n + c] = perm[k] == c ? 1. : 0.;
+    for (int c = lane; c < n; c += 32) W[k * n + c] = k == c ? 1. : 0.;
   __syncthreads();
   if (n == 1) {
-    if (tid == 0) X[0] = X[0] * uinv[0];
+    if (tid == 0) W[0] = W[0] * uinv[0];
     __syncthreads();
     return;
   }
@@ -361,11 +371,11 @@ __device__ void cta_lu_inverse(const double *LU, const int *perm, int n, double 
   for (int j = 0; j < n - 1; ++j) {
     for (int k = j + 1 + warp; k < n; k += nw) {
       const double l = LU[k * n + j];
-      if (j == n - 2) {  // warp-uniform: only the last row is scaled
+      if (j == n - 2) {  // warp-uniform: only the last row is scaled, over all its columns
         const double sc = uinv[k];
-        for (int c = lane; c < n; c += 32) X[k * n + c] = (X[k * n + c] - l * X[j * n + c]) * sc;
+        for (int c = lane; c < n; c += 32) W[k * n + c] = (W[k * n + c] - l * W[j * n + c]) * sc;
       } else {
-        for (int c = lane; c < n; c += 32) X[k * n + c] -= l * X[j * n + c];
+        for (int c = lane; c <= j; c += 32) W[k * n + c] -= l * W[j * n + c];
       }
     }
     __syncthreads();
@@ -376,76 +386,131 @@ __device__ void cta_lu_inverse(const double *LU, const int *perm, int n, double 
       const double u = LU[k * n + j];
       if (k == j - 1) {  // warp-uniform: the row completed in this step is scaled
         const double sc = uinv[k];
-        for (int c = lane; c < n; c += 32) X[k * n + c] = (X[k * n + c] - u * X[j * n + c]) * sc;
+        for (int c = lane; c < n; c += 32) W[k * n + c] = (W[k * n + c] - u * W[j * n + c]) * sc;
       } else {
-        for (int c = lane; c < n; c += 32) X[k * n + c] -= u * X[j * n + c];
+        for (int c = lane; c < n; c += 32) W[k * n + c] -= u * W[j * n + c];
       }
     }
     __syncthreads();
   }
 }
 
+// Shared-memory bytes of the factorization kernels: three row-major blocks, LU scratch, reciprocals, two
+// permutations.
+inline size_t factor_smem_bytes(int ns)
+{
+  return (size_t)3 * ns * ns * 8 + (size_t)(4 * ns + 1) * 8 + (size_t)2 * ns * 4 + 16;
+}
+
+// One CTA per (flamelet, half): even CTAs eliminate blocks 0..m-1 downward, odd CTAs blocks nzi-1..m+1 upward.
+// Each half ends with the multiplier block that feeds block m (L_m, or U_{m+1}); btddod_middle_kernel then forms
+// and factors block m.
 __global__ void __launch_bounds__(kFactorThreads) btddod_factor_kernel(int nf, int ns, const int *offz,
                                                                        const long long *offv, double *values,
                                                                        double *lvals, int *perms, const int *active)
 {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int f = blockIdx.x;
+  const int f = blockIdx.x >> 1;
+  const bool down = (blockIdx.x & 1) == 0;
   if (f >= nf || (active && !active[f])) return;
-  const int z0 = offz[f], nb = offz[f + 1] - z0;
+  const int z0 = offz[f], nb = offz[f + 1] - z0, m = nb / 2;
+  const int len = down ? m : nb - 1 - m;
+  if (len <= 0) return;
   const int bs2 = ns * ns;
   double *vals = values + offv[f];
   double *lv = lvals + (size_t)z0 * bs2;
   int *pv = perms + (size_t)z0 * ns;
   const double *sub = vals + (size_t)nb * bs2;
   const double *sup = sub + (size_t)(nb - 1) * ns;
-  // row-major shared copies: factors of D_{i-1}, D_i, inverse of D_{i-1}
+  // row-major shared copies: the block being factored, the next block, the inverse
   double *bufA = reinterpret_cast<double *>(smem);
   double *bufB = bufA + bs2;
-  double *X = bufB + bs2;
-  double *lu_scratch = X + bs2;  // 3 ns doubles + 1 int (cta_lu_perm)
+  double *W = bufB + bs2;
+  double *lu_scratch = W + bs2;  // 3 ns doubles + 1 int (cta_lu_perm)
   double *uinv = lu_scratch + 3 * ns + 1;
   int *permA = reinterpret_cast<int *>(uinv + ns);
   int *permB = permA + ns;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < bs2; e += nt) {
-    const int c = e / ns, r = e - c * ns;
-    bufA[r * ns + c] = vals[e];
-  }
-  __syncthreads();
-  cta_lu_perm(bufA, ns, permA, lu_scratch);
-  for (int e = tid; e < bs2; e += nt) {
-    const int c = e / ns, r = e - c * ns;
-    vals[e] = bufA[r * ns + c];
-  }
-  for (int k = tid; k < ns; k += nt) pv[k] = permA[k];
-  for (int i = 1; i < nb; ++i) {
-    cta_lu_inverse(bufA, permA, ns, X, uinv);
-    const double *sb = sub + (size_t)(i - 1) * ns;
-    const double *sp = sup + (size_t)(i - 1) * ns;
-    double *Di = vals + (size_t)i * bs2;
-    double *Li = lv + (size_t)i * bs2;
-    for (int e = tid; e < bs2; e += nt) {  // e: column-major index of the global arrays
-      const int c = e / ns, r = e - c * ns;
-      const double l = X[r * ns + c] * sb[r];
-      Li[e] = l;
-      bufB[r * ns + c] = Di[e] + (-sp[c]) * l;
-    }
-    __syncthreads();
-    cta_lu_perm(bufB, ns, permB, lu_scratch);
+  {
+    const double *D0 = vals + (size_t)(down ? 0 : nb - 1) * bs2;
     for (int e = tid; e < bs2; e += nt) {
       const int c = e / ns, r = e - c * ns;
-      Di[e] = bufB[r * ns + c];
+      bufA[r * ns + c] = D0[e];
     }
-    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = permB[k];
+  }
+  __syncthreads();
+  for (int t = 0; t < len; ++t) {
+    const int i = down ? t : nb - 1 - t;
+    cta_lu_perm(bufA, ns, permA, lu_scratch);
+    double *Di = vals + (size_t)i * bs2;
+    for (int e = tid; e < bs2; e += nt) {
+      const int c = e / ns, r = e - c * ns;
+      Di[e] = bufA[r * ns + c];
+    }
+    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = permA[k];
+    cta_lu_inverse(bufA, ns, W, uinv);
+    // multiplier: downward L_{i+1} = diag(sub_i) D_i^-1 at block i+1; upward U_i = diag(sup_{i-1}) T_i^-1 at block
+    // i. Then the next block of the chain: D_{i+1} - L_{i+1} diag(sup_i), or D_{i-1} - U_i diag(sub_{i-1}).
+    const double *rs = down ? sub + (size_t)i * ns : sup + (size_t)(i - 1) * ns;
+    const double *cs = down ? sup + (size_t)i * ns : sub + (size_t)(i - 1) * ns;
+    double *Lm = lv + (size_t)(down ? i + 1 : i) * bs2;
+    const double *Dn = vals + (size_t)(down ? i + 1 : i - 1) * bs2;
+    const bool more = t + 1 < len;
+    for (int e = tid; e < bs2; e += nt) {  // e over W's columns j; the inverse's column is perm[j]
+      const int j = e / ns, r = e - j * ns;
+      const int c = permA[j];
+      const double l = W[r * ns + j] * rs[r];
+      Lm[c * ns + r] = l;
+      if (more) bufB[r * ns + c] = Dn[c * ns + r] + (-cs[c]) * l;
+    }
+    __syncthreads();
     double *tb = bufA;
     bufA = bufB;
     bufB = tb;
     int *tp = permA;
     permA = permB;
     permB = tp;
-    __syncthreads();
   }
+}
+
+// Block m of each flamelet: M = D_m - L_m diag(sup_{m-1}) - U_{m+1} diag(sub_m) (terms present when m >= 1 and
+// m + 1 < nzi), then LU(M). One CTA per flamelet, after btddod_factor_kernel.
+__global__ void __launch_bounds__(kFactorThreads) btddod_middle_kernel(int nf, int ns, const int *offz,
+                                                                       const long long *offv, double *values,
+                                                                       const double *lvals, int *perms,
+                                                                       const int *active)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int f = blockIdx.x;
+  if (f >= nf || (active && !active[f])) return;
+  const int z0 = offz[f], nb = offz[f + 1] - z0, m = nb / 2;
+  const int bs2 = ns * ns;
+  double *vals = values + offv[f];
+  const double *lv = lvals + (size_t)z0 * bs2;
+  const double *sub = vals + (size_t)nb * bs2;
+  const double *sup = sub + (size_t)(nb - 1) * ns;
+  double *M = reinterpret_cast<double *>(smem);
+  double *lu_scratch = M + bs2;
+  int *perm = reinterpret_cast<int *>(lu_scratch + 3 * ns + 1);
+  double *Dm = vals + (size_t)m * bs2;
+  const double *La = m >= 1 ? lv + (size_t)m * bs2 : nullptr;
+  const double *Ub = m + 1 < nb ? lv + (size_t)(m + 1) * bs2 : nullptr;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    double v = Dm[e];
+    if (La) v = v + (-sup[(size_t)(m - 1) * ns + c]) * La[e];
+    if (Ub) v = v + (-sub[(size_t)m * ns + c]) * Ub[e];
+    M[r * ns + c] = v;
+  }
+  __syncthreads();
+  cta_lu_perm(M, ns, perm, lu_scratch);
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    Dm[e] = M[r * ns + c];
+  }
+  int *pv = perms + (size_t)(z0 + m) * ns;
+  for (int k = tid; k < ns; k += nt) pv[k] = perm[k];
 }
 
 // Per-lane asynchronous 8-byte copies global -> shared (cp.async, completion tracked by commit groups; no
@@ -473,141 +538,222 @@ __device__ __forceinline__ double vec_get(const double (&v)[R], int k)
   return out;
 }
 
-// Solve (btddod_matrix_kernels.cpp:82-119), one warp per flamelet:
-//   y_0 = b_0, y_i = b_i - L_i y_{i-1};  x_{nb-1} = D_{nb-1}^-1 y_{nb-1};  x_i = D_i^-1 (y_i - sup_i o x_{i+1}).
-// Vectors stay in registers; the next block's matrix is copied into shared memory while the current one is used.
 template <int R>
-__global__ void __launch_bounds__(32) btddod_solve_kernel(int nf, int ns, const int *offz, const long long *offv,
+__device__ __forceinline__ void vec_load(double (&v)[R], const double *src, int ns)
+{
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int k = lane + 32 * s;
+    v[s] = k < ns ? src[k] : 0.;
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void vec_store(double *dst, const double (&v)[R], int ns)
+{
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int k = lane + 32 * s;
+    if (k < ns) dst[k] = v[s];
+  }
+}
+
+// acc -= B y for the column-major ns x ns block B (shared memory) and register-distributed y.
+template <int R>
+__device__ __forceinline__ void vec_sub_matvec(const double *B, const double (&y)[R], int ns, double (&acc)[R])
+{
+  const int lane = threadIdx.x & 31;
+  for (int c = 0; c < ns; ++c) {
+    const double yc = vec_get<R>(y, c);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      if (k < ns) acc[s] += (-B[k + c * ns]) * yc;
+    }
+  }
+}
+
+// v <- D^-1 v for one block factored by cta_lu_perm (column-major LU in shared memory, pv the row permutation):
+// the permutation as one gather, then unit-lower and upper triangular solves (column-oriented, as dtrsm;
+// 1/U(j,j) multiplies instead of the division, at most one ulp apart).
+template <int R>
+__device__ __forceinline__ void vec_lu_solve(const double *LU, const int *pv, int ns, double (&v)[R])
+{
+  const int lane = threadIdx.x & 31;
+  double w[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int k = lane + 32 * s;
+    const int src = k < ns ? pv[k] : 0;
+    double out = 0.;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const double t = __shfl_sync(0xffffffffu, v[q], src & 31);
+      if ((src >> 5) == q) out = t;
+    }
+    w[s] = out;
+  }
+  // reciprocals of U's diagonal for this lane's rows, off the per-row critical path
+  double rinv[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    const int k = lane + 32 * s;
+    rinv[s] = k < ns ? 1. / LU[k + k * ns] : 0.;
+  }
+  for (int j = 0; j < ns - 1; ++j) {
+    const double xj = vec_get<R>(w, j);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      if (k > j && k < ns) w[s] -= xj * LU[k + j * ns];
+    }
+  }
+  for (int j = ns - 1; j >= 0; --j) {
+    const double xj = vec_get<R>(w, j) * vec_get<R>(rinv, j);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      const int k = lane + 32 * s;
+      if (k == j) w[s] = xj;
+      else if (k < j) w[s] -= xj * LU[k + j * ns];
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = w[s];
+}
+
+// Matrices of one warp's sweep, staged into shared memory: with two buffers the next block is copied while the
+// current one is used; with one (large blocks) each is copied when needed.
+struct SweepBuffers {
+  double *b0, *b1;
+  bool dbl;
+  int bs2;
+  __device__ __forceinline__ double *slot(int k) const { return (k & 1) ? b1 : b0; }  // parity, also for k < 0
+  template <class Src>
+  __device__ __forceinline__ const double *get(int t, int last, int step, Src src)
+  {
+    // blocks t, t + step, ... up to `last` inclusive are fetched in this order
+    __syncwarp();
+    if (dbl) {
+      if (t != last) {
+        async_copy_doubles(slot(t + step), src(t + step), bs2);
+        async_wait_all_but_one();
+      } else {
+        async_wait_all();
+      }
+    } else {
+      async_copy_doubles(b0, src(t), bs2);
+      async_wait_all();
+    }
+    __syncwarp();
+    return dbl ? slot(t) : b0;
+  }
+  template <class Src>
+  __device__ __forceinline__ void prime(int t, Src src)
+  {
+    if (dbl) async_copy_doubles(slot(t), src(t), bs2);
+  }
+};
+
+// Solve with the twisted factors (the reference's btddod_matrix_kernels.cpp:82-119 sweeps, run from both ends):
+// one CTA of two warps per flamelet, warp 0 over blocks 0..m-1, warp 1 over blocks nzi-1..m+1, m = nzi/2.
+//   downward  y_0 = b_0, y_i = b_i - L_i y_{i-1};       upward  z_{nzi-1} = b_{nzi-1}, z_i = b_i - U_{i+1} z_{i+1}
+//   middle    x_m = M^-1 (b_m - L_m y_{m-1} - U_{m+1} z_{m+1})
+//   back      x_i = D_i^-1 (y_i - sup_i o x_{i+1}) for i < m;   x_i = T_i^-1 (z_i - sub_{i-1} o x_{i-1}) for i > m.
+// Vectors stay in registers; y and z are parked in out_x until the back substitution overwrites them.
+template <int R>
+__global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const int *offz, const long long *offv,
                                                           const double *values, const double *lvals,
                                                           const int *perms, const double *rhs, double *x,
-                                                          const int *active)
+                                                          const int *active, int double_buffer)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int f = blockIdx.x;
   if (f >= nf || (active && !active[f])) return;
-  const int lane = threadIdx.x & 31;
-  const int z0 = offz[f], nb = offz[f + 1] - z0;
+  const int warp = threadIdx.x >> 5;
+  const bool down = warp == 0;
+  const int z0 = offz[f], nb = offz[f + 1] - z0, m = nb / 2;
+  const int len = down ? m : nb - 1 - m;
   const int bs2 = ns * ns;
-  double *buf[2] = {reinterpret_cast<double *>(smem), reinterpret_cast<double *>(smem) + bs2};
+  double *sm = reinterpret_cast<double *>(smem);
+  const int nbuf = double_buffer ? 2 : 1;
+  SweepBuffers sb{sm + (size_t)(warp * nbuf) * bs2, sm + (size_t)(warp * nbuf + nbuf - 1) * bs2, double_buffer != 0,
+                  bs2};
+  double *feed = sm + (size_t)(2 * nbuf) * bs2;  // 2 ns doubles: -L_m y_{m-1} and -U_{m+1} z_{m+1}
+  double *xmid = feed + 2 * ns;                  // ns doubles
   const double *vals = values + offv[f];
   const double *lv = lvals + (size_t)z0 * bs2;
   const int *pv = perms + (size_t)z0 * ns;
-  const double *sup = vals + (size_t)nb * bs2 + (size_t)(nb - 1) * ns;
+  const double *sub = vals + (size_t)nb * bs2;
+  const double *sup = sub + (size_t)(nb - 1) * ns;
   const double *b = rhs + (size_t)z0 * ns;
   double *xs = x + (size_t)z0 * ns;
+  auto blk = [&](int t) { return down ? t : nb - 1 - t; };
+  // ---- sweeps toward block m: step t (1 <= t <= len) applies multiplier block blk(t) (+1 upward); step len feeds m
+  auto lsrc = [&](int t) { return lv + (size_t)(down ? t : nb - t) * bs2; };
   double y[R];
-  // ---- forward sweep with the L blocks
-  if (nb > 1) async_copy_doubles(buf[1], lv + (size_t)bs2, bs2);
 #pragma unroll
-  for (int s = 0; s < R; ++s) {
-    const int k = lane + 32 * s;
-    y[s] = k < ns ? b[k] : 0.;
-    if (k < ns) xs[k] = y[s];
-  }
-  for (int i = 1; i < nb; ++i) {
-    __syncwarp();
-    if (i + 1 < nb) {
-      async_copy_doubles(buf[(i + 1) & 1], lv + (size_t)(i + 1) * bs2, bs2);
-      async_wait_all_but_one();
-    } else {
-      async_wait_all();
-    }
-    __syncwarp();
-    const double *Li = buf[i & 1];
-    double acc[R];
+  for (int s = 0; s < R; ++s) y[s] = 0.;
+  if (len > 0) {
+    sb.prime(1, lsrc);
+    vec_load<R>(y, b + (size_t)blk(0) * ns, ns);
+    vec_store<R>(xs + (size_t)blk(0) * ns, y, ns);
+    for (int t = 1; t <= len; ++t) {
+      const double *B = sb.get(t, len, 1, lsrc);
+      double acc[R];
+      if (t < len) {
+        vec_load<R>(acc, b + (size_t)blk(t) * ns, ns);
+      } else {
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      acc[s] = k < ns ? b[(size_t)i * ns + k] : 0.;
-    }
-    for (int c = 0; c < ns; ++c) {
-      const double yc = vec_get<R>(y, c);
-#pragma unroll
-      for (int s = 0; s < R; ++s) {
-        const int k = lane + 32 * s;
-        if (k < ns) acc[s] += (-Li[k + c * ns]) * yc;
+        for (int s = 0; s < R; ++s) acc[s] = 0.;
       }
-    }
+      vec_sub_matvec<R>(B, y, ns, acc);
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      y[s] = acc[s];
-      if (k < ns) xs[(size_t)i * ns + k] = acc[s];
+      for (int s = 0; s < R; ++s) y[s] = acc[s];
+      if (t < len) vec_store<R>(xs + (size_t)blk(t) * ns, y, ns);
     }
   }
-  // ---- backward sweep with the LU factors of the modified diagonal blocks
-  __syncwarp();
-  async_copy_doubles(buf[(nb - 1) & 1], vals + (size_t)(nb - 1) * bs2, bs2);
+  vec_store<R>(feed + (size_t)warp * ns, y, ns);  // zero when this half is empty
+  __syncthreads();
+  // ---- block m
+  auto fsrc = [&](int i) { return vals + (size_t)i * bs2; };
+  if (down) {
+    sb.prime(m, fsrc);
+    const double *F = sb.get(m, m, 1, fsrc);  // single fetch (t == last)
+    double v[R], f0[R], f1[R];
+    vec_load<R>(v, b + (size_t)m * ns, ns);
+    vec_load<R>(f0, feed, ns);
+    vec_load<R>(f1, feed + ns, ns);
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = (v[s] + f0[s]) + f1[s];
+    vec_lu_solve<R>(F, pv + (size_t)m * ns, ns, v);
+    vec_store<R>(xs + (size_t)m * ns, v, ns);
+    vec_store<R>(xmid, v, ns);
+  }
+  __syncthreads();
+  if (len == 0) return;
+  // ---- back substitution away from block m: blocks blk(len-1), ..., blk(0)
   double xn[R];
-#pragma unroll
-  for (int s = 0; s < R; ++s) xn[s] = 0.;
-  for (int i = nb - 1; i >= 0; --i) {
-    __syncwarp();
-    if (i >= 1) {
-      async_copy_doubles(buf[(i - 1) & 1], vals + (size_t)(i - 1) * bs2, bs2);
-      async_wait_all_but_one();
-    } else {
-      async_wait_all();
-    }
-    __syncwarp();
-    const double *LU = buf[i & 1];
+  vec_load<R>(xn, xmid, ns);
+  auto bsrc = [&](int t) { return vals + (size_t)blk(t) * bs2; };
+  sb.prime(len - 1, bsrc);
+  for (int t = len - 1; t >= 0; --t) {
+    const double *F = sb.get(t, 0, -1, bsrc);
+    const int i = blk(t);
+    const double *cpl = down ? sup + (size_t)i * ns : sub + (size_t)(i - 1) * ns;
     double v[R];
+    vec_load<R>(v, xs + (size_t)i * ns, ns);
+    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int s = 0; s < R; ++s) {
       const int k = lane + 32 * s;
-      double t = 0.;
-      if (k < ns) {
-        t = xs[(size_t)i * ns + k];
-        if (i < nb - 1) t = t - sup[(size_t)i * ns + k] * xn[s];
-      }
-      v[s] = t;
+      if (k < ns) v[s] = v[s] - cpl[k] * xn[s];
     }
-    // apply the row permutation: v'[k] = v[perm[k]]
-    double w[R];
+    vec_lu_solve<R>(F, pv + (size_t)i * ns, ns, v);
+    vec_store<R>(xs + (size_t)i * ns, v, ns);
 #pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      const int src = k < ns ? pv[(size_t)i * ns + k] : 0;
-      double out = 0.;
-#pragma unroll
-      for (int q = 0; q < R; ++q) {
-        const double t = __shfl_sync(0xffffffffu, v[q], src & 31);
-        if ((src >> 5) == q) out = t;
-      }
-      w[s] = out;
-    }
-    // reciprocals of U's diagonal for this lane's rows, off the per-row critical path
-    double rinv[R];
-#pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      rinv[s] = k < ns ? 1. / LU[k + k * ns] : 0.;
-    }
-    // unit-lower then upper triangular solves (column-oriented, as dtrsm; 1/U(j,j) multiplies instead of the
-    // division, at most one ulp apart)
-    for (int j = 0; j < ns - 1; ++j) {
-      const double xj = vec_get<R>(w, j);
-#pragma unroll
-      for (int s = 0; s < R; ++s) {
-        const int k = lane + 32 * s;
-        if (k > j && k < ns) w[s] -= xj * LU[k + j * ns];
-      }
-    }
-    for (int j = ns - 1; j >= 0; --j) {
-      const double xj = vec_get<R>(w, j) * vec_get<R>(rinv, j);
-#pragma unroll
-      for (int s = 0; s < R; ++s) {
-        const int k = lane + 32 * s;
-        if (k == j) w[s] = xj;
-        else if (k < j) w[s] -= xj * LU[k + j * ns];
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      if (k < ns) xs[(size_t)i * ns + k] = w[s];
-      xn[s] = w[s];
-    }
+    for (int s = 0; s < R; ++s) xn[s] = v[s];
   }
 }
 
@@ -748,14 +894,18 @@ int launch_solve(int nf, int ns, const int *offz, const long long *offv, const d
                  const double *l_values, const int *pivots, const double *rhs, double *out_x, const int *active,
                  cudaStream_t st)
 {
-  const size_t smem = (size_t)2 * ns * ns * 8;
   int dev, smem_max;
   CUDA_THROW(cudaGetDevice(&dev));
   CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  // two warps, each with two staged blocks (one when four do not fit), plus the middle block's feed vectors
+  const size_t extra = (size_t)3 * ns * 8;
+  const int dbl = (size_t)4 * ns * ns * 8 + extra <= (size_t)smem_max ? 1 : 0;
+  const size_t smem = (size_t)(dbl ? 4 : 2) * ns * ns * 8 + extra;
   if (smem > (size_t)smem_max)
     throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas solve");
   CUDA_THROW(cudaFuncSetAttribute(btddod_solve_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  btddod_solve_kernel<R><<<nf, 32, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active);
+  btddod_solve_kernel<R><<<nf, 64, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active,
+                                               dbl);
   return check_launch();
 }
 
@@ -880,16 +1030,20 @@ int sf_btddod_factor_batch(int nf, int ns, const int *offz, const long long *off
     return SF_ERR_INVALID_ARGUMENT;
   }
   (void)offz_host;
-  const size_t smem = (size_t)3 * ns * ns * 8 + (size_t)(4 * ns + 1) * 8 + (size_t)2 * ns * 4 + 16;
+  const size_t smem = factor_smem_bytes(ns);
   return guarded([&] {
     int dev, smem_max;
     CUDA_THROW(cudaGetDevice(&dev));
     CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (smem > (size_t)smem_max)
       throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas factorization");
+    if ((long long)nf * 2 > 0x7fffffffLL) throw sf_error(SF_ERR_INVALID_ARGUMENT, "too many flamelets");
     CUDA_THROW(cudaFuncSetAttribute(btddod_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    btddod_factor_kernel<<<nf, kFactorThreads, smem, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, l_values,
-                                                                             pivots, active);
+    CUDA_THROW(cudaFuncSetAttribute(btddod_middle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaStream_t st = (cudaStream_t)stream;
+    btddod_factor_kernel<<<2 * nf, kFactorThreads, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, active);
+    CUDA_THROW(cudaGetLastError());
+    btddod_middle_kernel<<<nf, kFactorThreads, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, active);
     return check_launch();
   });
 }
