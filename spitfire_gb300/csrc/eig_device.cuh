@@ -71,6 +71,49 @@ __device__ void warp_balance(double *A, int n, int max_sweeps = 32)
   }
 }
 
+// Sufficient test that every eigenvalue of the n x n column-major A has real part below `cutoff`, by Gershgorin's
+// theorem under the best diagonal scaling: if the comparison matrix M = diag(cutoff - a_ii) - |offdiag(A)| is a
+// nonsingular M-matrix, some x > 0 has M x > 0, and then every Gershgorin disc of X^-1 A X (X = diag(x)) lies left
+// of the cutoff. A Z-matrix is a nonsingular M-matrix iff its LU factorization without pivoting has positive
+// pivots (all leading principal minors positive; A. Berman and R. J. Plemmons, "Nonnegative Matrices in the
+// Mathematical Sciences", ch. 6). Each pivot must stay above 1e-10 of the diagonal entry it starts from, far above
+// the rounding of the elimination, so a pass holds for the exact matrix. A is overwritten with M's partial
+// factors; dg: n doubles of shared work. Lanes over rows (contiguous in column-major storage); a zero entry of
+// the pivot row is skipped by the whole warp, which exploits the sparsity of chemistry Jacobians.
+__device__ bool warp_hmatrix_below(double *A, int n, double cutoff, double *dg)
+{
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+  for (int e = lane; e < n * n; e += 32) {
+    const int c = e / n, r = e - c * n;
+    const double a = A[e];
+    if (r == c) {
+      const double m = cutoff - a;
+      A[e] = m;
+      dg[r] = m;
+      ok = ok && m > 0.;  // false for NaN too
+    } else {
+      A[e] = -fabs(a);
+    }
+  }
+  if (!__all_sync(0xffffffffu, ok)) return false;
+  __syncwarp();
+  for (int k = 0; k < n; ++k) {
+    const double p = A[k + k * n];
+    if (!(p > 1e-10 * dg[k])) return false;  // the same value in every lane: a warp-uniform exit
+    const double ip = 1. / p;
+    for (int i = k + 1 + lane; i < n; i += 32) {
+      const double l = A[i + k * n] * ip;
+      for (int j = k + 1; j < n; ++j) {
+        const double mkj = A[k + j * n];
+        if (mkj != 0.) A[i + j * n] -= l * mkj;
+      }
+    }
+    __syncwarp();
+  }
+  return true;
+}
+
 // Upper bound of the real parts of the eigenvalues by Gershgorin's theorem applied to rows and to columns.
 __device__ double warp_gershgorin_bound(const double *A, int n)
 {

@@ -28,6 +28,7 @@ HostMech::~HostMech()
   }
   if (d_blob) cudaFree(d_blob);
   if (d_status) cudaFree(d_status);
+  if (d_work_counter) cudaFree(d_work_counter);
   if (tps_scratch) cudaFree(tps_scratch);
   for (cudaEvent_t e : events) cudaEventDestroy(e);
   if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -331,6 +332,8 @@ void HostMech::build(const sf_mech_desc *d)
   CUDA_THROW(cudaMemcpy(d_blob, bytes.data(), m.blob_bytes, cudaMemcpyHostToDevice));
   CUDA_THROW(cudaMalloc(&d_status, 16));
   CUDA_THROW(cudaMemset(d_status, 0, 16));
+  CUDA_THROW(cudaMalloc(&d_work_counter, 64));
+  CUDA_THROW(cudaMemset(d_work_counter, 0, 64));
   CUDA_THROW(cudaGetDevice(&device));
 }
 

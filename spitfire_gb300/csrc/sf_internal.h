@@ -45,6 +45,9 @@ struct HostMech {
   std::vector<std::vector<int>> net_entry_of, slot_entry_of;
   void *d_blob = nullptr;
   int *d_status = nullptr;  // device error word of kernels using this mechanism
+  // work counter of the dynamically scheduled kernels (zeroed on the launching stream before each launch; like
+  // the scratch below it serves one stream at a time)
+  int *d_work_counter = nullptr;
   int device = 0;
   int tune[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // launch shapes chosen by the autotuner (sf_tune_knob), 0 = default
   double *tps_scratch = nullptr;           // interleaved scratch of the thread-per-state kernels
