@@ -385,12 +385,14 @@ int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
  * D_i <- D_i - L_i diag(sup_{i-1})), blocks nzi-1..m+1 upward (U_i = diag(sup_{i-1}) D_i^-1,
  * D_{i-1} <- D_{i-1} - U_i diag(sub_{i-1})), and block m takes both updates; the two halves run concurrently, which
  * halves a flamelet's chain of dependent block steps. With nzi <= 2 this is the reference's order exactly.
- * values: DEVICE, layout per flamelet as above, overwritten with each block's LU factors; l_values: DEVICE output of
- * nzi*ns*ns per flamelet at point offset offsets_z[f]*ns*ns (block i: L_i for 1 <= i <= m, U_i for m < i < nzi);
- * pivots: DEVICE int [points][ns], the row permutation of each block's LU factorization (factored row k is row
- * pivots[k] of the block; the reference stores LAPACK swap indices there, which only its own solve reads). The
- * factors are read only by sf_btddod_solve_batch. ns <= 128 and 3*ns*ns doubles must fit in the shared memory of
- * one block (ns <= 97 on GB300). */
+ * Each eliminated block is inverted by Gauss-Jordan elimination with partial pivoting (the multiplier blocks need
+ * the inverse; the reference forms it with dgetrs on the identity).
+ * values: DEVICE, layout per flamelet as above, its diagonal blocks overwritten with the inverses of the eliminated
+ * blocks; l_values: DEVICE output of nzi*ns*ns per flamelet at point offset offsets_z[f]*ns*ns (block i: L_i for
+ * 1 <= i <= m, U_i for m < i < nzi); pivots: DEVICE int [points][ns], the pivot row of each elimination step of
+ * each block (the reference stores LAPACK swap indices there; neither solve needs them with these factors). The
+ * factors are read only by sf_btddod_solve_batch. ns <= 128 and 2*ns*ns doubles must fit in the shared memory of
+ * one block (ns <= 119 on GB300). */
 int sf_btddod_factor_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
                            const int *offsets_z_host, double *values, double *l_values, int *pivots,
                            const int *active, void *stream);

@@ -285,140 +285,143 @@ __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *
 // above, a second CTA eliminates blocks nzi-1..m+1 upward (T_{nzi-1} = D_{nzi-1}; U_i = diag(sup_{i-1}) T_i^-1;
 // T_{i-1} = D_{i-1} - U_i diag(sub_{i-1})), and block m receives both: M = D_m - L_m diag(sup_{m-1})
 // - U_{m+1} diag(sub_m). Same flops, half the chain, and as stable for these block-diagonally dominant matrices.
-// Storage: l_values block i holds L_i for 1 <= i <= m and U_i for m < i < nzi (block 0 unused); values block i
-// the LU factors of the eliminated block. With nzi <= 2 it is the reference's order exactly.
-// Within a block every step is spread over the CTA's threads: the inverse is a triangular solve over all ns
-// columns at once, the LU a right-looking factorization with two barriers per column. Pivots are stored as the
-// row permutation of each factorization (factored row k is row perm[k] of the block), which the solve applies as
-// one gather.
-constexpr int kFactorThreads = 512;  // 16 warps: 9 % faster than 8 on the 64-flamelet batch, 1024 no faster
+// Every eliminated block is inverted once (the multiplier blocks need the inverse anyway), by Gauss-Jordan
+// elimination with one CTA barrier per column, and the inverse is what the solve applies.
+// Storage: values block i holds the inverse of the eliminated block i; l_values block i holds L_i for
+// 1 <= i <= m and U_i for m < i < nzi (block 0 unused).
+constexpr int kFactorThreads = 512;  // 16 warps: warp 0 runs the pivot look-ahead, 15 update the block
 
-// In-place LU with partial pivoting of the n x n ROW-major A (shared memory) by the whole CTA (8 warps); perm
-// (shared, n ints) receives the row permutation. scratch: 3n doubles + 1 int of shared memory. n <= 128.
-// Per column k: warp 0 finds the pivot (integer comparison of magnitudes, the first largest as idamax), forms the
-// multipliers (scaled by 1/pivot, as dgetf2) and stages the two swapped rows; then all warps write the swapped and
-// updated trailing rows (warps over rows, lanes over contiguous columns), each element by one thread.
-__device__ void cta_lu_perm(double *A, int n, int *perm, double *scratch)
+// Inverse of the n x n row-major matrix in S by Gauss-Jordan elimination with partial pivoting (G. H. Golub and
+// C. F. Van Loan, "Matrix Computations", section 3.2; rows are not moved, the pivot order is recorded). Phase k
+// maps the source buffer to the destination (S and D alternate): with pivot row p, ip = 1/S[p][k] and
+// f_i = S[i][k] ip,
+//   D[p][j] = S[p][j] ip,   D[i][j] = S[i][j] - f_i S[p][j]   (j != k),   D[p][k] = ip,   D[i][k] = -f_i.
+// Warps 1.. update the block while warp 0 forms column k+1 of D and, before the phase's barrier, chooses the next
+// pivot among the unused rows (largest magnitude, lowest row on ties, as idamax) and its multipliers: one barrier
+// per column. Returns the buffer Z holding the inverse permuted: inverse(r, c) = Z[piv[r]][pinv[c]], where
+// pinv[piv[k]] = k. ws: 2n + 2 doubles (the multipliers and pivot reciprocals of two phases); used: n ints. A pivot
+// column of zeros gives ip = 0 (a singular block; the output is then not an inverse). n <= 128.
+__device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pinv, double *ws, int *used)
 {
-  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-  double *mcol = scratch, *prow = scratch + n, *krow = scratch + 2 * n;
-  int *pvt = reinterpret_cast<int *>(scratch + 3 * n);
-  for (int i = tid; i < n; i += nt) perm[i] = i;
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  double *ipb = ws + 2 * n;
+  // warp 0: choose the pivot of column j among the unused rows from the lane-held column values v (row lane+32s),
+  // publish it with its multipliers for phase j
+  auto choose = [&](int j, const double (&v)[4]) {
+    unsigned long long best = 0ull;
+    int bp = n;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int i = lane + 32 * s;
+      if (i < n && !used[i]) {
+        const unsigned long long key = (unsigned long long)__double_as_longlong(v[s]) & 0x7fffffffffffffffull;
+        if (bp == n || key > best) { best = key; bp = i; }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bp, o);
+      if (oi < n && (bp >= n || ob > best || (ob == best && oi < bp))) { best = ob; bp = oi; }
+    }
+    double pv = 0.;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const double t = __shfl_sync(0xffffffffu, v[s], bp & 31);
+      if ((bp >> 5) == s) pv = t;
+    }
+    const double ip = pv != 0. ? 1. / pv : 0.;
+    double *f = ws + (j & 1) * n;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int i = lane + 32 * s;
+      if (i < n) f[i] = v[s] * ip;
+    }
+    if (lane == 0) {
+      ipb[j & 1] = ip;
+      piv[j] = bp;
+      pinv[bp] = j;
+      used[bp] = 1;
+    }
+    __syncwarp();
+  };
+  if (warp == 0) {
+    for (int i = lane; i < n; i += 32) used[i] = 0;
+    __syncwarp();
+    double v[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int i = lane + 32 * s;
+      v[s] = i < n ? S[i * n] : 0.;
+    }
+    choose(0, v);
+  }
   __syncthreads();
   for (int k = 0; k < n; ++k) {
+    const int p = piv[k];
+    const double ip = ipb[k & 1];
+    const double *f = ws + (k & 1) * n;
+    const double *Sp = S + (size_t)p * n;
     if (warp == 0) {
-      unsigned long long best = 0ull;
-      int p = k;
-      bool any = false;
-      for (int i = k + lane; i < n; i += 32) {
-        const unsigned long long key = (unsigned long long)__double_as_longlong(A[i * n + k]) & 0x7fffffffffffffffull;
-        if (!any || key > best) { best = key; p = i; any = true; }
-      }
-      if (!any) p = n;  // lanes without rows lose every comparison
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, p, o);
-        if (oi < n && (p >= n || ob > best || (ob == best && oi < p))) { best = ob; p = oi; }
-      }
-      const double pv = A[p * n + k];
-      const double inv = pv != 0. ? 1. / pv : 0.;
-      for (int i = k + lane; i < n; i += 32) {
-        const double x = A[(i == k ? p : (i == p ? k : i)) * n + k];
-        mcol[i] = i == k ? x : x * inv;
-      }
-      for (int j = k + 1 + lane; j < n; j += 32) {
-        prow[j] = A[p * n + j];
-        krow[j] = A[k * n + j];
-      }
-      if (lane == 0) {
-        *pvt = p;
-        if (p != k) {
-          const int t = perm[k];
-          perm[k] = perm[p];
-          perm[p] = t;
+      if (k + 1 < n) {
+        const int j = k + 1;
+        const double spj = Sp[j];
+        double v[4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const int i = lane + 32 * s;
+          double val = 0.;
+          if (i < n) {
+            val = i == p ? spj * ip : S[i * n + j] + (-f[i]) * spj;
+            D[i * n + j] = val;
+          }
+          v[s] = val;
         }
+        choose(j, v);
+      }
+    } else {
+      const int kn = k + 1;
+      for (int e = tid - 32; e < n * n; e += nt - 32) {
+        const int i = e / n, j = e - i * n;
+        if (j == kn) continue;  // warp 0's column
+        double val;
+        if (j == k) val = i == p ? ip : -f[i];
+        else if (i == p) val = Sp[j] * ip;
+        else val = S[e] + (-f[i]) * Sp[j];
+        D[e] = val;
       }
     }
     __syncthreads();
-    const int p = *pvt;
-    for (int i = k + tid; i < n; i += nt) A[i * n + k] = mcol[i];
-    if (p != k)
-      for (int j = tid; j < k; j += nt) {
-        const double t = A[k * n + j];
-        A[k * n + j] = A[p * n + j];
-        A[p * n + j] = t;
-      }
-    for (int i = k + warp; i < n; i += nw) {
-      const double m = mcol[i];
-      for (int j = k + 1 + lane; j < n; j += 32) {
-        double v;
-        if (i == k) v = prow[j];
-        else if (i == p) v = krow[j] - m * prow[j];
-        else v = A[i * n + j] - m * prow[j];
-        A[i * n + j] = v;
-      }
-    }
-    __syncthreads();
+    double *t = S;
+    S = D;
+    D = t;
   }
+  return S;
 }
 
-// W <- U^-1 L^-1 for the row-major factors of cta_lu_perm; the inverse of the original block is W P, i.e. its
-// column perm[j] is W's column j. W is formed in place, all columns at once: warps over rows, lanes over columns.
-// The unit-lower forward sweep starts from the identity, so row j of W is zero right of the diagonal until the
-// sweep reaches it and step j only touches columns <= j (the updates it skips are exact no-ops: x - l*0). uinv: n
-// doubles of shared scratch for the reciprocals of U's diagonal, computed in parallel up front so that no division
-// sits on the per-row critical path (a multiplication by the reciprocal instead of dtrsm's division: at most one
-// ulp apart).
-__device__ void cta_lu_inverse(const double *LU, int n, double *W, double *uinv)
-{
-  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-  for (int k = tid; k < n; k += nt) uinv[k] = 1. / LU[k * n + k];
-  for (int k = warp; k < n; k += nw)
-    for (int c = lane; c < n; c += 32) W[k * n + c] = k == c ? 1. : 0.;
-  __syncthreads();
-  if (n == 1) {
-    if (tid == 0) W[0] = W[0] * uinv[0];
-    __syncthreads();
-    return;
-  }
-  // unit-lower forward substitution (as dtrsm); the last row is scaled by 1/U(n-1,n-1) when complete
-  for (int j = 0; j < n - 1; ++j) {
-    for (int k = j + 1 + warp; k < n; k += nw) {
-      const double l = LU[k * n + j];
-      if (j == n - 2) {  // warp-uniform: only the last row is scaled, over all its columns
-        const double sc = uinv[k];
-        for (int c = lane; c < n; c += 32) W[k * n + c] = (W[k * n + c] - l * W[j * n + c]) * sc;
-      } else {
-        for (int c = lane; c <= j; c += 32) W[k * n + c] -= l * W[j * n + c];
-      }
-    }
-    __syncthreads();
-  }
-  // upper back substitution; row j-1 is scaled by its pivot's reciprocal once its last update (from row j) is in
-  for (int j = n - 1; j >= 1; --j) {
-    for (int k = warp; k < j; k += nw) {
-      const double u = LU[k * n + j];
-      if (k == j - 1) {  // warp-uniform: the row completed in this step is scaled
-        const double sc = uinv[k];
-        for (int c = lane; c < n; c += 32) W[k * n + c] = (W[k * n + c] - u * W[j * n + c]) * sc;
-      } else {
-        for (int c = lane; c < n; c += 32) W[k * n + c] -= u * W[j * n + c];
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// Shared-memory bytes of the factorization kernels: three row-major blocks, LU scratch, reciprocals, two
-// permutations.
+// Shared-memory bytes of the factorization kernels: two row-major blocks, the elimination's multipliers and pivot
+// reciprocals, three index arrays.
 inline size_t factor_smem_bytes(int ns)
 {
-  return (size_t)3 * ns * ns * 8 + (size_t)(4 * ns + 1) * 8 + (size_t)2 * ns * 4 + 16;
+  return (size_t)2 * ns * ns * 8 + (size_t)(2 * ns + 2) * 8 + (size_t)3 * ns * 4 + 16;
 }
+
+struct FactorShared {
+  double *buf0, *buf1, *ws;
+  int *piv, *pinv, *used;
+  __device__ FactorShared(unsigned char *smem, int ns)
+  {
+    buf0 = reinterpret_cast<double *>(smem);
+    buf1 = buf0 + (size_t)ns * ns;
+    ws = buf1 + (size_t)ns * ns;
+    piv = reinterpret_cast<int *>(ws + 2 * ns + 2);
+    pinv = piv + ns;
+    used = pinv + ns;
+  }
+};
 
 // One CTA per (flamelet, half): even CTAs eliminate blocks 0..m-1 downward, odd CTAs blocks nzi-1..m+1 upward.
 // Each half ends with the multiplier block that feeds block m (L_m, or U_{m+1}); btddod_middle_kernel then forms
-// and factors block m.
+// and inverts block m.
 __global__ void __launch_bounds__(kFactorThreads) btddod_factor_kernel(int nf, int ns, const int *offz,
                                                                        const long long *offv, double *values,
                                                                        double *lvals, int *perms, const int *active)
@@ -436,59 +439,46 @@ __global__ void __launch_bounds__(kFactorThreads) btddod_factor_kernel(int nf, i
   int *pv = perms + (size_t)z0 * ns;
   const double *sub = vals + (size_t)nb * bs2;
   const double *sup = sub + (size_t)(nb - 1) * ns;
-  // row-major shared copies: the block being factored, the next block, the inverse
-  double *bufA = reinterpret_cast<double *>(smem);
-  double *bufB = bufA + bs2;
-  double *W = bufB + bs2;
-  double *lu_scratch = W + bs2;  // 3 ns doubles + 1 int (cta_lu_perm)
-  double *uinv = lu_scratch + 3 * ns + 1;
-  int *permA = reinterpret_cast<int *>(uinv + ns);
-  int *permB = permA + ns;
+  FactorShared sh(smem, ns);
+  double *cur = sh.buf0, *other = sh.buf1;  // cur: the block to invert (row-major)
   const int tid = threadIdx.x, nt = blockDim.x;
   {
     const double *D0 = vals + (size_t)(down ? 0 : nb - 1) * bs2;
     for (int e = tid; e < bs2; e += nt) {
       const int c = e / ns, r = e - c * ns;
-      bufA[r * ns + c] = D0[e];
+      cur[r * ns + c] = D0[e];
     }
   }
   __syncthreads();
   for (int t = 0; t < len; ++t) {
     const int i = down ? t : nb - 1 - t;
-    cta_lu_perm(bufA, ns, permA, lu_scratch);
-    double *Di = vals + (size_t)i * bs2;
-    for (int e = tid; e < bs2; e += nt) {
-      const int c = e / ns, r = e - c * ns;
-      Di[e] = bufA[r * ns + c];
-    }
-    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = permA[k];
-    cta_lu_inverse(bufA, ns, W, uinv);
+    double *Z = cta_gj_inverse(cur, other, ns, sh.piv, sh.pinv, sh.ws, sh.used);
+    double *nxt = Z == cur ? other : cur;  // the buffer the elimination no longer needs
     // multiplier: downward L_{i+1} = diag(sub_i) D_i^-1 at block i+1; upward U_i = diag(sup_{i-1}) T_i^-1 at block
     // i. Then the next block of the chain: D_{i+1} - L_{i+1} diag(sup_i), or D_{i-1} - U_i diag(sub_{i-1}).
     const double *rs = down ? sub + (size_t)i * ns : sup + (size_t)(i - 1) * ns;
     const double *cs = down ? sup + (size_t)i * ns : sub + (size_t)(i - 1) * ns;
+    double *Di = vals + (size_t)i * bs2;
     double *Lm = lv + (size_t)(down ? i + 1 : i) * bs2;
     const double *Dn = vals + (size_t)(down ? i + 1 : i - 1) * bs2;
     const bool more = t + 1 < len;
-    for (int e = tid; e < bs2; e += nt) {  // e over W's columns j; the inverse's column is perm[j]
-      const int j = e / ns, r = e - j * ns;
-      const int c = permA[j];
-      const double l = W[r * ns + j] * rs[r];
-      Lm[c * ns + r] = l;
-      if (more) bufB[r * ns + c] = Dn[c * ns + r] + (-cs[c]) * l;
+    for (int e = tid; e < bs2; e += nt) {  // e: column-major index of the global arrays
+      const int c = e / ns, r = e - c * ns;
+      const double inv = Z[sh.piv[r] * ns + sh.pinv[c]];
+      Di[e] = inv;
+      const double l = inv * rs[r];
+      Lm[e] = l;
+      if (more) nxt[r * ns + c] = Dn[e] + (-cs[c]) * l;
     }
+    for (int k = tid; k < ns; k += nt) pv[(size_t)i * ns + k] = sh.piv[k];
     __syncthreads();
-    double *tb = bufA;
-    bufA = bufB;
-    bufB = tb;
-    int *tp = permA;
-    permA = permB;
-    permB = tp;
+    cur = nxt;
+    other = Z;
   }
 }
 
 // Block m of each flamelet: M = D_m - L_m diag(sup_{m-1}) - U_{m+1} diag(sub_m) (terms present when m >= 1 and
-// m + 1 < nzi), then LU(M). One CTA per flamelet, after btddod_factor_kernel.
+// m + 1 < nzi), then its inverse. One CTA per flamelet, after btddod_factor_kernel.
 __global__ void __launch_bounds__(kFactorThreads) btddod_middle_kernel(int nf, int ns, const int *offz,
                                                                        const long long *offv, double *values,
                                                                        const double *lvals, int *perms,
@@ -503,9 +493,7 @@ __global__ void __launch_bounds__(kFactorThreads) btddod_middle_kernel(int nf, i
   const double *lv = lvals + (size_t)z0 * bs2;
   const double *sub = vals + (size_t)nb * bs2;
   const double *sup = sub + (size_t)(nb - 1) * ns;
-  double *M = reinterpret_cast<double *>(smem);
-  double *lu_scratch = M + bs2;
-  int *perm = reinterpret_cast<int *>(lu_scratch + 3 * ns + 1);
+  FactorShared sh(smem, ns);
   double *Dm = vals + (size_t)m * bs2;
   const double *La = m >= 1 ? lv + (size_t)m * bs2 : nullptr;
   const double *Ub = m + 1 < nb ? lv + (size_t)(m + 1) * bs2 : nullptr;
@@ -515,16 +503,16 @@ __global__ void __launch_bounds__(kFactorThreads) btddod_middle_kernel(int nf, i
     double v = Dm[e];
     if (La) v = v + (-sup[(size_t)(m - 1) * ns + c]) * La[e];
     if (Ub) v = v + (-sub[(size_t)m * ns + c]) * Ub[e];
-    M[r * ns + c] = v;
+    sh.buf0[r * ns + c] = v;
   }
   __syncthreads();
-  cta_lu_perm(M, ns, perm, lu_scratch);
+  const double *Z = cta_gj_inverse(sh.buf0, sh.buf1, ns, sh.piv, sh.pinv, sh.ws, sh.used);
   for (int e = tid; e < bs2; e += nt) {
     const int c = e / ns, r = e - c * ns;
-    Dm[e] = M[r * ns + c];
+    Dm[e] = Z[sh.piv[r] * ns + sh.pinv[c]];
   }
   int *pv = perms + (size_t)(z0 + m) * ns;
-  for (int k = tid; k < ns; k += nt) pv[k] = perm[k];
+  for (int k = tid; k < ns; k += nt) pv[k] = sh.piv[k];
 }
 
 // Per-lane asynchronous 8-byte copies global -> shared (cp.async, completion tracked by commit groups; no
@@ -589,52 +577,24 @@ __device__ __forceinline__ void vec_sub_matvec(const double *B, const double (&y
   }
 }
 
-// v <- D^-1 v for one block factored by cta_lu_perm (column-major LU in shared memory, pv the row permutation):
-// the permutation as one gather, then unit-lower and upper triangular solves (column-oriented, as dtrsm;
-// 1/U(j,j) multiplies instead of the division, at most one ulp apart).
+// v <- B v for the column-major ns x ns block B (shared memory) and register-distributed v.
 template <int R>
-__device__ __forceinline__ void vec_lu_solve(const double *LU, const int *pv, int ns, double (&v)[R])
+__device__ __forceinline__ void vec_apply(const double *B, int ns, double (&v)[R])
 {
   const int lane = threadIdx.x & 31;
-  double w[R];
+  double acc[R];
 #pragma unroll
-  for (int s = 0; s < R; ++s) {
-    const int k = lane + 32 * s;
-    const int src = k < ns ? pv[k] : 0;
-    double out = 0.;
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const double t = __shfl_sync(0xffffffffu, v[q], src & 31);
-      if ((src >> 5) == q) out = t;
-    }
-    w[s] = out;
-  }
-  // reciprocals of U's diagonal for this lane's rows, off the per-row critical path
-  double rinv[R];
-#pragma unroll
-  for (int s = 0; s < R; ++s) {
-    const int k = lane + 32 * s;
-    rinv[s] = k < ns ? 1. / LU[k + k * ns] : 0.;
-  }
-  for (int j = 0; j < ns - 1; ++j) {
-    const double xj = vec_get<R>(w, j);
+  for (int s = 0; s < R; ++s) acc[s] = 0.;
+  for (int c = 0; c < ns; ++c) {
+    const double vc = vec_get<R>(v, c);
 #pragma unroll
     for (int s = 0; s < R; ++s) {
       const int k = lane + 32 * s;
-      if (k > j && k < ns) w[s] -= xj * LU[k + j * ns];
-    }
-  }
-  for (int j = ns - 1; j >= 0; --j) {
-    const double xj = vec_get<R>(w, j) * vec_get<R>(rinv, j);
-#pragma unroll
-    for (int s = 0; s < R; ++s) {
-      const int k = lane + 32 * s;
-      if (k == j) w[s] = xj;
-      else if (k < j) w[s] -= xj * LU[k + j * ns];
+      if (k < ns) acc[s] += B[k + c * ns] * vc;
     }
   }
 #pragma unroll
-  for (int s = 0; s < R; ++s) v[s] = w[s];
+  for (int s = 0; s < R; ++s) v[s] = acc[s];
 }
 
 // Matrices of one warp's sweep, staged into shared memory: with two buffers the next block is copied while the
@@ -675,7 +635,8 @@ struct SweepBuffers {
 //   downward  y_0 = b_0, y_i = b_i - L_i y_{i-1};       upward  z_{nzi-1} = b_{nzi-1}, z_i = b_i - U_{i+1} z_{i+1}
 //   middle    x_m = M^-1 (b_m - L_m y_{m-1} - U_{m+1} z_{m+1})
 //   back      x_i = D_i^-1 (y_i - sup_i o x_{i+1}) for i < m;   x_i = T_i^-1 (z_i - sub_{i-1} o x_{i-1}) for i > m.
-// Vectors stay in registers; y and z are parked in out_x until the back substitution overwrites them.
+// Every block step is a matrix-vector product (the factors hold the inverses). Vectors stay in registers; y and z are
+// parked in out_x until the back substitution overwrites them.
 template <int R>
 __global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const int *offz, const long long *offv,
                                                           const double *values, const double *lvals,
@@ -698,7 +659,7 @@ __global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const 
   double *xmid = feed + 2 * ns;                  // ns doubles
   const double *vals = values + offv[f];
   const double *lv = lvals + (size_t)z0 * bs2;
-  const int *pv = perms + (size_t)z0 * ns;
+  (void)perms;  // the pivot order of each block's elimination; the stored inverses need none
   const double *sub = vals + (size_t)nb * bs2;
   const double *sup = sub + (size_t)(nb - 1) * ns;
   const double *b = rhs + (size_t)z0 * ns;
@@ -741,7 +702,7 @@ __global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const 
     vec_load<R>(f1, feed + ns, ns);
 #pragma unroll
     for (int s = 0; s < R; ++s) v[s] = (v[s] + f0[s]) + f1[s];
-    vec_lu_solve<R>(F, pv + (size_t)m * ns, ns, v);
+    vec_apply<R>(F, ns, v);
     vec_store<R>(xs + (size_t)m * ns, v, ns);
     vec_store<R>(xmid, v, ns);
   }
@@ -764,7 +725,7 @@ __global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const 
       const int k = lane + 32 * s;
       if (k < ns) v[s] = v[s] - cpl[k] * xn[s];
     }
-    vec_lu_solve<R>(F, pv + (size_t)i * ns, ns, v);
+    vec_apply<R>(F, ns, v);
     vec_store<R>(xs + (size_t)i * ns, v, ns);
 #pragma unroll
     for (int s = 0; s < R; ++s) xn[s] = v[s];
