@@ -289,14 +289,15 @@ __global__ void flamelet_expeig_kernel(int n_points, int nf, int ns, const int *
 // elimination with one CTA barrier per column, and the inverse is what the solve applies.
 // Storage: values block i holds the inverse of the eliminated block i; l_values block i holds L_i for
 // 1 <= i <= m and U_i for m < i < nzi (block 0 unused).
-constexpr int kFactorThreads = 512;  // 16 warps: warp 0 runs the pivot look-ahead, 15 update the block
+constexpr int kFactorThreads = 512;  // 16 warps: warp 0 runs the pivot look-ahead, 12 update the block
+static_assert(kFactorThreads >= 64 && kFactorThreads % 32 == 0, "the elimination needs updating warps");
 
 // Inverse of the n x n row-major matrix in S by Gauss-Jordan elimination with partial pivoting (G. H. Golub and
 // C. F. Van Loan, "Matrix Computations", section 3.2; rows are not moved, the pivot order is recorded). Phase k
 // maps the source buffer to the destination (S and D alternate): with pivot row p, ip = 1/S[p][k] and
 // f_i = S[i][k] ip,
 //   D[p][j] = S[p][j] ip,   D[i][j] = S[i][j] - f_i S[p][j]   (j != k),   D[p][k] = ip,   D[i][k] = -f_i.
-// Warps 1.. update the block while warp 0 forms column k+1 of D and, before the phase's barrier, chooses the next
+// The other warps update the block while warp 0 forms column k+1 of D and, before the phase's barrier, chooses the next
 // pivot among the unused rows (largest magnitude, lowest row on ties, as idamax) and its multipliers: one barrier
 // per column. Returns the buffer Z holding the inverse permuted: inverse(r, c) = Z[piv[r]][pinv[c]], where
 // pinv[piv[k]] = k. ws: 2n + 2 doubles (the multipliers and pivot reciprocals of two phases); used: n ints. A pivot
@@ -305,6 +306,14 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
 {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   double *ipb = ws + 2 * n;
+  // The updating warps leave warp 0's scheduler partition (warps 4, 8, ... share it; warps are dealt to the four
+  // partitions by warp index) to warp 0 alone, so that its serial look-ahead does not queue for the FP64 unit
+  // behind their updates. Elements are dealt to the updating threads in row-major order with incremental indices.
+  const int nw = nt >> 5;
+  const int uw = (warp & 3) ? warp - (warp >> 2) - 1 : -1;
+  const int ustride = 32 * (nw - (nw + 3) / 4);
+  const int ut = uw * 32 + lane;
+  const int i0 = ut / n, j0 = ut - (ut / n) * n, di = ustride / n, dj = ustride - (ustride / n) * n;
   // warp 0: choose the pivot of column j among the unused rows from the lane-held column values v (row lane+32s),
   // publish it with its multipliers for phase j
   auto choose = [&](int j, const double (&v)[4]) {
@@ -378,16 +387,23 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
         }
         choose(j, v);
       }
-    } else {
+    } else if (uw >= 0) {
       const int kn = k + 1;
-      for (int e = tid - 32; e < n * n; e += nt - 32) {
-        const int i = e / n, j = e - i * n;
-        if (j == kn) continue;  // warp 0's column
-        double val;
-        if (j == k) val = i == p ? ip : -f[i];
-        else if (i == p) val = Sp[j] * ip;
-        else val = S[e] + (-f[i]) * Sp[j];
-        D[e] = val;
+      int i = i0, j = j0;
+      for (int e = ut; e < n * n; e += ustride) {
+        if (j != kn) {  // column k+1 is warp 0's
+          double val;
+          if (j == k) val = i == p ? ip : -f[i];
+          else if (i == p) val = Sp[j] * ip;
+          else val = S[e] + (-f[i]) * Sp[j];
+          D[e] = val;
+        }
+        i += di;
+        j += dj;
+        if (j >= n) {
+          j -= n;
+          ++i;
+        }
       }
     }
     __syncthreads();
@@ -1019,10 +1035,17 @@ int sf_btddod_factor_batch(int nf, int ns, const int *offz, const long long *off
     if (smem > (size_t)smem_max)
       throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas factorization");
     if ((long long)nf * 2 > 0x7fffffffLL) throw sf_error(SF_ERR_INVALID_ARGUMENT, "too many flamelets");
-    CUDA_THROW(cudaFuncSetAttribute(btddod_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nsm;
+    CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    // Each CTA is bound by its SM's FP64 unit. When every CTA can have an SM of its own, ask for more than half an
+    // SM's shared memory so that no two CTAs share one (the block scheduler may otherwise pair them).
+    const size_t smem_launch = 2LL * nf <= nsm ? std::max(smem, (size_t)smem_max / 2 + 1024) : smem;
+    CUDA_THROW(cudaFuncSetAttribute(btddod_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_launch));
     CUDA_THROW(cudaFuncSetAttribute(btddod_middle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     cudaStream_t st = (cudaStream_t)stream;
-    btddod_factor_kernel<<<2 * nf, kFactorThreads, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, active);
+    btddod_factor_kernel<<<2 * nf, kFactorThreads, smem_launch, st>>>(nf, ns, offz, offv, values, l_values, pivots,
+                                                                      active);
     CUDA_THROW(cudaGetLastError());
     btddod_middle_kernel<<<nf, kFactorThreads, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, active);
     return check_launch();
