@@ -297,11 +297,11 @@ static_assert(kFactorThreads >= 64 && kFactorThreads % 32 == 0, "the elimination
 // maps the source buffer to the destination (S and D alternate): with pivot row p, ip = 1/S[p][k] and
 // f_i = S[i][k] ip,
 //   D[p][j] = S[p][j] ip,   D[i][j] = S[i][j] - f_i S[p][j]   (j != k),   D[p][k] = ip,   D[i][k] = -f_i.
-// The other warps update the block while warp 0 forms column k+1 of D and, before the phase's barrier, chooses the next
-// pivot among the unused rows (largest magnitude, lowest row on ties, as idamax) and its multipliers: one barrier
-// per column. Returns the buffer Z holding the inverse permuted: inverse(r, c) = Z[piv[r]][pinv[c]], where
-// pinv[piv[k]] = k. ws: 2n + 2 doubles (the multipliers and pivot reciprocals of two phases); used: n ints. A pivot
-// column of zeros gives ip = 0 (a singular block; the output is then not an inverse). n <= 128.
+// The other warps update the block while warp 0 forms column k+1 of D and, before the phase's barrier, chooses the
+// next pivot among the unused rows (largest magnitude, lowest row on ties, as idamax) and its multipliers: one
+// barrier per column. Returns the buffer Z holding the inverse permuted: inverse(r, c) = Z[piv[r]][pinv[c]], where
+// pinv[piv[k]] = k. ws: 2n + 2 doubles (the negated multipliers and pivot reciprocals of two phases); used: n ints.
+// A pivot column of zeros gives ip = 0 (a singular block; the output is then not an inverse). n <= 128.
 __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pinv, double *ws, int *used)
 {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
@@ -339,11 +339,12 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
       if ((bp >> 5) == s) pv = t;
     }
     const double ip = pv != 0. ? 1. / pv : 0.;
-    double *f = ws + (j & 1) * n;
+    const double nip = -ip;
+    double *f = ws + (j & 1) * n;  // the negated multipliers -f_i
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int i = lane + 32 * s;
-      if (i < n) f[i] = v[s] * ip;
+      if (i < n) f[i] = v[s] * nip;
     }
     if (lane == 0) {
       ipb[j & 1] = ip;
@@ -368,7 +369,7 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
   for (int k = 0; k < n; ++k) {
     const int p = piv[k];
     const double ip = ipb[k & 1];
-    const double *f = ws + (k & 1) * n;
+    const double *nf = ws + (k & 1) * n;  // -f_i
     const double *Sp = S + (size_t)p * n;
     if (warp == 0) {
       if (k + 1 < n) {
@@ -380,7 +381,8 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
           const int i = lane + 32 * s;
           double val = 0.;
           if (i < n) {
-            val = i == p ? spj * ip : S[i * n + j] + (-f[i]) * spj;
+            val = S[i * n + j] + nf[i] * spj;
+            if (i == p) val = spj * ip;
             D[i * n + j] = val;
           }
           v[s] = val;
@@ -392,10 +394,12 @@ __device__ double *cta_gj_inverse(double *S, double *D, int n, int *piv, int *pi
       int i = i0, j = j0;
       for (int e = ut; e < n * n; e += ustride) {
         if (j != kn) {  // column k+1 is warp 0's
-          double val;
-          if (j == k) val = i == p ? ip : -f[i];
-          else if (i == p) val = Sp[j] * ip;
-          else val = S[e] + (-f[i]) * Sp[j];
+          // one FMA per element and warp; the column-k value is a select, the pivot row (in at most two of a warp's
+          // iterations) a multiplication
+          const double nfi = nf[i];
+          double val = S[e] + nfi * Sp[j];
+          if (j == k) val = nfi;
+          if (i == p) val = j == k ? ip : Sp[j] * ip;
           D[e] = val;
         }
         i += di;
