@@ -323,3 +323,36 @@ def test_nonadiabatic_steady_slfm_library_matches_reference_gold(cuda):
     assert len(keys) == 4 + m.n_species
     for k in keys:
         np.testing.assert_allclose(lib[k[5:]], g[k], rtol=2e-4, atol=1e-4, err_msg=k)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_block_thomas_short_flamelets(cuda, name):
+    """Flamelets of 1 to 5 interior points, where the twisted elimination's halves are empty or one block long, in
+    one ragged batch: the factorization and solve against the reference's block-Thomas algorithm (the oracle)."""
+    import torch
+    import oracle as orc
+    from spitfire_gb300.flamelet import FlameletBatch, FlameletSetup, FlameletSpec
+    d, spec, og, setups0 = _setups(name, extra=False)
+    oxy, fuel, kw = FC.flamelet_case_setup(spec, FC.case(name))
+    rng = np.random.default_rng(21)
+    setups = []
+    for nzi in (1, 2, 3, 4, 5):
+        s = FlameletSetup(FlameletSpec(mech_spec=spec, initial_condition='Burke-Schumann',
+                                       **dict(kw, grid_points=nzi + 2, stoich_dissipation_rate=2.)))
+        assert s.nzi == nzi
+        s.initial_state = np.abs(s.initial_state * (1. + 0.02 * rng.standard_normal(s.initial_state.size)))
+        setups.append(s)
+    b = FlameletBatch(setups)
+    ops = _ops(og, setups)
+    ns = b.ns
+    x = torch.tensor(rng.standard_normal(b.npts * ns), dtype=torch.float64, device='cuda')
+    b.jacobian(b.initial_state())
+    b.values.neg_()
+    b.factor()
+    xsol = _split(b, b.solve(x))
+    xs = _split(b, x)
+    for f, s in enumerate(setups):
+        dd, l, piv = orc.btddod_full_factorize(-ops[f].jac(s.initial_state), s.nzi, ns)
+        ref = orc.btddod_full_solve(dd, l, piv, xs[f], s.nzi, ns)
+        assert np.max(np.abs(xsol[f] - ref)) / np.max(np.abs(ref)) < 1e-9, f
+    assert spec.griffon.device_status() == 0
