@@ -661,13 +661,16 @@ def main():
                      dtype=torch.float64, device=dev)
     g.reactor_jac_plain_batch(P, q, workspace=ws)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    g.reactor_jac_plain_batch(P, q, workspace=ws)
-    e1.record(stream)
-    e1.synchronize()
-    plain_ms = e0.elapsed_time(e1)
+    plain_runs = []
+    for _ in range(3):  # median of three launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.reactor_jac_plain_batch(P, q, workspace=ws)
+        e1.record(stream)
+        e1.synchronize()
+        plain_runs.append(e0.elapsed_time(e1))
+    plain_ms = sorted(plain_runs)[1]
     del ws
 
     # ---------------- roofline (FP64 pipe)
