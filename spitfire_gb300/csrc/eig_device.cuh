@@ -7,7 +7,8 @@
 //
 // GB300 issues FP64 at a fixed cost per warp instruction whatever the number of active lanes, so the warp
 // layout keeps lanes busy: column-parallel Hessenberg updates (no per-column reductions), reflectors in the
-// tau form (one reciprocal), and a lane-parallel deflation scan.
+// tau form (one reciprocal) in the Hessenberg reduction, unit-scaled reflectors (one reciprocal square root) in
+// the QR sweeps, and a lane-parallel deflation scan.
 //
 // Replaces the LAPACK dgeev call Griffon makes per flamelet Jacobian block for the pseudo-transient
 // continuation time step (flamelet_kernels.cpp:1329-1341).
@@ -169,46 +170,44 @@ __device__ void warp_hessenberg(double *A, int n, double *v, double *s)
   (void)s;
 }
 
-// Householder reflector P = I - tau u u^T mapping (x, y[, z]) to a multiple of e1 (u0 = x - alpha).
-__device__ __forceinline__ void house3(double x, double y, double z, int nr, double *u, double *tau)
+// Householder reflector P = I - v v^T mapping (x, y[, z]) to a multiple of e1: v = u / sqrt(beta) with
+// u = (x + sign(x) ||.||, y, z) and beta = u^T u / 2 = ||.|| (||.|| + |x|), so |v|^2 = 2. Normalizing u by one
+// reciprocal square root (instead of a square root and a reciprocal for tau = 1/beta) also drops the tau
+// multiplication from every application. Returns false when (x, y, z) is zero (P = I).
+template <int NR>
+__device__ __forceinline__ bool house3(double x, double y, double z, double *v)
 {
-  const double nn = x * x + y * y + (nr == 3 ? z * z : 0.);
-  if (nn == 0.) {
-    *tau = 0.;
-    u[0] = 1.;
-    u[1] = 0.;
-    u[2] = 0.;
-    return;
-  }
+  const double nn = x * x + y * y + (NR == 3 ? z * z : 0.);
+  if (nn == 0.) return false;
   const double nrm = sqrt(nn);
-  u[0] = x + copysign(nrm, x);
-  u[1] = y;
-  u[2] = nr == 3 ? z : 0.;
-  *tau = 1. / (nrm * (nrm + fabs(x)));
+  const double r = rsqrt(nrm * (nrm + fabs(x)));
+  v[0] = (x + copysign(nrm, x)) * r;
+  v[1] = y * r;
+  v[2] = NR == 3 ? z * r : 0.;
+  return true;
 }
 
-// Apply P = I - tau u u^T (u of length nr <= 3) to rows r0..r0+nr-1 of H over columns c0..c1, and to columns
-// r0..r0+nr-1 over rows c2..c3.
-__device__ __forceinline__ void apply_reflector(double *H, int n, const double *u, int nr, double tau, int r0, int c0,
-                                                int c1, int c2, int c3)
+// Apply P = I - v v^T (v of length NR <= 3) to rows r0..r0+NR-1 of H over columns c0..c1, and to columns
+// r0..r0+NR-1 over rows c2..c3.
+template <int NR>
+__device__ __forceinline__ void apply_reflector(double *H, int n, const double *v, int r0, int c0, int c1, int c2,
+                                                int c3)
 {
   const int lane = threadIdx.x & 31;
   for (int j = c0 + lane; j <= c1; j += 32) {
-    double s = u[0] * H[r0 + j * n] + u[1] * H[(r0 + 1) + j * n];
-    if (nr == 3) s += u[2] * H[(r0 + 2) + j * n];
-    s *= tau;
-    H[r0 + j * n] -= s * u[0];
-    H[(r0 + 1) + j * n] -= s * u[1];
-    if (nr == 3) H[(r0 + 2) + j * n] -= s * u[2];
+    double s = v[0] * H[r0 + j * n] + v[1] * H[(r0 + 1) + j * n];
+    if (NR == 3) s += v[2] * H[(r0 + 2) + j * n];
+    H[r0 + j * n] -= s * v[0];
+    H[(r0 + 1) + j * n] -= s * v[1];
+    if (NR == 3) H[(r0 + 2) + j * n] -= s * v[2];
   }
   __syncwarp();
   for (int i = c2 + lane; i <= c3; i += 32) {
-    double s = H[i + r0 * n] * u[0] + H[i + (r0 + 1) * n] * u[1];
-    if (nr == 3) s += H[i + (r0 + 2) * n] * u[2];
-    s *= tau;
-    H[i + r0 * n] -= s * u[0];
-    H[i + (r0 + 1) * n] -= s * u[1];
-    if (nr == 3) H[i + (r0 + 2) * n] -= s * u[2];
+    double s = H[i + r0 * n] * v[0] + H[i + (r0 + 1) * n] * v[1];
+    if (NR == 3) s += H[i + (r0 + 2) * n] * v[2];
+    H[i + r0 * n] -= s * v[0];
+    H[i + (r0 + 1) * n] -= s * v[1];
+    if (NR == 3) H[i + (r0 + 2) * n] -= s * v[2];
   }
   __syncwarp();
 }
@@ -300,20 +299,16 @@ __device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_ma
     double y = H[(lo + 1) + lo * n] * (H[lo + lo * n] + H[(lo + 1) + (lo + 1) * n] - s);
     double z = H[(lo + 1) + lo * n] * H[(lo + 2) + (lo + 1) * n];
     for (int k = lo - 1; k <= hi - 3; ++k) {
-      double tau;
-      house3(x, y, z, 3, u, &tau);
-      if (tau != 0.) {
+      if (house3<3>(x, y, z, u)) {
         const int c0 = k < lo ? lo : k;
         const int r1 = k + 4 < hi ? k + 4 : hi;
-        apply_reflector(H, n, u, 3, tau, k + 1, c0, hi, lo, r1);
+        apply_reflector<3>(H, n, u, k + 1, c0, hi, lo, r1);
       }
       x = H[(k + 2) + (k + 1) * n];
       y = H[(k + 3) + (k + 1) * n];
       if (k < hi - 3) z = H[(k + 4) + (k + 1) * n];
     }
-    double tau;
-    house3(x, y, 0., 2, u, &tau);
-    if (tau != 0.) apply_reflector(H, n, u, 2, tau, hi - 1, hi - 2, hi, lo, hi);
+    if (house3<2>(x, y, 0., u)) apply_reflector<2>(H, n, u, hi - 1, hi - 2, hi, lo, hi);
   }
   *out_max = vmax;
   return ok;

@@ -6,8 +6,8 @@
 //
 // Points of all flamelets are flattened: flamelet f owns interior points offsets_z[f] .. offsets_z[f+1]-1. One state
 // group evaluates one point (isobaric chemistry via reactor_eval, then the mixture-fraction stencils). The
-// block-Thomas factorization and solve are sequential in mixture fraction, so one CTA (factorization) or one warp
-// (solve) works through one flamelet, parallel within each block.
+// block-Thomas factorization and solve are sequential in mixture fraction; they run from both ends of a flamelet
+// toward its middle block, two CTAs (factorization) or two warps (solve) per flamelet, parallel within each block.
 #include "reactor_eval.cuh"
 #include "sf_internal.h"
 #include "warp_lu.cuh"
