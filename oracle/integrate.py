@@ -82,12 +82,22 @@ C = A.sum(axis=1)  # stage times t + c_s dt
 def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tolerance=1.e-10,
               nonlinear_tolerance=1.e-12, minimum_time_step_count=40, maximum_time_step_count=np.inf,
               max_nonlinear_iter=20, maximum_steps_per_jacobian=1, stop_at_time=None, delta_temperature_ignition=None,
-              minimum_allowable_residual=1.e-12, stop_at_steady=None, max_attempts=1000000, save_each_step=False):
-    """Returns dict(state, t, steps, newton_iters, jac_setups, failed_steps, status[, times, states])."""
+              minimum_allowable_residual=1.e-12, stop_at_steady=None, max_attempts=1000000, save_each_step=False,
+              stop_criteria=None, post_step_clip=True):
+    """Returns dict(state, t, steps, newton_iters, jac_setups, failed_steps, status[, times, states]).
+
+    prob gives rhs(q, t) and either jac(q) (dense; LAPACK LU of dt*gamma*J - I) or linear_setup(q, prefactor) and
+    linear_solve(r) (its own factorization of prefactor*J - I), and either Tidx (one temperature scaled by 1e3) or
+    weights (the norm weighting, 1 / variable scales). stop_criteria(t, state, residual, steps) -> bool is checked
+    after every attempt, before the minimum step count, as odesolve does (integrator.py:629-641)."""
     neq = q0.size
-    w = np.ones(neq)
-    w[prob.Tidx] = 1. / 1.e3  # 1 / variable_scales (reactors.py:321-322)
-    T0 = q0[prob.Tidx]
+    if hasattr(prob, 'weights'):
+        w = np.asarray(prob.weights, dtype=np.float64)
+    else:
+        w = np.ones(neq)
+        w[prob.Tidx] = 1. / 1.e3  # 1 / variable_scales (reactors.py:321-322)
+    T0 = q0[prob.Tidx] if delta_temperature_ignition is not None else None
+    own_setup = hasattr(prob, 'linear_setup')
     state = q0.astype(np.float64).copy()
     t = 0.
     dt = first_time_step
@@ -111,9 +121,12 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
         if coerce and t + dt > stop_at_time:
             dt = stop_at_time - t
         if eval_setup:
-            Jm = prob.jac(state) * (dt * GAMMA)
-            Jm[np.diag_indices(neq)] -= 1.
-            lu, piv, _ = dgetrf(Jm)
+            if own_setup:
+                prob.linear_setup(state, dt * GAMMA)
+            else:
+                Jm = prob.jac(state) * (dt * GAMMA)
+                Jm[np.diag_indices(neq)] -= 1.
+                lu, piv, _ = dgetrf(Jm)
             njac += 1
         setup_count += 1
         # ---- ESDIRK64 single step (methods.py:502-612)
@@ -128,7 +141,7 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
             conv = False
             f = k[s - 1]
             for it in range(1, max_nonlinear_iter + 1):
-                dx = dgetrs(lu, piv, resid)[0]
+                dx = prob.linear_solve(resid) if own_setup else dgetrs(lu, piv, resid)[0]
                 Y = Y - dx
                 f = prob.rhs(Y, t + C[s] * dt)
                 resid = dt * (GAMMA * f + prior) - (Y - state)
@@ -150,7 +163,8 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
             state = state + dstate
             t = t + dt
             nsteps += 1
-            state[state < 0.] = 0.  # post_step_callback (reactors.py:506-508)
+            if post_step_clip:
+                state[state < 0.] = 0.  # post_step_callback (reactors.py:506-508, flamelet.py:1119-1121)
             if save_each_step:
                 times.append(t)
                 states.append(state.copy())
@@ -180,6 +194,8 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
             eval_setup = True
             nfail += 1
         cont = True
+        if stop_criteria is not None:
+            cont = not stop_criteria(t, state, residual, nsteps)
         if delta_temperature_ignition is not None:
             ignited = state[prob.Tidx] > T0 + delta_temperature_ignition
             if residual > minimum_allowable_residual:

@@ -23,7 +23,13 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
   nonadiabatic_steady_slfm_gold.npz  dimensions, temperature, mass fractions and enthalpy defect of
                        tests/tabulation/nonadiabatic_defect_steady_slfm/gold.pkl
 
+  nonadiabatic_transient_slfm_gold.npz  the reference's transient heat-loss trajectory of one H2 flamelet
+                       (times, temperatures, sampled mass fractions, heat-loss parameters) and the dimensions,
+                       temperature, mass fractions and enthalpy defect of
+                       tests/tabulation/nonadiabatic_defect_transient_slfm/gold.pkl
+
 Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
+                                           [transient]
 """
 import json
 import os
@@ -354,6 +360,57 @@ def nonadiabatic():
     print('nonadiabatic steady slfm gold', np.asarray(st['properties']['temperature']).shape)
 
 
+def transient():
+    """The reference's transient heat-loss integration (Flamelet.integrate_for_heat_loss) of the H2 flamelet of
+    tests/tabulation/nonadiabatic_defect_transient_slfm (air 1200 K / H2 300 K, 34 points) at chi_st = 1, started
+    from the reference's own adiabatic steady solution with the transient defect builder's settings
+    (tabulation.py:341-352), and that test's gold library."""
+    import ref_harness as rh
+    ns_ref = rh.load_reference()
+    ref = rh.ReferenceMechanism(os.path.join(MECHS, 'h2-burke.yaml'), 'h2-burke')
+    spec = ref.spec
+    air = spec.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = spec.stream('TPY', (300., 101325., 'H2:1'))
+    FSpec, Fl = ns_ref.flamelet.FlameletSpec, ns_ref.flamelet.Flamelet
+    base = dict(mech_spec=ref, oxy_stream=air, fuel_stream=fuel, grid_points=34)
+    # the reference's Burke-Schumann start needs Cantera stream enthalpies: the same profile from this project's
+    # burke_schumann_state on the reference's grid instead
+    from spitfire_gb300.flamelet import burke_schumann_state
+    z = np.asarray(Fl(FSpec(initial_condition='linear-TY', stoich_dissipation_rate=1., **base))._z)
+    ic = burke_schumann_state(spec, air, fuel, z, 101325.)
+    f0 = Fl(FSpec(initial_condition=ic, stoich_dissipation_rate=1., **base))
+    f0.compute_steady_state(tolerance=1.e-6)
+    ad = np.copy(f0._current_state)
+    heat = dict(heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                convection_coefficient=1.e7, radiative_emissivity=0.)
+    f1 = Fl(FSpec(initial_condition=ad, stoich_dissipation_rate=1., **dict(base, **heat)))
+    lib = f1.integrate_for_heat_loss(first_time_step=1.e-9, max_time_step=1.e-1, transient_tolerance=1.e-10,
+                                     write_log=False, log_rate=100, print_exception_on_failure=False)
+    t = np.asarray(lib.dim('time').values)
+    T = np.asarray(lib['temperature'])
+    names = spec.species_names
+    Y = np.stack([np.asarray(lib['mass fraction ' + n]) for n in names], axis=-1)
+    pick = np.unique(np.r_[np.arange(0, t.size, 25), t.size - 1])
+    out = dict(z=np.asarray(f1._z), adiabatic_state=ad, times=t, T=T, pick=pick, Y_pick=Y[pick],
+               T_conv=np.asarray(f1._T_conv), h_conv=np.asarray(f1._h_conv), T_rad=np.asarray(f1._T_rad),
+               h_rad=np.asarray(f1._h_rad))
+    print('transient heat loss: steps', t.size - 1, 'final max T', T[-1].max())
+    d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'nonadiabatic_defect_transient_slfm', 'gold.pkl'),
+                'rb')).load()
+    st = d._st
+    for i in range(len(st['dim_ordering'])):
+        n = st['dim_ordering'][i]
+        out['dim%d_name' % i] = np.array(n)
+        out['dim%d_values' % i] = np.asarray(st['dimensions'][n]['values'])
+    for k, v in st['properties'].items():
+        if k in ('temperature', 'enthalpy_defect', 'enthalpy', 'pressure') or k.startswith('mass fraction'):
+            out['prop:' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'nonadiabatic_transient_slfm_gold.npz'), **out)
+    print('nonadiabatic transient slfm gold', np.asarray(st['properties']['temperature']).shape)
+
+
 def slfm_gold():
     d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'adiabatic_slfm', 'gold.pkl'), 'rb')).load()
     st = d._st
@@ -387,3 +444,5 @@ if __name__ == '__main__':
         open_kernels()
     if 'nonadiabatic' in what:
         nonadiabatic()
+    if 'transient' in what:
+        transient()
