@@ -578,6 +578,11 @@ class FlameletBatch:
         conv = run & ~dead & (res <= tolerance)
         return state, conv, it
 
+    def integrate(self, state=None, **kwargs):
+        """Transient integration of every flamelet of the batch (Flamelet.integrate, flamelet.py:1046-1213, for all
+        of them at once); see _integrate_batch for the arguments and results."""
+        return _integrate_batch(self, state, **kwargs)
+
     def compute_steady_state(self, state=None, tolerance=1.e-6, newton_iterations=38, psitc_iterations=400):
         """Newton (38 iterations), then psitc (400) for the flamelets Newton did not converge
         (flamelet.py:1705-1778; the ESDIRK fallback is not on the GPU path)."""
@@ -589,6 +594,180 @@ class FlameletBatch:
         s2, c2, i2 = self.steady_solve_psitc(init, active=~c1, tolerance=tolerance, max_iterations=psitc_iterations)
         out = torch.where(self.expand(c1), s1, s2)
         return out, c1 | c2, {'newton': c1, 'psitc': c2 & ~c1}
+
+
+# ESDIRK64 (Kennedy & Carpenter's six-stage, fourth-order ESDIRK with a third-order embedded estimate), the
+# published tableau that spitfire/time/methods.py:464-500 and the batched reactor integrator use
+_ESDIRK_GAMMA = 0.25
+_ESDIRK_A = np.array([[0., 0., 0., 0., 0., 0.],
+                      [0.25, 0.25, 0., 0., 0., 0.],
+                      [8611. / 62500., -1743. / 31250., 0.25, 0., 0., 0.],
+                      [5012029. / 34652500., -654441. / 2922500., 174375. / 388108., 0.25, 0., 0.],
+                      [15267082809. / 155376265600., -71443401. / 120774400., 730878875. / 902184768.,
+                       2285395. / 8070912., 0.25, 0.],
+                      [82889. / 524892., 0., 15625. / 83664., 69875. / 102672., -2260. / 8211., 0.25]])
+_ESDIRK_B = _ESDIRK_A[5].copy()
+_ESDIRK_BH = np.array([4586570599. / 29645900160., 0., 178811875. / 945068544., 814220225. / 1159782912.,
+                       -3700637. / 11593932., 61727. / 225920.])
+
+
+def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_at_steady=None,
+                     first_time_step=1.e-6, max_time_step=1.e-3, minimum_time_step_count=40,
+                     maximum_time_step_count=None, transient_tolerance=1.e-10, maximum_steps_per_jacobian=10,
+                     nonlinear_solve_tolerance=1.e-12, max_nonlinear_iter=20, save_each_step=True, active=None,
+                     max_attempts=1000000):
+    """Transient integration of every flamelet of the batch b, each with its own time, step size and Jacobian.
+
+    Batched restatement of Flamelet.integrate (flamelet.py:1046-1213) with its defaults: odesolve
+    (time/integrator.py:229-713) driving ESDIRK64 (time/methods.py:441-612), SimpleNewtonSolver (time/nonlinear.py:
+    185-268; frozen Jacobian, weighted inf-norm below nonlinear_solve_tolerance, max_nonlinear_iter iterations) and
+    PIController (time/stepcontrol.py:84-101). The linear setup is prefactor * J - I with prefactor = gamma * dt,
+    factorized by the block-Thomas kernels (flamelet.py:756-761, 881-886). It is reused for up to
+    maximum_steps_per_jacobian steps and redone after a slow Newton solve or a step-size change beyond
+    [0.9, 1.05] (integrator.py:100-130). Negative entries are clipped after every accepted step
+    (flamelet.py:1119-1121). Each round of the loop is one step attempt of every running flamelet: every Newton
+    iteration is one batched solve and one batched right-hand side over the flamelets still iterating.
+
+    stop_criteria: None or a callable (f, t, state_f, residual, steps) -> bool for flamelet f (host arrays), checked
+    after every attempt and overridden below minimum_time_step_count steps, as odesolve does (integrator.py:
+    629-641). Returns (trajectories, stats): trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted
+    step (first and last only without save_each_step); stats: per-flamelet steps, failed_steps, newton_iters,
+    jac_setups and status (1 stop_at_time, 3 steady, 4 step limit, 7 stop criteria)."""
+    torch = _torch()
+    dev = b.values.device
+    nf, ns = b.nf, b.ns
+    state = (b.initial_state() if state is None else state).clone()
+    run = np.ones(nf, dtype=bool) if active is None else \
+        np.asarray(active.cpu().numpy() if torch.is_tensor(active) else active, dtype=bool).copy()
+    seg = [(int(b.offz_host[f]) * ns, int(b.offz_host[f + 1]) * ns) for f in range(nf)]
+    t = np.zeros(nf)
+    dt = np.full(nf, float(first_time_step))
+    eval_setup = np.ones(nf, dtype=bool)
+    setup_count = np.zeros(nf, dtype=np.int64)
+    steps = np.zeros(nf, dtype=np.int64)
+    failed = np.zeros(nf, dtype=np.int64)
+    newton = np.zeros(nf, dtype=np.int64)
+    jac_setups = np.zeros(nf, dtype=np.int64)
+    attempts = np.zeros(nf, dtype=np.int64)
+    status = np.zeros(nf, dtype=np.int64)
+    host = state.cpu().numpy()
+    times = [[0.] for _ in range(nf)]
+    states = [[host[a:e].copy()] for (a, e) in seg]
+    onehot = torch.eye(nf, dtype=torch.bool, device=dev)
+    G, A, B, BH = _ESDIRK_GAMMA, _ESDIRK_A, _ESDIRK_B, _ESDIRK_BH
+    k = [torch.zeros_like(state) for _ in range(6)]
+    coerce = stop_at_time is not None
+    mask = lambda m: torch.from_numpy(np.ascontiguousarray(m)).to(dev)
+    while run.any():
+        attempts[run] += 1
+        over = run & (attempts > max_attempts)
+        status[over] = 4
+        run &= ~over
+        if not run.any():
+            break
+        if coerce:
+            dt = np.where(run & (t + dt > stop_at_time), stop_at_time - t, dt)
+        need = run & eval_setup
+        for f in np.flatnonzero(need):
+            b.jacobian(state, scale_and_offset=True, prefactor=float(dt[f] * G), active=onehot[f])
+        if need.any():
+            b.factor(active=mask(need))
+            jac_setups[need] += 1
+        setup_count[run] += 1
+        runm = mask(run)
+        dtd = b.expand(torch.from_numpy(dt).to(dev))
+        k[0] = b.rhs(state, out=k[0], active=runm)
+        Y = state.clone()
+        nl_ok = np.ones(nf, dtype=bool)
+        for st in range(1, 6):
+            prior = A[st, 0] * k[0]
+            for j in range(1, st):
+                prior = prior + A[st, j] * k[j]
+            fs = k[st - 1].clone()
+            resid = dtd * (G * fs + prior) - (Y - state)
+            go = runm.clone()
+            conv = torch.zeros(nf, dtype=torch.bool, device=dev)
+            for _ in range(max_nonlinear_iter):
+                newton += go.cpu().numpy()
+                god = b.expand(go)
+                dx = b.solve(resid, active=go)
+                Y = torch.where(god, Y - dx, Y)
+                fs = torch.where(god, b.rhs(Y, active=go), fs)
+                resid = torch.where(god, dtd * (G * fs + prior) - (Y - state), resid)
+                c = go & (b.norms(resid) < nonlinear_solve_tolerance)
+                conv |= c
+                go &= ~c
+                if not bool(go.any()):
+                    break
+            k[st] = fs
+            nl_ok &= conv.cpu().numpy() | ~run
+        dstate = B[0] * k[0]
+        derr = (B[0] - BH[0]) * k[0]
+        for j in range(1, 6):
+            dstate = dstate + B[j] * k[j]
+            derr = derr + (B[j] - BH[j]) * k[j]
+        dstate = dtd * dstate
+        err = b.norms(dtd * derr).cpu().numpy()
+        residual = b.norms(dstate).cpu().numpy() / dt
+        fin = b.finite(dstate).cpu().numpy()
+        acc = run & fin
+        if acc.any():
+            new = state + dstate
+            new = torch.where(new < 0., torch.zeros_like(new), new)
+            state = torch.where(b.expand(mask(acc)), new, state)
+        host = state.cpu().numpy()
+        for f in np.flatnonzero(run):
+            recent = dt[f]
+            if fin[f]:
+                t[f] += dt[f]
+                steps[f] += 1
+                if save_each_step:
+                    times[f].append(t[f])
+                    states[f].append(host[seg[f][0]:seg[f][1]].copy())
+                e = err[f]
+                dt[f] = min(dt[f] * 1.1, max_time_step) if e < 1.e-16 else \
+                    min(dt[f] * min(1.1, (transient_tolerance / e) ** 0.1333333333), max_time_step)
+                if setup_count[f] == maximum_steps_per_jacobian:
+                    setup_count[f] = 0
+                    eval_setup[f] = True
+                elif not nl_ok[f]:
+                    dt[f] *= 0.8
+                    eval_setup[f] = True
+                elif dt[f] > recent * 1.05 or dt[f] < recent * 0.9:
+                    eval_setup[f] = True
+                else:
+                    eval_setup[f] = False
+            else:
+                dt[f] *= 0.8
+                eval_setup[f] = True
+                failed[f] += 1
+            cont = True
+            if stop_criteria is not None:
+                cont = not stop_criteria(f, t[f], host[seg[f][0]:seg[f][1]], residual[f], steps[f])
+                if not cont:
+                    status[f] = 7
+            if steps[f] < minimum_time_step_count:
+                cont = True
+                status[f] = 0
+            if maximum_time_step_count is not None and steps[f] > maximum_time_step_count:
+                cont = False
+                status[f] = 4
+            elif coerce and t[f] >= stop_at_time:
+                cont = False
+                status[f] = 1
+            elif stop_at_steady is not None and residual[f] < stop_at_steady:
+                cont = False
+                status[f] = 3
+            if not cont:
+                run[f] = False
+    out = []
+    for f in range(nf):
+        if save_each_step:
+            out.append((np.array(times[f]), np.array(states[f])))
+        else:
+            out.append((np.array([0., t[f]]), np.array([states[f][0], host[seg[f][0]:seg[f][1]].copy()])))
+    return out, dict(steps=steps, failed_steps=failed, newton_iters=newton, jac_setups=jac_setups, status=status)
+
 
 
 class Flamelet:
@@ -678,6 +857,77 @@ class Flamelet:
             raise RuntimeError('steady flamelet solve failed (Newton and psitc)')
         self._current_state = out.cpu().numpy()
         return self.make_library_from_interior_state(self._current_state)
+
+    def integrate(self, stop_at_time=None, stop_at_steady=None, stop_criteria=None, first_time_step=1.e-6,
+                  max_time_step=1.e-3, minimum_time_step_count=40, transient_tolerance=1.e-10, write_log=False,
+                  log_rate=100, maximum_steps_per_jacobian=10, nonlinear_solve_tolerance=1.e-12,
+                  linear_solver='block thomas', save_first_and_last_only=False, print_exception_on_failure=False,
+                  **kw):
+        """Transient integration from the current state (flamelet.py:1046-1213), on the GPU kernels: ESDIRK64,
+        simple Newton and PI control with the block-Thomas linear solver. stop_criteria(t, state, residual, steps)
+        as in the reference. Returns a Library over (time, mixture_fraction) with temperature, pressure and mass
+        fractions; the current state and time move to the last step."""
+        torch = _torch()
+        if linear_solver.lower() != 'block thomas':
+            raise ValueError('only the block-Thomas linear solver is on the GPU path')
+        if stop_at_time is None and stop_at_steady is None and stop_criteria is None:
+            raise ValueError('integrate needs stop_at_time, stop_at_steady or stop_criteria')
+        crit = None if stop_criteria is None else (lambda f, t, st, res, n: stop_criteria(t, st, res, n))
+        st = torch.tensor(self._current_state, dtype=torch.float64, device='cuda')
+        t0 = getattr(self, '_current_time', 0.)
+        traj, _ = self._b().integrate(st, stop_criteria=crit,
+                                      stop_at_time=None if stop_at_time is None else stop_at_time - t0,
+                                      stop_at_steady=stop_at_steady, first_time_step=first_time_step,
+                                      max_time_step=max_time_step, minimum_time_step_count=minimum_time_step_count,
+                                      transient_tolerance=transient_tolerance,
+                                      maximum_steps_per_jacobian=maximum_steps_per_jacobian,
+                                      nonlinear_solve_tolerance=nonlinear_solve_tolerance,
+                                      save_each_step=not save_first_and_last_only)
+        times, states = traj[0]
+        times = times + t0
+        self._current_state = states[-1].copy()
+        self._current_time = float(times[-1])
+        if save_first_and_last_only:
+            times, states = times[-1:], states[-1:]
+        return self._library_over_time(times, states)
+
+    def integrate_to_steady(self, steady_tolerance=1.e-4, **kwargs):
+        """flamelet.py:1215-1225."""
+        return self.integrate(stop_at_steady=steady_tolerance, **kwargs)
+
+    def integrate_to_time(self, final_time, **kwargs):
+        """flamelet.py:1227-1237."""
+        return self.integrate(stop_at_time=final_time, **kwargs)
+
+    def integrate_for_heat_loss(self, temperature_tolerance=0.05, steady_tolerance=1.e-4, **kwargs):
+        """flamelet.py:1263-1286: integrate until max(state) < (1 + temperature_tolerance) max(T_oxy, T_fuel) or
+        the step residual falls below steady_tolerance."""
+        T_bc_max = max(self.oxy_stream.T, self.fuel_stream.T)
+
+        def stop(t, state, residual, *args):
+            return np.max(state) < (1. + temperature_tolerance) * T_bc_max or residual < steady_tolerance
+
+        return self.integrate(stop_criteria=stop, **kwargs)
+
+    def _library_over_time(self, times, states):
+        from .library import Dimension, Library
+        s = self._setup
+        ns = s.mech.n_species
+        lib = Library(Dimension('time', np.asarray(times)), Dimension('mixture_fraction', s.z))
+        lib.extra_attributes['mech_spec'] = s.mech
+        nt = len(times)
+        st = np.asarray(states).reshape(nt, s.nzi, ns)
+        full = np.concatenate([np.broadcast_to(s.state_oxy, (nt, 1, ns)), st,
+                               np.broadcast_to(s.state_fuel, (nt, 1, ns))], axis=1)
+        lib['temperature'] = full[:, :, 0].copy()
+        lib['pressure'] = np.full((nt, s.z.size), s.pressure)
+        names = s.mech.species_names
+        last = np.ones((nt, s.z.size))
+        for i, sp in enumerate(names[:-1]):
+            lib['mass fraction ' + sp] = full[:, :, 1 + i].copy()
+            last -= full[:, :, 1 + i]
+        lib['mass fraction ' + names[-1]] = last
+        return lib
 
     def make_library_from_interior_state(self, state):
         from .library import Dimension, Library

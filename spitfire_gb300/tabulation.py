@@ -1,5 +1,5 @@
 """Steady laminar flamelet (SLFM) libraries on the GPU flamelet solvers: adiabatic, and nonadiabatic with an
-enthalpy-defect dimension from quasisteady heat loss.
+enthalpy-defect dimension from quasisteady or transient heat loss.
 
 ``build_adiabatic_slfm_library`` keeps the interface and behaviour of spitfire/chemistry/tabulation.py:229-336:
 a sequential continuation in the dissipation rate, each flamelet started from the previous converged profile,
@@ -16,6 +16,10 @@ subsampled every h_stoich_spacing of stoichiometric enthalpy, then interpolated 
 stoichiometric enthalpy defects (tabulation.py:594-665) and returned over (mixture_fraction,
 dissipation_rate_stoich, enthalpy_defect_stoich). The continuations of all dissipation rates advance together,
 each step one batched steady solve.
+
+``build_nonadiabatic_defect_transient_slfm_library`` keeps the interface of tabulation.py:727-784: the same
+defect dimension from transient heat loss instead, every burning dissipation rate's heat-loss flamelet integrated
+in time (ESDIRK64 on the GPU kernels) until its temperature profile is nearly linear, all of them in one batch.
 
 ``solve_steady_flamelets`` solves any number of independent flamelets (own grids, dissipation rates, initial
 profiles) at once, every solver iteration one batched launch per operation over all of them.
@@ -267,6 +271,15 @@ def build_nonadiabatic_defect_steady_slfm_library(flamelet_specs, diss_rate_valu
     if verbose:
         print('expanding (steady) enthalpy defect dimension ...', flush=True)
     unstructured = _expand_defect_steady(flamelet_specs, table, list(x_values), h_stoich_spacing, verbose)
+    lib = _defect_library(m, unstructured, n_defect_st, extend_defect_dim, diss_rate_log_scaled)
+    if verbose:
+        print(f'library built in {perf_counter() - t00:6.2f} s')
+    return lib
+
+
+def _defect_library(m, unstructured, n_defect_st, extend_defect_dim, diss_rate_log_scaled):
+    """The structured defect table as a Library over (mixture_fraction, dissipation_rate_stoich,
+    enthalpy_defect_stoich) (tabulation.py:694-724)."""
     st, xs, gs = _structure_defect(unstructured, n_defect_st, extend_defect_dim)
     key0 = next(iter(st))
     lib = Library(Dimension(_mixture_fraction_name, st[key0][_mixture_fraction_name]),
@@ -279,13 +292,106 @@ def build_nonadiabatic_defect_steady_slfm_library(flamelet_specs, diss_rate_valu
             for ig, g in enumerate(gs):
                 vals[:, ix, ig] = st[(x, g)][q]
         lib[q] = vals
-    if verbose:
-        print(f'library built in {perf_counter() - t00:6.2f} s')
     return lib
 
 
-def build_nonadiabatic_defect_transient_slfm_library(*args, **kwargs):
-    """tabulation.py:727-784 expands the defect dimension by transient flamelet integration
-    (Flamelet.integrate_for_heat_loss), which is not on the GPU path; the steady variant is."""
-    raise NotImplementedError('transient flamelet integration is not on the GPU path; use '
-                              'build_nonadiabatic_defect_steady_slfm_library')
+def _expand_defect_transient(flamelet_specs, table, chis, h_stoich_spacing, integration_args, verbose):
+    """Transient heat loss of every dissipation rate (tabulation.py:339-406), all integrated together: each
+    flamelet starts from its adiabatic steady state with scaled convective heat loss (coefficient 1e7 unless the
+    specs give one, scaled by the temperature range and the dissipation rate, linear reference temperature profile,
+    no radiation) and runs until its temperature profile is nearly linear or it is steady (integrate_for_heat_loss,
+    flamelet.py:1263-1286). Flamelets whose integration fails are retried with a 100x lower tolerance, as the
+    reference does, down to 1e-15. Each trajectory is subsampled every h_stoich_spacing of stoichiometric enthalpy,
+    the first and last states always kept. Returns the unstructured table {(chi_st, g_st): data}."""
+    m = flamelet_specs.mech_spec
+    hc = flamelet_specs.convection_coefficient if flamelet_specs.convection_coefficient is not None else 1.e7
+    fs = _spec_copy(flamelet_specs, heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                    scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                    convection_coefficient=hc, radiative_emissivity=0., dissipation_rate=None,
+                    max_dissipation_rate=None)
+    args = {'first_time_step': 1.e-9, 'max_time_step': 1.e-1}
+    args.update(integration_args or {})
+    for key in ('write_log', 'log_rate', 'print_exception_on_failure', 'linear_solver'):
+        args.pop(key, None)
+    tol = args.pop('transient_tolerance', 1.e-8)
+    temperature_tolerance = args.pop('temperature_tolerance', 0.05)
+    steady_tolerance = args.pop('steady_tolerance', 1.e-4)
+    T_bc_max = max(flamelet_specs.oxy_stream.T, flamelet_specs.fuel_stream.T)
+
+    def stop(f, t, state, residual, steps):
+        return np.max(state) < (1. + temperature_tolerance) * T_bc_max or residual < steady_tolerance
+
+    pending = list(range(len(chis)))
+    done = {}
+    while pending:
+        if tol <= 1.e-15:
+            raise RuntimeError('transient heat-loss integration failed for chi_st = '
+                               + ', '.join(f'{chis[i]:.3e}' for i in pending))
+        setups = [FlameletSetup(_spec_copy(fs, stoich_dissipation_rate=float(chis[i]),
+                                           initial_condition=table[chis[i]]['adiabatic_state'])) for i in pending]
+        traj, stats = FlameletBatch(setups).integrate(stop_criteria=stop, transient_tolerance=tol, **args)
+        retry = []
+        for j, i in enumerate(pending):
+            ok = stats['status'][j] != 4 and np.all(np.isfinite(traj[j][1][-1]))
+            if ok:
+                done[i] = (setups[j], traj[j])
+            else:
+                retry.append(i)
+        if verbose:
+            print(f'  transient heat loss at tolerance {tol:.1e}: {len(pending) - len(retry)} of {len(pending)} '
+                  f'flamelets done', flush=True)
+        pending = retry
+        tol *= 1.e-2
+    z_st = m.stoich_mixture_fraction(flamelet_specs.fuel_stream, flamelet_specs.oxy_stream)
+    out = {}
+    for i, chi in enumerate(chis):
+        setup, (times, states) = done[i]
+        z = setup.z
+        sols = [_library_of(setup, st) for st in states]
+        h_tz = np.stack([_enthalpy_of_props(m, sol) for sol in sols], axis=0)  # [nt, nz]
+        h_ad = h_tz[0]
+        nt = h_tz.shape[0]
+        indices = [0]
+        last_hst = np.interp(z_st, z, h_ad)
+        for t in range(nt):
+            this_hst = np.interp(z_st, z, h_tz[t])
+            if last_hst - this_hst > h_stoich_spacing:
+                indices.append(t)
+                last_hst = this_hst
+        if nt - 1 not in indices:
+            indices.append(nt - 1)
+        for t in indices:
+            defect = h_tz[t] - h_ad
+            gst = float(np.interp(z_st, z, defect))
+            data = {'enthalpy_defect': defect.copy(), 'enthalpy_cons': h_ad.copy(), 'enthalpy': h_tz[t].copy(),
+                    _mixture_fraction_name: z.copy()}
+            for q, v in sols[t].items():
+                data[q] = np.asarray(v).copy()
+            out[(chi, gst)] = data
+    return out
+
+
+def build_nonadiabatic_defect_transient_slfm_library(flamelet_specs, diss_rate_values=np.logspace(-3, 2, 16),
+                                                     diss_rate_ref='stoichiometric', verbose=True,
+                                                     solver_verbose=False, h_stoich_spacing=10.e3, num_procs=1,
+                                                     integration_args=None, n_defect_st=32,
+                                                     extend_defect_dim=False, diss_rate_log_scaled=True):
+    """SLFM library with an enthalpy-defect dimension from transient heat loss (tabulation.py:727-784): the adiabatic
+    library, then every burning dissipation rate's heat-loss flamelet integrated in time on the GPU (all of them in
+    one batch), subsampled, and interpolated onto n_defect_st stoichiometric enthalpy defects. num_procs is accepted
+    for interface compatibility: the integrations already run together on the device. integration_args go to the
+    heat-loss integration as in the reference (transient_tolerance, first_time_step, max_time_step, ...)."""
+    if isinstance(flamelet_specs, dict):
+        flamelet_specs = FlameletSpec(**flamelet_specs)
+    m = flamelet_specs.mech_spec
+    t00 = perf_counter()
+    table, z, x_values = build_adiabatic_slfm_library(flamelet_specs, diss_rate_values, diss_rate_ref,
+                                                      verbose, solver_verbose, _return_intermediates=True)
+    if verbose:
+        print('expanding (transient) enthalpy defect dimension ...', flush=True)
+    unstructured = _expand_defect_transient(flamelet_specs, table, list(x_values), h_stoich_spacing,
+                                            integration_args, verbose)
+    lib = _defect_library(m, unstructured, n_defect_st, extend_defect_dim, diss_rate_log_scaled)
+    if verbose:
+        print(f'library built in {perf_counter() - t00:6.2f} s')
+    return lib

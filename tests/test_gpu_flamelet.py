@@ -357,3 +357,63 @@ def test_block_thomas_short_flamelets(cuda, name):
         ref = orc.btddod_full_solve(dd, l, piv, xs[f], s.nzi, ns)
         assert np.max(np.abs(xsol[f] - ref)) / np.max(np.abs(ref)) < 1e-9, f
     assert spec.griffon.device_status() == 0
+
+
+def test_heat_loss_integration_matches_reference_trajectory(cuda):
+    """Flamelet.integrate_for_heat_loss on the GPU kernels (ESDIRK64, simple Newton, PI control, block-Thomas
+    setups) against the reference's own heat-loss trajectory of the H2 flamelet of
+    tests/tabulation/nonadiabatic_defect_transient_slfm at chi_st = 1 (tests/golden/nonadiabatic_transient_slfm_gold.npz):
+    the same accepted-step count, step times and interior temperatures within 1e-7 relative, sampled mass
+    fractions within 1e-5 relative (1e-9 absolute)."""
+    import os
+    from spitfire_gb300.flamelet import Flamelet, FlameletSpec
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    g = np.load(os.path.join(FC.GOLD, 'nonadiabatic_transient_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    f = Flamelet(FlameletSpec(mech_spec=m, oxy_stream=air, fuel_stream=fuel, grid_points=34,
+                              initial_condition=g['adiabatic_state'], stoich_dissipation_rate=1.,
+                              heat_transfer='nonadiabatic', scale_heat_loss_by_temp_range=True,
+                              scale_convection_by_dissipation=True, use_linear_ref_temp_profile=True,
+                              convection_coefficient=1.e7, radiative_emissivity=0.))
+    lib = f.integrate_for_heat_loss(first_time_step=1.e-9, max_time_step=1.e-1, transient_tolerance=1.e-10)
+    t = lib.dim('time').values
+    assert t.size == g['times'].size
+    np.testing.assert_allclose(t, g['times'], rtol=1e-7)
+    np.testing.assert_allclose(lib['temperature'], g['T'], rtol=1e-7)
+    pick = g['pick']
+    for i, n in enumerate(m.species_names):
+        np.testing.assert_allclose(lib['mass fraction ' + n][pick], g['Y_pick'][:, :, i], rtol=1e-5, atol=1e-9,
+                                   err_msg=n)
+    assert m.griffon.device_status() == 0
+
+
+def test_nonadiabatic_transient_slfm_library_matches_reference_gold(cuda):
+    """tests/tabulation/nonadiabatic_defect_transient_slfm of the reference (h2-burke, air 1200 K / H2 300 K, 34
+    points, chi_st = logspace(0, 1, 4), transient_tolerance 1e-10, 32 stoichiometric enthalpy defects) through the
+    drop-in build_nonadiabatic_defect_transient_slfm_library: that test's bars (rtol 2e-4, atol 1e-4) on
+    temperature, pressure, every mass fraction, the enthalpy and the enthalpy defect, and the library dimensions;
+    the enthalpy recomputed from the library's states afterwards, as that test does."""
+    import os
+    from spitfire_gb300.analysis import compute_specific_enthalpy
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    from spitfire_gb300.tabulation import build_nonadiabatic_defect_transient_slfm_library
+    g = np.load(os.path.join(FC.GOLD, 'nonadiabatic_transient_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    lib = build_nonadiabatic_defect_transient_slfm_library(
+        dict(mech_spec=m, oxy_stream=air, fuel_stream=fuel, grid_points=34), verbose=False,
+        diss_rate_values=np.logspace(0, 1, 4), integration_args={'transient_tolerance': 1e-10}, num_procs=1)
+    lib = compute_specific_enthalpy(m, lib)
+    assert lib.dim_names == ['mixture_fraction', 'dissipation_rate_stoich', 'enthalpy_defect_stoich']
+    np.testing.assert_allclose(lib.dims[0].values, g['dim0_values'], rtol=1e-14)
+    np.testing.assert_allclose(lib.dims[1].values, g['dim1_values'], rtol=1e-12)
+    np.testing.assert_allclose(lib.dims[2].values, g['dim2_values'], rtol=2e-4, atol=1e-4)
+    keys = [k for k in g.files if k.startswith('prop:')]
+    assert len(keys) == 4 + m.n_species
+    for k in keys:
+        np.testing.assert_allclose(lib[k[5:]], g[k], rtol=2e-4, atol=1e-4, err_msg=k)
