@@ -396,7 +396,8 @@ def bench_flamelet(spec, rank, stream, cpu):
     res = {'flamelets': N_FLAMELETS, 'points': pts, 'value': world * N_FLAMELETS / wall, 'unit': 'flamelets/s',
            'seconds': wall, 'points_per_s': world * pts / wall,
            'converged': int(conv_h.sum()), 'by_newton': int(how['newton'].sum().item()),
-           'by_psitc': int(how['psitc'].sum().item()), 'extinguished': int(sum(ext)),
+           'by_psitc': int(how['psitc'].sum().item()), 'by_esdirk': int(how['esdirk'].sum().item()),
+           'extinguished': int(sum(ext)),
            'device_status': spec.griffon.device_status()}
     # one batched launch of each operation on the converged profiles
     x = out.clone()

@@ -576,6 +576,10 @@ class FlameletBatch:
                     rhs = torch.where(e, self.rhs(state, active=rst), rhs)
         state = torch.clamp(state, min=0.)
         conv = run & ~dead & (res <= tolerance)
+        # smallest pseudo-time step of each flamelet where it stopped (the reference's psitc returns it, and
+        # compute_steady_state starts its ESDIRK fallback from 1e-2 of it)
+        self.last_psitc_min_ds = torch.full((nf,), float('inf'), dtype=torch.float64, device=dev).scatter_reduce(
+            0, self.dof_flamelet, ds, reduce='amin', include_self=True)
         return state, conv, it
 
     def integrate(self, state=None, **kwargs):
@@ -583,17 +587,37 @@ class FlameletBatch:
         of them at once); see _integrate_batch for the arguments and results."""
         return _integrate_batch(self, state, **kwargs)
 
-    def compute_steady_state(self, state=None, tolerance=1.e-6, newton_iterations=38, psitc_iterations=400):
-        """Newton (38 iterations), then psitc (400) for the flamelets Newton did not converge
-        (flamelet.py:1705-1778; the ESDIRK fallback is not on the GPU path)."""
+    def compute_steady_state(self, state=None, tolerance=1.e-6, newton_iterations=38, psitc_iterations=400,
+                             transient_args=None):
+        """compute_steady_state of flamelet.py:1705-1778 for the whole batch: Newton (38 iterations); psitc (400) for
+        the flamelets Newton did not converge; ESDIRK64 time integration to a steady state from the initial guess
+        for those psitc did not converge either (steady tolerance `tolerance`, transient tolerance 1e-8, steps of at
+        most 1e4 starting at 1e-2 of psitc's smallest pseudo-time step, the Jacobian reused for up to 10 steps;
+        transient_args override these). Returns (state, converged [nf], {'newton', 'psitc', 'esdirk'} masks)."""
         torch = _torch()
         init = self.initial_state() if state is None else state
         s1, c1, i1 = self.steady_solve_newton(init, tolerance=tolerance, max_iterations=newton_iterations)
+        none = torch.zeros_like(c1)
         if bool(c1.all()):
-            return s1, c1, {'newton': c1, 'psitc': torch.zeros_like(c1)}
+            return s1, c1, {'newton': c1, 'psitc': none, 'esdirk': none}
         s2, c2, i2 = self.steady_solve_psitc(init, active=~c1, tolerance=tolerance, max_iterations=psitc_iterations)
         out = torch.where(self.expand(c1), s1, s2)
-        return out, c1 | c2, {'newton': c1, 'psitc': c2 & ~c1}
+        conv = c1 | c2
+        esdirk = none.clone()
+        if not bool(conv.all()):
+            fail = (~conv).cpu().numpy()
+            mds = self.last_psitc_min_ds.cpu().numpy()
+            args = dict(stop_at_steady=tolerance, transient_tolerance=1.e-8, max_time_step=1.e4,
+                        first_time_step=np.where(np.isfinite(mds), 1.e-2 * mds, 1.e-8),
+                        maximum_steps_per_jacobian=10, save_each_step=False)
+            args.update(transient_args or {})
+            traj, stats = self.integrate(init, active=fail, **args)
+            for f in np.flatnonzero(fail & (stats['status'] == 3)):
+                lo, hi = int(self.offz_host[f]) * self.ns, int(self.offz_host[f + 1]) * self.ns
+                out[lo:hi] = torch.from_numpy(traj[f][1][-1]).to(out.device)
+                esdirk[f] = True
+            conv = conv | esdirk
+        return out, conv, {'newton': c1, 'psitc': c2 & ~c1, 'esdirk': esdirk}
 
 
 # ESDIRK64 (Kennedy & Carpenter's six-stage, fourth-order ESDIRK with a third-order embedded estimate), the
@@ -628,9 +652,9 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
     (flamelet.py:1119-1121). Each round of the loop is one step attempt of every running flamelet: every Newton
     iteration is one batched solve and one batched right-hand side over the flamelets still iterating.
 
-    stop_criteria: None or a callable (f, t, state_f, residual, steps) -> bool for flamelet f (host arrays), checked
-    after every attempt and overridden below minimum_time_step_count steps, as odesolve does (integrator.py:
-    629-641). Returns (trajectories, stats): trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted
+    first_time_step: a number or one per flamelet. stop_criteria: None or a callable (f, t, state_f, residual,
+    steps) -> bool for flamelet f (host arrays), checked after every attempt and overridden below
+    minimum_time_step_count steps, as odesolve does (integrator.py:629-641). Returns (trajectories, stats): trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted
     step (first and last only without save_each_step); stats: per-flamelet steps, failed_steps, newton_iters,
     jac_setups and status (1 stop_at_time, 3 steady, 4 step limit, 7 stop criteria)."""
     torch = _torch()
@@ -641,7 +665,7 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
         np.asarray(active.cpu().numpy() if torch.is_tensor(active) else active, dtype=bool).copy()
     seg = [(int(b.offz_host[f]) * ns, int(b.offz_host[f + 1]) * ns) for f in range(nf)]
     t = np.zeros(nf)
-    dt = np.full(nf, float(first_time_step))
+    dt = np.broadcast_to(np.asarray(first_time_step, dtype=np.float64), (nf,)).copy()  # a number or one per flamelet
     eval_setup = np.ones(nf, dtype=bool)
     setup_count = np.zeros(nf, dtype=np.int64)
     steps = np.zeros(nf, dtype=np.int64)
@@ -854,7 +878,7 @@ class Flamelet:
         st = torch.tensor(self._current_state, dtype=torch.float64, device='cuda')
         out, conv, _ = b.compute_steady_state(st, tolerance=tolerance)
         if not bool(conv[0]):
-            raise RuntimeError('steady flamelet solve failed (Newton and psitc)')
+            raise RuntimeError('steady flamelet solve failed (Newton, psitc and ESDIRK time integration)')
         self._current_state = out.cpu().numpy()
         return self.make_library_from_interior_state(self._current_state)
 

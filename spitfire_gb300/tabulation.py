@@ -66,11 +66,12 @@ def solve_steady_flamelets(setups, tolerance=1.e-6):
     out = out.cpu().numpy()
     conv = conv.cpu().numpy()
     newton = how['newton'].cpu().numpy()
+    esdirk = how['esdirk'].cpu().numpy()
     states, methods = [], []
     for f, s in enumerate(setups):
         lo, hi = b.offz_host[f] * b.ns, b.offz_host[f + 1] * b.ns
         states.append(out[lo:hi].copy() if conv[f] else None)
-        methods.append(None if not conv[f] else ('newton' if newton[f] else 'psitc'))
+        methods.append(None if not conv[f] else ('newton' if newton[f] else ('esdirk' if esdirk[f] else 'psitc')))
     return states, methods
 
 

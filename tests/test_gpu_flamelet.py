@@ -417,3 +417,34 @@ def test_nonadiabatic_transient_slfm_library_matches_reference_gold(cuda):
     assert len(keys) == 4 + m.n_species
     for k in keys:
         np.testing.assert_allclose(lib[k[5:]], g[k], rtol=2e-4, atol=1e-4, err_msg=k)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_integrate_to_steady_matches_oracle_and_newton(cuda, name):
+    """The ESDIRK64 path compute_steady_state falls back to (integrate_to_steady with steady tolerance 1e-6,
+    transient tolerance 1e-8, steps up to 1e4 from 1e-8): from the case's perturbed Burke-Schumann profile, the
+    accepted-step count of the oracle's restatement of odesolve within two steps and final states within 1e-5
+    relative. The run stops when the step residual falls below 1e-6, and in the last steps the residual sits at the
+    threshold to rounding (h2: 177 steps here, 178 in the oracle). The steady temperatures of the batched Newton
+    solver agree within 1e-4 relative."""
+    import torch
+    import flamelet_steady as FS
+    import flamelet_transient as FT
+    from integrate import integrate
+    from spitfire_gb300.flamelet import FlameletBatch
+    d, spec, og, setups = _setups(name, extra=False)
+    s = setups[0]
+    b = FlameletBatch(setups)
+    st0 = torch.tensor(s.initial_state, dtype=torch.float64, device='cuda')
+    kw = dict(stop_at_steady=1.e-6, transient_tolerance=1.e-8, max_time_step=1.e4, first_time_step=1.e-8,
+              maximum_steps_per_jacobian=10)
+    traj, stats = b.integrate(st0, save_each_step=False, **kw)
+    op = FS.FlameletOperator(og, s.z, s.x, s.state_oxy, s.state_fuel)
+    r = integrate(FT.FlameletTransientProblem(op), s.initial_state, **kw)
+    assert stats['status'][0] == 3
+    assert abs(int(stats['steps'][0]) - r['steps']) <= 2
+    np.testing.assert_allclose(traj[0][1][-1], r['state'], rtol=1e-5, atol=1e-10)
+    newton, conv, _ = b.compute_steady_state(st0)
+    assert bool(conv[0])
+    ns = spec.n_species
+    np.testing.assert_allclose(traj[0][1][-1][::ns], newton.cpu().numpy()[::ns], rtol=1e-4)
