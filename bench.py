@@ -721,7 +721,7 @@ def main():
 
     line = {'metric': METRIC, 'value': value, 'unit': 'states/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
-            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded GRI-3.0 states, config 2 distribution)',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded GRI-3.0 states of the workloads.gri_states distribution)',
             'config': {'workload': f'GRI-3.0 isochoric RHS + analytical Jacobian (rates option 0), {N_STATES} '
                                    f'states per GPU', 'mechanism': 'methane-gri30 (53 species, 325 reactions)',
                        'states_per_gpu': N_STATES, 'parallelism': f'replicas x{world}',

@@ -10,7 +10,6 @@
 // toward its middle block, two CTAs (factorization) or two warps (solve) per flamelet, parallel within each block.
 #include "reactor_eval.cuh"
 #include "sf_internal.h"
-#include "warp_lu.cuh"
 #include "eig_device.cuh"
 
 namespace sfgb {
