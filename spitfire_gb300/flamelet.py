@@ -654,8 +654,9 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
 
     first_time_step: a number or one per flamelet. stop_criteria: None or a callable (f, t, state_f, residual,
     steps) -> bool for flamelet f (host arrays), checked after every attempt and overridden below
-    minimum_time_step_count steps, as odesolve does (integrator.py:629-641). Returns (trajectories, stats): trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted
-    step (first and last only without save_each_step); stats: per-flamelet steps, failed_steps, newton_iters,
+    minimum_time_step_count steps, as odesolve does (integrator.py:629-641). Returns (trajectories, stats):
+    trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted step (first and last only without
+    save_each_step); stats: per-flamelet steps, failed_steps, newton_iters,
     jac_setups and status (1 stop_at_time, 3 steady, 4 step limit, 7 stop criteria)."""
     torch = _torch()
     dev = b.values.device

@@ -4,8 +4,8 @@ There is no public benchmark for this path; states are drawn as follows.
 * H2 states: h2-burke, T ~ U(800, 2500) K, p = 1 atm, Y = 0.5 Dir(0.5) over the nine named species
   (H2, O2, H2O, H, O, OH, HO2, H2O2, N2) + 0.5 e_N2, AR = HE = 0; isochoric state [rho, T, Y_0..Y_{ns-2}].
 * GRI states (the batched RHS + Jacobian workload): methane-gri30, T ~ U(600, 2800) K,
-  p = 101325 exp(U(0, ln 40)) Pa, Y = 0.7 Dir(1 over 53) + 0.3 Y_maj(phi), phi ~ U(0.5, 2), where Y_maj is the complete-combustion product of
-  CH4/air at phi (lean: CO2, H2O, N2, O2 excess; rich: CO2, CO, H2O, H2, N2 with the carbon and hydrogen deficit
+  p = 101325 exp(U(0, ln 40)) Pa, Y = 0.7 Dir(1 over 53) + 0.3 Y_maj(phi), phi ~ U(0.5, 2), where Y_maj is the
+  complete-combustion product of CH4/air at phi (lean: CO2, H2O, N2, O2 excess; rich: CO2, CO, H2O, H2, N2 with the carbon and hydrogen deficit
   split 1:1 between CO and H2); Newton factor gamma*h = exp(U(ln 1e-9, ln 1e-5)) s.
 * Ignition batch: isobaric CH4/air, T0 ~ U(900, 1500) K, phi ~ U(0.5, 2), p = 101325 exp(U(0, ln 20)).
 * Adjoint batch: isobaric CH4/air, T0 ~ U(1000, 1400) K, phi ~ U(0.7, 1.5), p = 10 atm, t_end = 5e-3 s.

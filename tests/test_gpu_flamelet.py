@@ -362,8 +362,8 @@ def test_block_thomas_short_flamelets(cuda, name):
 def test_heat_loss_integration_matches_reference_trajectory(cuda):
     """Flamelet.integrate_for_heat_loss on the GPU kernels (ESDIRK64, simple Newton, PI control, block-Thomas
     setups) against the reference's own heat-loss trajectory of the H2 flamelet of
-    tests/tabulation/nonadiabatic_defect_transient_slfm at chi_st = 1 (tests/golden/nonadiabatic_transient_slfm_gold.npz):
-    the same accepted-step count, step times and interior temperatures within 1e-7 relative, sampled mass
+    tests/tabulation/nonadiabatic_defect_transient_slfm at chi_st = 1
+    (tests/golden/nonadiabatic_transient_slfm_gold.npz): the same accepted-step count, step times and interior temperatures within 1e-7 relative, sampled mass
     fractions within 1e-5 relative (1e-9 absolute)."""
     import os
     from spitfire_gb300.flamelet import Flamelet, FlameletSpec
