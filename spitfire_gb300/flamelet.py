@@ -895,6 +895,16 @@ class Flamelet:
         torch = _torch()
         if linear_solver.lower() != 'block thomas':
             raise ValueError('only the block-Thomas linear solver is on the GPU path')
+        custom = [k for k in ('stepper_type', 'nlsolver_type', 'stepcontrol_type') if kw.get(k) is not None] + \
+            [k for k in ('extra_integrator_args', 'extra_stepper_args', 'extra_nlsolver_args',
+                         'extra_stepcontrol_args') if kw.get(k)]
+        if custom:
+            raise NotImplementedError('the GPU path integrates with the defaults of Flamelet.integrate (ESDIRK64, '
+                                      'simple Newton, PI control); not supported: ' + ', '.join(custom))
+        unknown = set(kw) - {'stepper_type', 'nlsolver_type', 'stepcontrol_type', 'extra_integrator_args',
+                             'extra_stepper_args', 'extra_nlsolver_args', 'extra_stepcontrol_args'}
+        if unknown:
+            raise TypeError('integrate() got unexpected arguments: ' + ', '.join(sorted(unknown)))
         if stop_at_time is None and stop_at_steady is None and stop_criteria is None:
             raise ValueError('integrate needs stop_at_time, stop_at_steady or stop_criteria')
         crit = None if stop_criteria is None else (lambda f, t, st, res, n: stop_criteria(t, st, res, n))

@@ -126,3 +126,22 @@ def test_integrate_batch_ragged_flamelets_match_their_own_runs():
         np.testing.assert_array_equal(both[f][0], alone[0][0])
         np.testing.assert_array_equal(both[f][1], alone[0][1])
     assert sb['steps'][0] != sb['steps'][1]
+
+
+def test_flamelet_integrate_rejects_what_the_gpu_path_does_not_implement():
+    """Flamelet.integrate fails loudly, before touching the device, for a non-default stepper, nonlinear solver,
+    step controller or extra arguments, for another linear solver, without a stop rule, and for unknown
+    arguments."""
+    import pytest
+    from spitfire_gb300.flamelet import Flamelet
+    f = Flamelet.__new__(Flamelet)
+    with pytest.raises(NotImplementedError):
+        f.integrate(stop_at_time=1., stepper_type=object)
+    with pytest.raises(NotImplementedError):
+        f.integrate(stop_at_time=1., extra_stepcontrol_args={'kp': 0.})
+    with pytest.raises(ValueError):
+        f.integrate(stop_at_time=1., linear_solver='superlu')
+    with pytest.raises(ValueError):
+        f.integrate()
+    with pytest.raises(TypeError):
+        f.integrate(stop_at_time=1., bogus=1)
