@@ -73,7 +73,8 @@ class CpuBatch:
 
     def norms(self, v):
         out = torch.zeros(self.nf, dtype=torch.float64)
-        return out.scatter_reduce(0, self.dof_flamelet, (v * self.inv_scales).abs(), reduce='amax', include_self=True)
+        return out.scatter_reduce(0, self.dof_flamelet, (v * self.inv_scales).abs(), reduce='amax',
+                                  include_self=True)
 
     def finite(self, v):
         bad = torch.zeros(self.nf, dtype=torch.float64)
@@ -111,8 +112,8 @@ def test_integrate_batch_host_logic_reproduces_reference_trajectory():
 
 
 def test_integrate_batch_ragged_flamelets_match_their_own_runs():
-    """Two flamelets of different dissipation rates (and so different step sequences) in one batch: each follows the
-    trajectory it has alone (the masks keep them independent)."""
+    """Two flamelets of different dissipation rates (and so different step sequences) in one batch: each follows
+    the trajectory it has alone (the masks keep them independent)."""
     from spitfire_gb300.flamelet import _integrate_batch
     g, spec, og, s1, Tb = _case(1.)
     _, _, _, s2, _ = _case(3.)
