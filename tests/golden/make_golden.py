@@ -28,8 +28,11 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
                        temperature, mass fractions and enthalpy defect of
                        tests/tabulation/nonadiabatic_defect_transient_slfm/gold.pkl
 
+  structure_defect_ref.npz  a seeded unstructured defect table and the reference's structured interpolation of
+                       it (tabulation.py:594-665), without and with the extended defect range
+
 Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
-                                           [transient]
+                                           [transient] [structure]
 """
 import json
 import os
@@ -411,6 +414,47 @@ def transient():
     print('nonadiabatic transient slfm gold', np.asarray(st['properties']['temperature']).shape)
 
 
+def structure():
+    """The reference's interpolation onto the structured enthalpy-defect dimension (tabulation.py:594-665), on a
+    seeded unstructured table of three dissipation rates with 4-7 ragged defects each, without and with the
+    extended defect range."""
+    ns_ref = rh_load()
+    rng = np.random.default_rng(77)
+    nz = 5
+    table = {}
+    out = {}
+    chis = [0.3, 1.7, 9.1]
+    for ci, chi in enumerate(chis):
+        ng = 4 + ci + (ci == 2)
+        gs = np.sort(-rng.uniform(0., 4.e6, ng))
+        gs[-1] = 0.
+        out['g_%d' % ci] = gs
+        for gi, g in enumerate(gs):
+            d = {'temperature': rng.uniform(300., 2200., nz), 'enthalpy': rng.uniform(-1.e6, 1.e6, nz),
+                 'enthalpy_defect': g * rng.uniform(0.5, 1.5, nz), 'mass fraction X': rng.uniform(0., 1., nz),
+                 'mixture_fraction': np.linspace(0., 1., nz)}
+            table[(chi, float(g))] = d
+            for q, v in d.items():
+                out['in_%d_%d_%s' % (ci, gi, q)] = v
+    out['chis'] = np.array(chis)
+    for ext in (False, True):
+        st, xs, gs = ns_ref.tabulation._interpolate_to_structured_defect_dimension(table, 6, extend=ext)
+        tag = 'ext' if ext else 'plain'
+        out[tag + '_x'] = xs
+        out[tag + '_g'] = gs
+        for ix, x in enumerate(xs):
+            for ig, g in enumerate(gs):
+                for q, v in st[(x, g)].items():
+                    out['%s_%d_%d_%s' % (tag, ix, ig, q)] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'structure_defect_ref.npz'), **out)
+    print('structured defect dimension', len(table), 'entries')
+
+
+def rh_load():
+    import ref_harness as rh
+    return rh.load_reference()
+
+
 def slfm_gold():
     d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'adiabatic_slfm', 'gold.pkl'), 'rb')).load()
     st = d._st
@@ -446,3 +490,5 @@ if __name__ == '__main__':
         nonadiabatic()
     if 'transient' in what:
         transient()
+    if 'structure' in what:
+        structure()
