@@ -146,3 +146,27 @@ def test_flamelet_integrate_rejects_what_the_gpu_path_does_not_implement():
         f.integrate()
     with pytest.raises(TypeError):
         f.integrate(stop_at_time=1., bogus=1)
+
+
+def test_integrate_batch_stop_at_time_active_mask_and_first_last_output():
+    """stop_at_time clips the last step onto the end time (odesolve's coerced final step), matching the oracle's
+    restatement step for step; a flamelet outside `active` is left at its initial state with no steps; without
+    save_each_step only the first and last states come back."""
+    import flamelet_transient as FT
+    from integrate import integrate
+    from spitfire_gb300.flamelet import _integrate_batch
+    g, spec, og, s1, Tb = _case(1.)
+    _, _, _, s2, _ = _case(3.)
+    ops = [_heat_op(og, s1), _heat_op(og, s2)]
+    st = [g['adiabatic_state'], g['adiabatic_state']]
+    kw = dict(stop_at_time=2.e-5, first_time_step=1.e-9, max_time_step=1.e-1, transient_tolerance=1.e-10)
+    traj, stats = _integrate_batch(CpuBatch(ops, st), active=np.array([True, False]), save_each_step=False, **kw)
+    ref = integrate(FT.FlameletTransientProblem(ops[0]), st[0], **kw)
+    assert stats['status'][0] == 1 and stats['steps'][0] == ref['steps']
+    times, states = traj[0]
+    assert times.shape == (2,) and states.shape[0] == 2
+    assert times[-1] == 2.e-5
+    np.testing.assert_allclose(states[-1], ref['state'], rtol=1e-8, atol=1e-12)  # stage sums ordered differently
+    np.testing.assert_array_equal(states[0], st[0])
+    assert stats['steps'][1] == 0 and stats['status'][1] == 0
+    np.testing.assert_array_equal(traj[1][1][-1], st[1])
