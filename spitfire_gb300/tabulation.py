@@ -21,6 +21,10 @@ each step one batched steady solve.
 defect dimension from transient heat loss instead, every burning dissipation rate's heat-loss flamelet integrated
 in time (ESDIRK64 on the GPU kernels) until its temperature profile is nearly linear, all of them in one batch.
 
+The unstrained libraries need no flamelet solve and keep the reference's interfaces as well:
+``build_unreacted_library``, ``build_adiabatic_bs_library`` and ``build_nonadiabatic_defect_bs_library``
+(tabulation.py:55-226). The equilibrium variants need Cantera's equilibrium solver and raise NotImplementedError.
+
 ``solve_steady_flamelets`` solves any number of independent flamelets (own grids, dissipation rates, initial
 profiles) at once, every solver iteration one batched launch per operation over all of them.
 """
@@ -29,7 +33,7 @@ from time import perf_counter
 
 import numpy as np
 
-from .flamelet import FlameletBatch, FlameletSetup, FlameletSpec, compute_dissipation_rate
+from .flamelet import Flamelet, FlameletBatch, FlameletSetup, FlameletSpec, compute_dissipation_rate
 from .library import Dimension, Library
 
 _mixture_fraction_name = 'mixture_fraction'
@@ -56,6 +60,78 @@ def _library_of(setup, state):
         last = last - full[:, 1 + i]
     props['mass fraction ' + names[-1]] = last
     return props
+
+
+def _as_spec(flamelet_specs, **changes):
+    fs = FlameletSpec(**flamelet_specs) if isinstance(flamelet_specs, dict) else flamelet_specs
+    return _spec_copy(fs, **changes)
+
+
+def build_unreacted_library(flamelet_specs, verbose=True):
+    """Nonreacting library over the mixture fraction (tabulation.py:55-72): the streams mixed at constant enthalpy
+    and pressure, no reaction."""
+    f = Flamelet(_as_spec(flamelet_specs, initial_condition='unreacted'))
+    return f.make_library_from_interior_state(f.initial_interior_state)
+
+
+def build_adiabatic_bs_library(flamelet_specs, verbose=True):
+    """Burke-Schumann (infinitely fast one-step combustion) library over the mixture fraction (tabulation.py:
+    96-113)."""
+    f = Flamelet(_as_spec(flamelet_specs, initial_condition='Burke-Schumann'))
+    return f.make_library_from_interior_state(f.initial_interior_state)
+
+
+def build_adiabatic_eq_library(flamelet_specs, verbose=True):
+    """tabulation.py:75-93 needs Cantera's HP equilibrium, which is not available."""
+    raise NotImplementedError('equilibrium libraries need Cantera\'s equilibrium solver, which is not available')
+
+
+def build_nonadiabatic_defect_bs_library(flamelet_specs, n_defect_st=16, verbose=True):
+    """Burke-Schumann library with a presumed triangular enthalpy defect (tabulation.py:116-187, 209-226): the
+    adiabatic profile's enthalpy lowered by g fz(Z) (fz = Z / Z_st below the stoichiometric mixture fraction,
+    (1 - Z) / (1 - Z_st) above) for n_defect_st stoichiometric defects g from 0 down to the defect of the profile
+    cooled to the linear temperature, the temperature solved from each enthalpy at fixed composition and
+    pressure. Returns a Library over (mixture_fraction, enthalpy_defect_stoich)."""
+    fs = _as_spec(flamelet_specs, initial_condition='Burke-Schumann')
+    m = fs.mech_spec
+    fuel, oxy = fs.fuel_stream, fs.oxy_stream
+    z_st = m.stoich_mixture_fraction(fuel, oxy)
+    f = Flamelet(fs)
+    ns = m.n_species
+    state_ad = f.initial_interior_state
+    ad = f.make_library_from_interior_state(state_ad)
+    h_ad = _enthalpy_of_props(m, ad)
+    z = f.mixfrac_grid
+    cooled = state_ad.copy()
+    cooled[::ns] = z[1:-1] * fuel.T + (1. - z[1:-1]) * oxy.T
+    h_ce = _enthalpy_of_props(m, f.make_library_from_interior_state(cooled))
+    defect_ext = float(np.interp(z_st, z, h_ad)) - float(np.interp(z_st, z, h_ce))
+    defects = np.linspace(-defect_ext, 0., n_defect_st)[::-1]
+    lib = Library(Dimension(_mixture_fraction_name, z), Dimension(_enthalpy_defect_name + _stoich_suffix, defects))
+    lib.extra_attributes['mech_spec'] = m
+    fz = np.where(z <= z_st, z / z_st, (1. - z) / (1. - z_st))
+    names = m.species_names
+    Y = np.stack([np.asarray(ad['mass fraction ' + n]) for n in names], axis=-1)
+    props = {q: lib.get_empty_dataset() for q in list(ad.props) + ['enthalpy_defect', 'enthalpy_cons', 'enthalpy',
+                                                                   _mixture_fraction_name]}
+    T = np.array(ad['temperature'], dtype=np.float64)
+    for ig, g in enumerate(defects):
+        h = h_ad + g * fz
+        T[1:-1] = m.temperature_from_enthalpy_vec(h[1:-1], Y[1:-1], 1500.)
+        for q in ad.props:
+            props[q][:, ig] = T if q == 'temperature' else np.asarray(ad[q])
+        props['enthalpy_defect'][:, ig] = h - h_ad
+        props['enthalpy_cons'][:, ig] = h_ad
+        props['enthalpy'][:, ig] = h
+        props[_mixture_fraction_name][:, ig] = z
+    for q, v in props.items():
+        lib[q] = v
+    return lib
+
+
+def build_nonadiabatic_defect_eq_library(flamelet_specs, n_defect_st=16, verbose=True):
+    """tabulation.py:189-206 needs Cantera's HP equilibrium, which is not available."""
+    raise NotImplementedError('equilibrium libraries need Cantera\'s equilibrium solver, which is not available')
 
 
 def solve_steady_flamelets(setups, tolerance=1.e-6):

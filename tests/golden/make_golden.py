@@ -31,8 +31,11 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
   structure_defect_ref.npz  a seeded unstructured defect table and the reference's structured interpolation of
                        it (tabulation.py:594-665), without and with the extended defect range
 
+  adiabatic_unreacted_gold.npz, adiabatic_burke_schumann_gold.npz, nonadiabatic_defect_burke_schumann_gold.npz
+                       dimensions and properties (all but viscosity) of the reference's unstrained library golds
+
 Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
-                                           [transient] [structure]
+                                           [transient] [structure] [unstrained]
 """
 import json
 import os
@@ -450,6 +453,25 @@ def structure():
     print('structured defect dimension', len(table), 'entries')
 
 
+def unstrained():
+    """Dimensions and properties of the reference's unstrained library golds (tests/tabulation/adiabatic_unreacted,
+    adiabatic_burke_schumann, nonadiabatic_defect_burke_schumann: h2-burke, air 1200 K / H2 300 K, 34 points),
+    all but viscosity."""
+    for name in ('adiabatic_unreacted', 'adiabatic_burke_schumann', 'nonadiabatic_defect_burke_schumann'):
+        d = _U(open(os.path.join(REF, 'tests', 'tabulation', name, 'gold.pkl'), 'rb')).load()
+        st = d._st
+        arrs = {}
+        for i in range(len(st['dim_ordering'])):
+            n = st['dim_ordering'][i]
+            arrs['dim%d_name' % i] = np.array(n)
+            arrs['dim%d_values' % i] = np.asarray(st['dimensions'][n]['values'])
+        for k, v in st['properties'].items():
+            if k != 'viscosity':
+                arrs['prop:' + k] = np.asarray(v)
+        np.savez_compressed(os.path.join(HERE, name + '_gold.npz'), **arrs)
+        print(name, sorted(k for k in arrs if not k.startswith('prop:mass'))[:12])
+
+
 def rh_load():
     import ref_harness as rh
     return rh.load_reference()
@@ -492,3 +514,5 @@ if __name__ == '__main__':
         transient()
     if 'structure' in what:
         structure()
+    if 'unstrained' in what:
+        unstrained()
