@@ -790,3 +790,24 @@ class ChemicalMechanismSpec:
     def stoich_mixture_fraction(self, fuel_stream, oxy_stream):
         eta = self.stoich_mass_fuel_to_oxy_ratio(fuel_stream, oxy_stream)
         return eta / (1. + eta)
+
+    def mix_fuels_for_stoich_mixture_fraction(self, fuel1, fuel2, zstoich, oxy):
+        """Mole-basis mix of two fuel streams whose stoichiometric mixture fraction with `oxy` is zstoich
+        (mechanism.py:724-757), e.g. a fuel diluted with nitrogen; hydrocarbon oxidation (C -> CO2, H -> H2O).
+
+        With k moles of fuel1 and 1 - k of fuel2, the oxygen atoms the fuel needs per mole are k n1 + (1 - k) n2
+        (n = 2 C + H/2 - O), the oxidizer brings e = O - H/2 - 2 C per mole, and the stoichiometric fuel-to-oxidizer
+        mass ratio zstoich / (1 - zstoich) equals (k M1 + (1 - k) M2) e / (M_oxy (k n1 + (1 - k) n2)); that is
+        linear in k. Raises ValueError when no k in [0, 1] reaches zstoich."""
+        names = ['H', 'O', 'C']
+        a = self._get_atoms_in_stream(fuel1, names)
+        b = self._get_atoms_in_stream(fuel2, names)
+        x = self._get_atoms_in_stream(oxy, names)
+        need = lambda c: 2. * c['C'] + 0.5 * c['H'] - c['O']
+        n1, n2, e = need(a), need(b), -need(x)
+        m1, m2, mx = fuel1.mean_molecular_weight, fuel2.mean_molecular_weight, oxy.mean_molecular_weight
+        lhs = mx / e * zstoich / (1. - zstoich)  # fuel molar mass per unit oxygen demand at stoichiometry
+        k = (m2 - lhs * n2) / (lhs * (n1 - n2) - (m1 - m2))
+        if not 0. <= k <= 1.:
+            raise ValueError('The provided fuel combination cannot reach the desired stoichiometric mixture fraction!')
+        return self.mix_streams([(fuel1, k), (fuel2, 1. - k)], 'mole')
