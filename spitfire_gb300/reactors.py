@@ -281,6 +281,18 @@ def _surface_to_volume(shape_dimension_dict):
     return float(l2s(d['char. length'])) if 'char. length' in d else float(v2s(d['volume']))
 
 
+def _join_trajectories(lib1, lib2, first_and_last_only=False):
+    """One Library over 'time' from two consecutive trajectories; the second starts at the first one's last
+    state, which is kept once."""
+    from .library import Dimension, Library
+    t = np.concatenate([lib1.dim('time').values, lib2.dim('time').values[1:]])
+    pick = np.array([0, t.size - 1]) if first_and_last_only else np.arange(t.size)
+    out = Library(Dimension('time', t[pick]))
+    for q in lib1.props:
+        out[q] = np.concatenate([np.asarray(lib1[q]), np.asarray(lib2[q])[1:]])[pick]
+    return out
+
+
 class HomogeneousReactor:
     """Drop-in for spitfire.chemistry.reactors.HomogeneousReactor (reactors.py:27-794): closed or open (mass
     exchange with a feed), adiabatic, isothermal or diathermal, isobaric or isochoric. Time-dependent parameters are
@@ -365,6 +377,16 @@ class HomogeneousReactor:
         return self._initial_pressure
 
     @property
+    def current_pressure(self):
+        """reactors.py:391-394: an isobaric reactor's constant pressure; for an isochoric one the ideal-gas pressure
+        rho R T / M of the current state (the reference evaluates rho T M there, without the gas constant)."""
+        if self._configuration == 'isobaric' or self._integrations == 0:
+            return self._initial_pressure
+        rho, T = self._current_state[0], self._current_state[1]
+        Y = self.current_mass_fractions
+        return float(rho * 8314.46261815324 * T * np.sum(Y / np.asarray(self._mechanism.molecular_weights)))
+
+    @property
     def initial_mass_fractions(self):
         return self._initial_mass_fractions.copy()
 
@@ -376,6 +398,10 @@ class HomogeneousReactor:
     @property
     def n_species(self):
         return self._mechanism.n_species
+
+    @property
+    def n_reactions(self):
+        return self._mechanism.n_reactions
 
     @property
     def n_equations(self):
@@ -457,6 +483,43 @@ class HomogeneousReactor:
 
     def integrate_to_time(self, final_time, **kwargs):
         return self.integrate(stop_at_time=final_time, **kwargs)
+
+    def integrate_to_steady_after_ignition(self, steady_tolerance=1.e-4, delta_temperature_ignition=400., **kwargs):
+        """Integrate until the reactor has ignited (T > T0 + delta_temperature_ignition) and the step residual is
+        below steady_tolerance (reactors.py:711-743), for slowly evolving mixtures whose first residuals are already
+        small. The reference runs one integration with that stop criterion. Here it is two integrations of the GPU
+        integrator: to ignition (its ignition stop rule, with no give-up on small residuals), then on to a steady
+        state from there, starting from the last accepted step size and completing the minimum step count. The
+        restart re-evaluates the Jacobian and restarts the step-size control at ignition, so the steps after
+        ignition are not the reference's; both runs end at the same steady state within steady_tolerance.
+        Returns the joined trajectory (first and last states only with save_first_and_last_only)."""
+        if self._heat_transfer == 'isothermal':
+            raise ValueError('integrate_to_steady_after_ignition() called on an isothermal reactor! This is not '
+                             'currently supported!')
+        if kwargs.get('stop_criteria') is not None or kwargs.get('stop_at_steady') is not None:
+            raise ValueError('integrate_to_steady_after_ignition() sets its own stop rules')
+        save_fl = kwargs.pop('save_first_and_last_only', False)
+        min_steps = kwargs.get('minimum_time_step_count', 40)
+        stop_at_time = kwargs.get('stop_at_time')
+        lib1 = self._integrate(save_first_and_last_only=False, delta_temperature_ignition=delta_temperature_ignition,
+                               minimum_allowable_residual=0.,
+                               first_time_step=kwargs.get('first_time_step', 1.e-6),
+                               max_time_step=kwargs.get('max_time_step', 1.e6),
+                               minimum_time_step_count=min_steps,
+                               transient_tolerance=kwargs.get('transient_tolerance', 1.e-10),
+                               nonlinear_tolerance=kwargs.get('nonlinear_solve_tolerance', 1.e-12),
+                               maximum_steps_per_jacobian=kwargs.get('maximum_steps_per_jacobian', 1),
+                               stop_at_time=None if stop_at_time is None else stop_at_time - self._current_time)
+        t1 = lib1.dim('time').values
+        if stop_at_time is not None and self._current_time >= stop_at_time:
+            return _join_trajectories(lib1, lib1[-1:], save_fl)
+        steps1 = t1.size - 1
+        rest = dict(kwargs)
+        rest['minimum_time_step_count'] = max(0, min_steps - steps1)
+        if t1.size > 1:
+            rest['first_time_step'] = float(t1[-1] - t1[-2])
+        lib2 = self.integrate(stop_at_steady=steady_tolerance, **rest)
+        return _join_trajectories(lib1, lib2, save_fl)
 
     def compute_ignition_delay(self, delta_temperature_ignition=400., minimum_allowable_residual=1.e-12,
                                return_solution=False, **kwargs):
