@@ -76,3 +76,44 @@ def test_reactor_steady_after_ignition_composition(monkeypatch):
     calls.clear()
     fl = r.integrate_to_steady_after_ignition(save_first_and_last_only=True)
     np.testing.assert_array_equal(fl.dim('time').values, [0., 3e-5])
+
+
+def test_reactor_front_end_accepts_every_configuration():
+    """Every combination the reference's reactor coverage test builds (tests/reactor/test_reactor_coverage.py:
+    isobaric and isochoric, closed and open with a feed, adiabatic, isothermal and diathermal over every supported
+    shape) constructs on the host with the reference's argument names; an unknown shape or a diathermal reactor
+    without its coefficients is rejected."""
+    from spitfire_gb300.reactors import HomogeneousReactor
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    fuel = m.stream('X', 'H2:1')
+    mix = m.mix_for_equivalence_ratio(1.0, fuel, air)
+    mix.TP = 1200., 101325.
+    feed = m.copy_stream(mix)
+    n = 0
+    for configuration in ('isobaric', 'isochoric'):
+        for mass_transfer in ('closed', 'open'):
+            for heat_transfer in ('adiabatic', 'isothermal', 'diathermal'):
+                shapes = list(HomogeneousReactor.get_supported_reactor_shapes()) if heat_transfer == 'diathermal' \
+                    else [None]
+                for shape in shapes:
+                    kw = {}
+                    if mass_transfer == 'open':
+                        kw.update(feed_temperature=feed.T, feed_mass_fractions=feed.Y, mixing_tau=1.e-3)
+                        if configuration == 'isochoric':
+                            kw['feed_density'] = feed.density
+                    if heat_transfer == 'diathermal':
+                        kw.update(convection_coefficient=1., convection_temperature=300., radiative_emissivity=1.,
+                                  radiation_temperature=300.,
+                                  shape_dimension_dict={'shape': shape, 'char. length': 1.e-3})
+                    r = HomogeneousReactor(m, mix, configuration=configuration, heat_transfer=heat_transfer,
+                                           mass_transfer=mass_transfer, **kw)
+                    assert r.n_equations == m.n_species + (1 if configuration == 'isochoric' else 0)
+                    n += 1
+    assert n > 12
+    with pytest.raises(Exception):
+        HomogeneousReactor(m, mix, 'isobaric', 'diathermal', 'closed', convection_coefficient=1.,
+                           convection_temperature=300., radiative_emissivity=1., radiation_temperature=300.,
+                           shape_dimension_dict={'shape': 'dodecahedron-ish', 'char. length': 1.e-3})
+    with pytest.raises(Exception):
+        HomogeneousReactor(m, mix, 'isobaric', 'diathermal', 'closed')
