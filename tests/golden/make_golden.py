@@ -24,7 +24,8 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
                        tests/tabulation/nonadiabatic_defect_steady_slfm/gold.pkl
 
   nonadiabatic_transient_slfm_gold.npz  the reference's transient heat-loss trajectory of one H2 flamelet
-                       (times, temperatures, sampled mass fractions, heat-loss parameters) and the dimensions,
+                       (times, temperatures, sampled mass fractions, heat-loss parameters), its adiabatic
+                       ignition transient from the linear profile to t = 2 ms, and the dimensions,
                        temperature, mass fractions and enthalpy defect of
                        tests/tabulation/nonadiabatic_defect_transient_slfm/gold.pkl
 
@@ -403,6 +404,13 @@ def transient():
                T_conv=np.asarray(f1._T_conv), h_conv=np.asarray(f1._h_conv), T_rad=np.asarray(f1._T_rad),
                h_rad=np.asarray(f1._h_rad))
     print('transient heat loss: steps', t.size - 1, 'final max T', T[-1].max())
+    # an adiabatic flamelet igniting from the linear T/Y profile (the hot air side ignites the mixing layer)
+    f2 = Fl(FSpec(initial_condition='linear-TY', stoich_dissipation_rate=1., **base))
+    lib2 = f2.integrate_to_time(2.e-3, first_time_step=1.e-6, transient_tolerance=1.e-10, write_log=False)
+    out['ign_ic'] = np.asarray(f2._initial_state)
+    out['ign_times'] = np.asarray(lib2.dim('time').values)
+    out['ign_T'] = np.asarray(lib2['temperature'])
+    print('adiabatic ignition transient: steps', out['ign_times'].size - 1, 'final max T', out['ign_T'][-1].max())
     d = _U(open(os.path.join(REF, 'tests', 'tabulation', 'nonadiabatic_defect_transient_slfm', 'gold.pkl'),
                 'rb')).load()
     st = d._st

@@ -448,3 +448,27 @@ def test_integrate_to_steady_matches_oracle_and_newton(cuda, name):
     assert bool(conv[0])
     ns = spec.n_species
     np.testing.assert_allclose(traj[0][1][-1][::ns], newton.cpu().numpy()[::ns], rtol=1e-4)
+
+
+def test_adiabatic_ignition_transient_matches_reference(cuda):
+    """Flamelet.integrate_to_time on the GPU kernels for an adiabatic H2 flamelet igniting from the linear T/Y
+    profile (air 1200 K / H2 300 K, 34 points, chi_st = 1) to t = 2 ms, against the reference's own run
+    (tests/golden/nonadiabatic_transient_slfm_gold.npz, 1216 accepted steps): the step count within three (over
+    a thousand step-size decisions, rounding may move one), and the temperatures at the end time within 1e-6
+    relative."""
+    import os
+    from spitfire_gb300.flamelet import Flamelet, FlameletSpec
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    g = np.load(os.path.join(FC.GOLD, 'nonadiabatic_transient_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    f = Flamelet(FlameletSpec(mech_spec=m, oxy_stream=air, fuel_stream=fuel, grid_points=34,
+                              initial_condition='linear-TY', stoich_dissipation_rate=1.))
+    lib = f.integrate_to_time(2.e-3, first_time_step=1.e-6, transient_tolerance=1.e-10)
+    t = lib.dim('time').values
+    assert abs(t.size - g['ign_times'].size) <= 3
+    assert t[-1] == 2.e-3
+    np.testing.assert_allclose(lib['temperature'][-1], g['ign_T'][-1], rtol=1e-6)
+    assert m.griffon.device_status() == 0

@@ -110,3 +110,26 @@ def test_oracle_transient_defect_library_matches_reference_gold():
     keys = [k for k in g.files if k.startswith('prop:')]
     for k in keys:
         np.testing.assert_allclose(props[k[5:]], g[k], rtol=2e-4, atol=1e-4, err_msg=k)
+
+
+def test_oracle_adiabatic_ignition_transient_matches_reference():
+    """An adiabatic H2 flamelet (same streams and grid) igniting from the linear T/Y profile, integrated to
+    t = 2 ms by the reference's Flamelet.integrate_to_time (first step 1e-6, tolerance 1e-10): the oracle takes
+    the same accepted steps, with step times and temperatures within 1e-7 relative."""
+    import flamelet_steady as FS
+    import flamelet_transient as FT
+    from integrate import integrate
+    from spitfire_gb300.flamelet import FlameletSetup, FlameletSpec
+    g = np.load(GOLD)
+    spec, og = pair('h2-burke')
+    air, fuel = _streams(spec)
+    s = FlameletSetup(FlameletSpec(mech_spec=spec, oxy_stream=air, fuel_stream=fuel, grid_points=34,
+                                   initial_condition='linear-TY', stoich_dissipation_rate=1.))
+    np.testing.assert_allclose(s.initial_state, g['ign_ic'], rtol=1e-14)
+    op = FS.FlameletOperator(og, s.z, s.x, s.state_oxy, s.state_fuel)
+    r = integrate(FT.FlameletTransientProblem(op), s.initial_state, stop_at_time=2.e-3, first_time_step=1.e-6,
+                  max_time_step=1.e-3, transient_tolerance=1.e-10, maximum_steps_per_jacobian=10,
+                  save_each_step=True)
+    assert r['steps'] == g['ign_times'].size - 1
+    np.testing.assert_allclose(r['times'], g['ign_times'], rtol=1e-7)
+    np.testing.assert_allclose(r['states'][:, ::spec.n_species], g['ign_T'][:, 1:-1], rtol=1e-7)
