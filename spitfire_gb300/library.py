@@ -23,6 +23,24 @@ import shutil
 import numpy as np
 
 
+class _ReferenceUnpickler(pickle.Unpickler):
+    """Unpickler that reads files written by the reference package: spitfire.chemistry.library.{Library, Dimension}
+    and spitfire.chemistry.mechanism.ChemicalMechanismSpec become this package's classes, and numpy's pre-2.0
+    module path numpy.core is read as numpy._core where that exists."""
+
+    _MAP = {('spitfire.chemistry.library', 'Library'): ('spitfire_gb300.library', 'Library'),
+            ('spitfire.chemistry.library', 'Dimension'): ('spitfire_gb300.library', 'Dimension'),
+            ('spitfire.chemistry.library', 'LibraryIndexError'): ('spitfire_gb300.library', 'LibraryIndexError'),
+            ('spitfire.chemistry.mechanism', 'ChemicalMechanismSpec'): ('spitfire_gb300.mechanism',
+                                                                       'ChemicalMechanismSpec')}
+
+    def find_class(self, module, name):
+        module, name = self._MAP.get((module, name), (module, name))
+        if module.startswith('numpy.core') and hasattr(np, '_core'):
+            module = 'numpy._core' + module[len('numpy.core'):]
+        return super().find_class(module, name)
+
+
 class Dimension:
     """A named, one-dimensional grid of unique values (library.py:21-89)."""
 
@@ -284,8 +302,15 @@ class Library:
 
     @classmethod
     def load_from_file(cls, file_name):
+        """Load a library saved by save_to_file, or one the reference wrote: its save_to_file pickles the
+        spitfire.chemistry.library.Library object itself (library.py:180-183), with the mechanism's
+        ChemicalMechanismSpec among the extra attributes, and its version-1.0 files pickle the plain dictionary
+        (library.py:246-256). Reference classes are mapped onto this package's Library, Dimension and
+        ChemicalMechanismSpec, whose __setstate__ read the same dictionaries."""
         with open(file_name, 'rb') as f:
-            st = pickle.load(f)
+            st = _ReferenceUnpickler(f).load()
+        if isinstance(st, Library):
+            return st
         lib = cls.__new__(cls)
         lib.__setstate__(st)
         return lib

@@ -35,8 +35,17 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
   adiabatic_unreacted_gold.npz, adiabatic_burke_schumann_gold.npz, nonadiabatic_defect_burke_schumann_gold.npz
                        dimensions and properties (all but viscosity) of the reference's unstrained library golds
 
+  dropin_ref.npz       the reference's single-state PyCombustionKernels methods called directly: every thermo getter
+                       at temperatures inside and outside the NASA7 ranges, flamelet_stencils, flamelet_jac_indices,
+                       flamelet_rhs and flamelet_jacobian (adiabatic and nonadiabatic, each flag combination its
+                       callers use, rates options 0/1/2) on the flamelet cases, and the ten module-level
+                       py_btddod_* functions on seeded block-diagonally dominant matrices of several sizes
+
+  reference_<name>_gold.pkl  byte copies of the reference's pickled gold libraries
+                       (tests/tabulation/<name>/gold.pkl): the reader of reference-written libraries is tested on them
+
 Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
-                                           [transient] [structure] [unstrained]
+                                           [transient] [structure] [unstrained] [dropin] [libraries]
 """
 import json
 import os
@@ -503,6 +512,154 @@ def slfm_gold():
     print('slfm gold', order, [a.shape for a in arrs.values()][:4])
 
 
+def dropin():
+    import ref_harness as rh
+    from flamelet_cases import FLAMELET_CASES, flamelet_case_setup
+    from spitfire_gb300.flamelet import burke_schumann_state, clustered_grid
+    ns_ref = rh.load_reference()
+    G = ns_ref.griffon
+    out = {}
+    for case in FLAMELET_CASES:
+        name, fname, phase = case[:3]
+        ref = rh.ReferenceMechanism(os.path.join(MECHS, fname), phase)
+        g = ref.griffon
+        ns = ref.n_species
+        pre = name + '_'
+        # thermodynamics, in and outside [Tmin, Tmax] of the NASA7 fits
+        rng = np.random.default_rng(77 + ns)
+        Ts = np.array([200., 300., 999., 1000., 1500., 2999., 3500., 6000.])
+        Y = rng.dirichlet(0.5 * np.ones(ns), Ts.size)
+        p = 101325. * np.exp(rng.uniform(0., np.log(40.), Ts.size))
+        th = {k: [] for k in ('mmw', 'x', 'rho', 'p', 'cp', 'cv', 'h', 'e', 'cpi', 'cvi', 'hi', 'ei', 'dcpdT')}
+        for T, y, pp in zip(Ts, Y, p):
+            v = np.zeros(ns)
+            th['mmw'].append(g.mixture_molecular_weight(y))
+            g.mole_fractions(y, v)
+            th['x'].append(v.copy())
+            rho = g.ideal_gas_density(pp, T, y)
+            th['rho'].append(rho)
+            th['p'].append(g.ideal_gas_pressure(rho, T, y))
+            th['cp'].append(g.cp_mix(T, y))
+            th['cv'].append(g.cv_mix(T, y))
+            th['h'].append(g.enthalpy_mix(T, y))
+            th['e'].append(g.energy_mix(T, y))
+            for k, f in (('cpi', g.species_cp), ('cvi', g.species_cv), ('hi', g.species_enthalpies),
+                         ('ei', g.species_energies)):
+                f(T, v)
+                th[k].append(v.copy())
+            g.dcpdT_species(T, y, v)
+            th['dcpdT'].append(v.copy())
+        out[pre + 'thermo_T'] = Ts
+        out[pre + 'thermo_Y'] = Y
+        out[pre + 'thermo_p'] = p
+        for k, v in th.items():
+            out[pre + 'thermo_' + k] = np.array(v)
+        # flamelet methods with the argument lists of the reference's Flamelet closures (flamelet.py:623-915)
+        oxy, fuel, kw = flamelet_case_setup(spec := ref.spec, case)
+        zst = spec.stoich_mixture_fraction(fuel, oxy)
+        z, _ = clustered_grid(kw['grid_points'], zst, 4.)
+        ic = burke_schumann_state(spec, oxy, fuel, z, 101325.)
+        F = ns_ref.flamelet.Flamelet(ns_ref.flamelet.FlameletSpec(mech_spec=ref, initial_condition=ic, **kw))
+        nzi = F._nz_interior
+        st = np.abs(ic * (1. + 0.02 * rng.standard_normal(ic.size)))
+        dz, chi, invle = F._dz, F._x, 1. / F._lewis_numbers
+        cma, csb, csp = np.zeros(nzi * ns), np.zeros(nzi * ns), np.zeros(nzi * ns)
+        mc, nc = np.zeros(nzi), np.zeros(nzi)
+        g.flamelet_stencils(dz, nzi, chi, invle, cma, csb, csp, mc, nc)
+        nel = ns * (nzi * ns + 2 * (nzi - 1))
+        rows, cols = np.zeros(nel, dtype=np.int32), np.zeros(nel, dtype=np.int32)
+        g.flamelet_jac_indices(nzi, rows, cols)
+        for k, v in (('dz', dz), ('chi', chi), ('invle', invle), ('cmajor', cma), ('csub', csb), ('csup', csp),
+                     ('mcoeff', mc), ('ncoeff', nc), ('rows', rows), ('cols', cols), ('state', st),
+                     ('oxy', F._state_oxy), ('fuel', F._state_fuel)):
+            out[pre + 'flm_' + k] = v
+        Tc = 300. + 1500. * rng.uniform(size=nzi)
+        Tr = 300. + 1500. * rng.uniform(size=nzi)
+        hc = 1.e5 * rng.uniform(size=nzi)
+        hr = rng.uniform(size=nzi)
+        for k, v in (('Tc', Tc), ('Tr', Tr), ('hc', hc), ('hr', hr)):
+            out[pre + 'flm_' + k] = v
+        null = np.zeros(1)
+        heat = {'ad': (True, null, null, null, null, False), 'na': (False, Tc, Tr, hc, hr, False),
+                'ns': (False, Tc, Tr, hc / 1.e3, hr, True)}
+        for hk, (adb, a1, a2, a3, a4, scaled) in heat.items():
+            for ef in (0, 1):
+                for vc in (0, 1):
+                    r = np.zeros(nzi * ns)
+                    g.flamelet_rhs(st, F._pressure, F._state_oxy, F._state_fuel, adb, a1, a2, a3, a4, nzi, cma, csb,
+                                   csp, mc, nc, chi, bool(ef), bool(vc), scaled, r)
+                    out[pre + f'flm_rhs_{hk}_e{ef}v{vc}'] = r
+        diffterm = 4. * F._max_dissipation_rate
+        jac_cases = {'plain_r0': ('ad', False, 0., False, 0., 0, True), 'plain_r1': ('ad', False, 0., False, 0., 1, True),
+                     'plain_r2': ('ad', False, 0., False, 0., 2, True), 'plain_e0': ('ad', False, 0., False, 0., 0, False),
+                     'scaled': ('ad', False, 0., True, 1.e-3, 0, True), 'eig': ('ad', True, diffterm, False, 0., 0, True),
+                     'eig_scaled': ('ad', True, diffterm, True, 1.e-3, 0, True),
+                     'na': ('na', False, 0., False, 0., 0, True), 'ns': ('ns', False, 0., False, 0., 0, True)}
+        if ns > 20:  # the larger mechanism: a subset, to keep the fixture small
+            jac_cases = {k: jac_cases[k] for k in ('plain_r1', 'eig_scaled', 'ns')}
+        for jk, (hk, eig, dt, sc, pf, ropt, ef) in jac_cases.items():
+            adb, a1, a2, a3, a4, scaled = heat[hk]
+            v = np.zeros(nel)
+            e = np.zeros(nzi * ns)
+            g.flamelet_jacobian(st, F._pressure, F._state_oxy, F._state_fuel, adb, a1, a2, a3, a4, nzi, cma, csb, csp,
+                                mc, nc, chi, eig, dt, sc, pf, ropt, 0, ef, True, scaled, e, v)
+            out[pre + f'flm_jac_{jk}'] = v
+            if eig:
+                out[pre + f'flm_expeig_{jk}'] = e
+        out[pre + 'flm_diffterm'] = np.array(diffterm)
+        print('dropin', name, 'nzi', nzi)
+    # module-level block algebra on seeded block-diagonally dominant BTDDOD matrices
+    for nb, bs in ((7, 5), (3, 53), (1, 3), (2, 11)):
+        rng = np.random.default_rng(1000 * nb + bs)
+        nv = bs * (nb * bs + 2 * (nb - 1))
+        A = rng.standard_normal(nv)
+        for i in range(nb):
+            A[i * bs * bs: (i + 1) * bs * bs: bs + 1] += 3. * bs
+        x = rng.standard_normal(nb * bs)
+        pre = f'bt{nb}x{bs}_'
+        out[pre + 'A'] = A
+        out[pre + 'x'] = x
+        y = np.zeros(nb * bs)
+        if nb > 1:  # with one block the reference adds both end couplings from outside its arrays
+            G.py_btddod_full_matvec(A, x, nb, bs, y)
+            out[pre + 'full_matvec'] = y.copy()
+        G.py_btddod_blockdiag_matvec(A, x, nb, bs, y)
+        out[pre + 'blockdiag_matvec'] = y.copy()
+        piv = np.zeros(nb * bs, dtype=np.int32)
+        fac = np.zeros(nb * bs * bs)
+        G.py_btddod_blockdiag_factorize(A, nb, bs, piv, fac)
+        G.py_btddod_blockdiag_solve(piv, fac, x, nb, bs, y)
+        out[pre + 'blockdiag_solve'] = y.copy()
+        G.py_btddod_lowerfulltriangle_solve(piv, fac, A, x, nb, bs, y)
+        out[pre + 'lower_solve'] = y.copy()
+        G.py_btddod_upperfulltriangle_solve(piv, fac, A, x, nb, bs, y)
+        out[pre + 'upper_solve'] = y.copy()
+        Af = A.copy()
+        lv = np.zeros(nb * bs * bs)
+        pv = np.zeros(nv, dtype=np.int32)
+        G.py_btddod_full_factorize(Af, nb, bs, lv, pv)
+        G.py_btddod_full_solve(Af, lv, pv, x, nb, bs, y)
+        out[pre + 'full_solve'] = y.copy()
+        B = rng.standard_normal(nb * bs * bs)
+        out[pre + 'B'] = B
+        As = A.copy()
+        G.py_btddod_scale_and_add_scaled_block_diagonal(As, 0.7, B, -1.3, nb, bs)
+        out[pre + 'scaled_block'] = As
+        d = rng.standard_normal(nb * bs)
+        out[pre + 'd'] = d
+        As = A.copy()
+        G.py_btddod_scale_and_add_diagonal(As, -1., d, 2.5, nb, bs)
+        out[pre + 'scaled_diag'] = As
+    np.savez_compressed(os.path.join(HERE, 'dropin_ref.npz'), **out)
+
+
+def libraries():
+    import shutil
+    for name in ('adiabatic_slfm', 'nonadiabatic_defect_burke_schumann'):
+        shutil.copyfile(os.path.join(REF, 'tests', 'tabulation', name, 'gold.pkl'),
+                        os.path.join(HERE, f'reference_{name}_gold.pkl'))
+
+
 if __name__ == '__main__':
     what = sys.argv[1:] or ['kernels', 'ignition', 'gold', 'flamelets']
     if 'flamelets' in what:
@@ -524,3 +681,7 @@ if __name__ == '__main__':
         structure()
     if 'unstrained' in what:
         unstrained()
+    if 'dropin' in what:
+        dropin()
+    if 'libraries' in what:
+        libraries()
