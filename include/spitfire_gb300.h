@@ -121,8 +121,8 @@ int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *cou
 /* Launch shapes of the kernels that use a mechanism, as chosen by an autotuner (spitfire_gb300/autotune.py times
  * the candidates on the device). 0 restores the built-in choice. Knobs and values:
  *   SF_TUNE_GROUP_{RATES,SENS,RHS,JAC}: lanes per state of the batched kernels, 8, 16 or 32, or 1 for the
- *     thread-per-state kernels (each lane one state, scratch interleaved across the warp in a device buffer the
- *     mechanism allocates when the knob is set);
+ *     thread-per-state kernels (each lane one state, scratch interleaved across the warp in the caller's
+ *     workspace, whose size sf_chem_workspace_size reports; no knob allocates anything);
  *   SF_TUNE_INTEGRATE_WARPS: warps (reactors) per block of sf_integrate_batch, 1..8 (0: as many as fit);
  *   SF_TUNE_INTEGRATE_SCRATCH: 1 keeps each integrating warp's Griffon scratch in global memory (L2-resident)
  *     instead of shared memory, so that more warps fit per SM; 2 also its iteration matrix and FP32 factors
@@ -130,7 +130,9 @@ int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *cou
  *   SF_TUNE_TPS_CTAS: resident 4-warp blocks per SM of the thread-per-state kernels, 1..16 (0: as many as fit);
  *     fewer keep more of their interleaved scratch in L2.
  * The integrator knobs do not change results; the lane-group width changes the order of per-species sums, so those
- * results agree to rounding. No reference counterpart. */
+ * results agree to rounding. No reference counterpart.
+ * Concurrency: a mechanism holds no scratch, so calls on one sf_mech may run on several streams at once, each with
+ * its own workspace. Set knobs while no call that uses the mechanism is being issued. */
 enum sf_tune_knob {
   SF_TUNE_GROUP_RATES = 0, SF_TUNE_GROUP_SENS = 1, SF_TUNE_GROUP_RHS = 2, SF_TUNE_GROUP_JAC = 3,
   SF_TUNE_INTEGRATE_WARPS = 4, SF_TUNE_INTEGRATE_SCRATCH = 5, SF_TUNE_TPS_CTAS = 6, SF_TUNE_KNOBS = 7
@@ -150,17 +152,25 @@ int sf_thermo_batch(const sf_mech *mech, int what, int n, const double *T, const
                     void *stream);
 
 /* --------------------------------------------------------------------------------------------------- kinetics */
+/* Device workspace of the batched chemistry calls below, in bytes, for n states: the thread-per-state kernels
+ * (lanes-per-state knob 1) interleave each warp's per-state scratch in it, at most one slot per warp that can be
+ * resident (GRI-3.0 Jacobians: about 1.2 GB for a full device); the lane-group kernels keep their scratch in shared
+ * memory and need none (0; the workspace pointer may then be NULL). The size depends on the mechanism's current
+ * knobs: query it after tuning. One workspace must not be used by two calls that run at the same time. */
+enum sf_chem_kind { SF_CHEM_RATES = 0, SF_CHEM_SENS = 1, SF_CHEM_RHS = 2, SF_CHEM_JAC = 3 };
+size_t sf_chem_workspace_size(const sf_mech *mech, int kind, int n);
+
 /* Production rates w[n][ns] (kg/m^3/s) at (T, rho, Y).
  * Replaces PyCombustionKernels.production_rates (griffon.pyx:763-768 -> chemistry_kernels.cpp:29-33). Note the
  * Cython wrapper passes its first positional argument as T; this entry point names T and rho explicitly. */
 int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const double *rho, const double *Y,
-                              double *out_w, void *stream);
+                              double *out_w, void *workspace, size_t workspace_bytes, void *stream);
 
 /* Production rates and their sensitivities to (rho, T, Y_0..Y_{ns-2}), out_sens[n][(ns+1)^2].
  * option: 0 exact dense, 2 exact sparse (identical values), 1 no third-body/falloff sensitivities.
  * Replaces prod_rates_primitive_sensitivities (griffon.pyx:773-783 -> chemistry_kernels.cpp:464-483). */
 int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const double *T, const double *Y, int option,
-                        double *out_w, double *out_sens, void *stream);
+                        double *out_w, double *out_sens, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------------------------ reactor kernels */
 /* Reactor parameters shared by every state of one batched call (the scalar arguments of
@@ -187,7 +197,9 @@ typedef struct sf_reactor_params {
  * the thread-per-state kernel's resident warps when the autotuner selected it, else half the batch), and each
  * chunk's results copied back on a second stream while the next chunk computes. `stream` is ordered after the last
  * copy. Pinned host buffers let the copies run asynchronously. workspace: DEVICE, at least
- * sf_reactor_jac_host_workspace_size bytes. */
+ * sf_reactor_jac_host_workspace_size bytes (device copies of inputs and outputs plus the kernel's workspace).
+ * Calls on one mechanism from several host threads take turns while they issue their work; their copies back share
+ * the mechanism's copy stream. */
 size_t sf_reactor_jac_host_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n);
 int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *params, int rates_option, int n,
                               const double *q_host, const double *pressures_host, double *out_rhs_host,
@@ -199,13 +211,16 @@ int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *para
  * Replaces reactor_rhs_isobaric / reactor_rhs_isochoric (isobaric_reactor_kernels.cpp:170-219,
  * isochoric_reactor_kernels.cpp:184-242). */
 int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *params, int n, const double *q,
-                         const double *pressures, double *out_rhs, void *stream);
+                         const double *pressures, double *out_rhs, void *workspace, size_t workspace_bytes,
+                         void *stream);
 
 /* Right-hand side and analytical Jacobian (column-major neq x neq per state). rates_option as in
  * sf_rates_sens_batch. Replaces reactor_jac_isobaric / reactor_jac_isochoric (isobaric_reactor_kernels.cpp:221-343,
- * isochoric_reactor_kernels.cpp:244-333). */
+ * isochoric_reactor_kernels.cpp:244-333). workspace: sf_chem_workspace_size(mech, SF_CHEM_JAC, n) bytes, as for
+ * the rates calls. */
 int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *params, int rates_option, int n,
-                         const double *q, const double *pressures, double *out_rhs, double *out_jac, void *stream);
+                         const double *q, const double *pressures, double *out_rhs, double *out_jac, void *workspace,
+                         size_t workspace_bytes, void *stream);
 
 /* The same evaluation in the plain single-state GPU form: one thread per state, the mechanism read from global
  * memory, Griffon's per-reaction dense scatter into a per-state scratch Jacobian. It exists as the comparison
@@ -230,7 +245,8 @@ int sf_reactor_jac_plain_batch(const sf_mech *mech, const sf_reactor_params *par
  * 8000 h2-burke states) are rejected with SF_ERR_WORKSPACE and a message giving the limit. All calls on a device
  * share the array: two calls that run at the same time on the GPU (e.g. on different streams) overwrite each
  * other's scratch and give wrong results; serialize them. Each call rewrites all scratch it reads, so contents
- * left by an earlier call do no harm. */
+ * left by an earlier call do no harm. The looked-up address is kept for the life of the process: after a
+ * cudaDeviceReset of that device, which unloads this library's device code, do not call this entry point again. */
 int sf_reactor_jac_plain_batch_static(const sf_mech *mech, const sf_reactor_params *params, int n, const double *q,
                                       const double *pressures, double *out_rhs, double *out_jac, void *stream);
 
@@ -376,7 +392,10 @@ int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
  * at flamelet_kernels.cpp:1329-1341. scale_and_offset must be 0 when out_expeig is requested. */
 int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, int rates_option,
                           int scale_and_offset, double prefactor, double diffterm, double *out_expeig,
-                          double *out_values, void *stream);
+                          double *out_values, void *workspace, size_t workspace_bytes, void *stream);
+/* Workspace of sf_flamelet_jac_batch: 256 bytes when eigenvalue bounds are requested (the eigenvalue kernel hands
+ * out points with a counter there, zeroed on the stream before each launch), else 0. */
+size_t sf_flamelet_jac_workspace_size(const sf_mech *mech, int eigenvalues);
 
 /* The four block-Thomas functions take `active`: DEVICE int [n_flamelets] or NULL; flamelets with active[f] == 0
  * are left untouched (their values, factors and outputs keep what they held).
@@ -411,15 +430,33 @@ int sf_btddod_scale_and_add_diagonal_batch(int n_flamelets, int ns, const int *o
                                            double matrix_scale, const double *diagonal, double diag_scale,
                                            const int *active, void *stream);
 
-/* ------------------------------------------------------------------------------------------- measurement */
-/* Measured FP64 FMA throughput of the current device (TFLOP/s): independent register FMA chains on every SM,
- * timed with CUDA events; synchronizes the stream. sink: DEVICE pointer to one double. No reference counterpart:
- * it gives the FP64 roofline denominator of the benchmark. */
-int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream);
-/* The same FMA chains with only `active_lanes` (1..32) lanes of every warp working: warp-level FP64 instructions
- * issued per second. Equal rates for every lane count mean FP64 work is charged per warp instruction, whatever the
- * number of active lanes. */
-int sf_fp64_issue_probe(int iters, int active_lanes, double *out_warp_instr_per_s, double *sink, void *stream);
+/* Block-diagonal algebra (the reference's py_btddod_blockdiag_* and *_fulltriangle_* functions, griffon.pyx:1019-1069,
+ * btddod_matrix_kernels.cpp:167-177 and :364-428). A block-diagonal factorization here is the list of the blocks'
+ * inverses, and its "solve" is the block-diagonal product with them.
+ * Inverse of every column-major ns x ns block of blocks[n_blocks][ns*ns] into out_inverses (same layout) by
+ * Gauss-Jordan elimination with partial pivoting; out_pivots[n_blocks][ns] receives each block's pivot order (the
+ * reference stores LAPACK swap indices there; nothing here reads them). All pointers DEVICE; ns <= 119 on GB300. */
+int sf_btddod_blockdiag_factor_batch(int n_blocks, int ns, const double *blocks, double *out_inverses,
+                                     int *out_pivots, void *stream);
+/* y_i = B_i x_i for every block (btddod_blockdiag_matvec, and btddod_blockdiag_solve when B holds the inverses of
+ * sf_btddod_blockdiag_factor_batch). blocks DEVICE [n_blocks][ns*ns] column-major, x and out_y DEVICE
+ * [n_blocks][ns] (must not alias). */
+int sf_btddod_blockdiag_matvec_batch(int n_blocks, int ns, const double *blocks, const double *x, double *out_y,
+                                     void *stream);
+/* Block-triangular solves of BTDDOD matrices with the inverses of their diagonal blocks (btddod_lowerfulltriangle_solve
+ * with upper = 0: x_0 = D_0^-1 b_0, x_i = D_i^-1 (b_i - sub_{i-1} o x_{i-1}); btddod_upperfulltriangle_solve with
+ * upper = 1: x_{nzi-1} = D_{nzi-1}^-1 b_{nzi-1}, x_i = D_i^-1 (b_i - sup_i o x_{i+1})). inverses DEVICE
+ * [points][ns*ns] (from sf_btddod_blockdiag_factor_batch on each flamelet's diagonal blocks), values the BTDDOD
+ * values (only sub / sup are read), rhs and out_x DEVICE [points][ns] (must not alias). */
+int sf_btddod_triangle_solve_batch(int n_flamelets, int ns, const int *offsets_z, const long long *offsets_v,
+                                   const int *offsets_z_host, const double *inverses, const double *values,
+                                   const double *rhs, double *out_x, int upper, const int *active, void *stream);
+/* A <- matrix_scale*A + diag_scale*B (btddod_matrix_kernels.cpp:430-446), B a block diagonal DEVICE
+ * [points][ns*ns] (column-major blocks) added to each flamelet's diagonal blocks. */
+int sf_btddod_scale_and_add_block_diagonal_batch(int n_flamelets, int ns, const int *offsets_z,
+                                                 const long long *offsets_v, const int *offsets_z_host,
+                                                 double *values, double matrix_scale, const double *block_diag,
+                                                 double diag_scale, const int *active, void *stream);
 
 #ifdef __cplusplus
 }

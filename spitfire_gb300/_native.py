@@ -33,10 +33,13 @@ def _declare(L):
     L.sf_mech_layout.argtypes = [_vp, C.POINTER(_ip), C.POINTER(_ip), C.POINTER(C.c_longlong)]
     L.sf_device_status.argtypes = [_vp, _ip]
     L.sf_thermo_batch.argtypes = [_vp, _ip, _ip, _vp, _vp, _vp, _vp]
-    L.sf_production_rates_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _vp, _vp]
-    L.sf_rates_sens_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _ip, _vp, _vp, _vp]
-    L.sf_reactor_rhs_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp]
-    L.sf_reactor_jac_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _vp]
+    L.sf_chem_workspace_size.argtypes = [_vp, _ip, _ip]
+    L.sf_chem_workspace_size.restype = C.c_size_t
+    L.sf_production_rates_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_rates_sens_batch.argtypes = [_vp, _ip, _vp, _vp, _vp, _ip, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_reactor_rhs_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_reactor_jac_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _vp,
+                                       C.c_size_t, _vp]
     L.sf_reactor_jac_host_workspace_size.argtypes = [_vp, C.POINTER(SfReactorParams), _ip]
     L.sf_reactor_jac_host_workspace_size.restype = C.c_size_t
     L.sf_reactor_jac_host_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip, _vp, _vp, _vp, _vp, _ip, _vp,
@@ -63,14 +66,19 @@ def _declare(L):
     L.sf_flamelet_jac_indices.argtypes = [_vp, _ip, C.POINTER(_ip), C.POINTER(_ip)]
     L.sf_flamelet_rhs_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _vp, _vp]
     L.sf_flamelet_jac_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _ip, _ip, C.c_double, C.c_double,
-                                        _vp, _vp, _vp]
+                                        _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_flamelet_jac_workspace_size.argtypes = [_vp, _ip]
+    L.sf_flamelet_jac_workspace_size.restype = C.c_size_t
     L.sf_btddod_factor_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_btddod_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.sf_btddod_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
-    L.sf_fp64_peak_probe.argtypes = [_ip, C.POINTER(C.c_double), _vp, _vp]
-    L.sf_fp64_issue_probe.argtypes = [_ip, _ip, C.POINTER(C.c_double), _vp, _vp]
     L.sf_btddod_scale_and_add_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                                          C.c_double, _vp, _vp]
+    L.sf_btddod_blockdiag_factor_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp]
+    L.sf_btddod_blockdiag_matvec_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp]
+    L.sf_btddod_triangle_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _ip, _vp, _vp]
+    L.sf_btddod_scale_and_add_block_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
+                                                               C.c_double, _vp, _vp]
 
 
 # Entry points declared in include/spitfire_gb300.h (the C-ABI test checks the library exports all of them).
@@ -83,9 +91,12 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_integrate_plain_workspace_size', 'sf_integrate_plain_batch',
             'sf_flamelet_stencils', 'sf_flamelet_jac_indices', 'sf_flamelet_rhs_batch', 'sf_flamelet_jac_batch',
             'sf_btddod_factor_batch', 'sf_btddod_solve_batch', 'sf_btddod_matvec_batch',
-            'sf_btddod_scale_and_add_diagonal_batch', 'sf_fp64_peak_probe', 'sf_integrate_record_batch',
+            'sf_btddod_scale_and_add_diagonal_batch', 'sf_integrate_record_batch',
             'sf_rate_param_adjoint_batch', 'sf_mech_set_tuning', 'sf_mech_get_tuning',
-            'sf_mech_layout', 'sf_fp64_issue_probe']
+            'sf_mech_layout', 'sf_btddod_blockdiag_factor_batch',
+            'sf_btddod_blockdiag_matvec_batch', 'sf_btddod_triangle_solve_batch',
+            'sf_btddod_scale_and_add_block_diagonal_batch', 'sf_chem_workspace_size',
+            'sf_flamelet_jac_workspace_size']
 
 
 def load(path=None):

@@ -196,8 +196,7 @@ int sf_rate_param_adjoint_batch(const sf_mech *mech, const sf_reactor_params *rp
     if (groups < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the parameter-adjoint kernel");
     p.groups_per_cta = groups;
     const size_t smem = hm.dm.blob_bytes + per * groups;
-    CUDA_THROW(cudaFuncSetAttribute(rate_param_adjoint_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
+    ensure_dynamic_smem((const void *)rate_param_adjoint_kernel<G>, smem);
     const int bps = std::max(1, (int)((size_t)smem_max / smem));
     const int grid = (int)std::max<long long>(
         1, std::min<long long>(((long long)n_items + groups - 1) / groups, (long long)nsm * bps));

@@ -192,29 +192,33 @@ __global__ void __launch_bounds__(128) chem_kernel_tps(const KParams p)
   }
 }
 
-// Interleaved scratch of the thread-per-state kernels: one slot of 32 x (Jacobian scratch) doubles per warp that
-// can be resident at once (the CTAS knob, else the occupancy of the Jacobian kernel at the blob's shared memory).
-void ensure_tps_scratch(HostMech &hm)
+// Interleaved scratch of the thread-per-state kernels: one slot of 32 x (per-state scratch) doubles per warp of
+// the launch, at most one per warp that can be resident at once (the CTAS knob, else the occupancy of the kernel at
+// the blob's shared memory). The caller's workspace holds the slots.
+constexpr int kTpsThreads = 128;
+
+size_t tps_resident_warps(const HostMech &hm)
 {
   int dev, nsm;
   CUDA_THROW(cudaGetDevice(&dev));
   CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const size_t smem = hm.dm.blob_bytes;
-  CUDA_THROW(cudaFuncSetAttribute(chem_kernel_tps<MODE_JAC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ctas = hm.tune[SF_TUNE_TPS_CTAS];
   if (ctas <= 0) {
-    CUDA_THROW(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, chem_kernel_tps<MODE_JAC>, 128, smem));
+    const size_t smem = hm.dm.blob_bytes;
+    ensure_dynamic_smem((const void *)chem_kernel_tps<MODE_JAC>, smem);
+    CUDA_THROW(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, chem_kernel_tps<MODE_JAC>, kTpsThreads, smem));
     if (ctas < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the thread-per-state kernels");
   }
-  const size_t bytes = (size_t)nsm * ctas * 4 * 32 * hm.sl.total * sizeof(double);
-  if (hm.tps_scratch && hm.tps_scratch_bytes == bytes) return;
-  if (hm.tps_scratch) {
-    CUDA_THROW(cudaFree(hm.tps_scratch));
-    hm.tps_scratch = nullptr;
-    hm.tps_scratch_bytes = 0;
-  }
-  CUDA_THROW(cudaMalloc(&hm.tps_scratch, bytes));
-  hm.tps_scratch_bytes = bytes;
+  return (size_t)nsm * ctas * (kTpsThreads / 32);
+}
+
+size_t tps_scratch_bytes(const HostMech &hm, int mode, long long n)
+{
+  if (n <= 0) return 0;
+  const size_t per_warp = (size_t)32 * (jac_mode(mode) ? hm.sl.total : hm.sl.total_rhs) * 8;
+  const size_t wpb = kTpsThreads / 32;  // whole blocks: every warp of a launch has a slot
+  const size_t warps = std::min<size_t>(((size_t)((n + 31) / 32) + wpb - 1) / wpb * wpb, tps_resident_warps(hm));
+  return per_warp * warps;
 }
 
 // ------------------------------------------------------------------------------------------------ launchers
@@ -222,10 +226,8 @@ namespace {
 
 int pick_group(const DevMech &m) { return m.nr >= 96 || m.ns >= 24 ? 32 : (m.nr >= 24 ? 16 : 8); }
 
-constexpr int kTpsThreads = 128;
-
 template <int MODE>
-int launch_tps(HostMech &hm, KParams &p, cudaStream_t st)
+int launch_tps(const HostMech &hm, KParams &p, cudaStream_t st, void *ws, size_t ws_bytes)
 {
   const auto &progs = hm.programs_for(1);
   p.m = hm.dm;
@@ -237,23 +239,27 @@ int launch_tps(HostMech &hm, KParams &p, cudaStream_t st)
   p.prog_j = (MODE == MODE_SENS) ? progs.progs[3] : progs.progs[2];
   if (p.n == 0) return SF_OK;
   const size_t per_warp = (size_t)32 * (jac_mode(MODE) ? hm.sl.total : hm.sl.total_rhs) * 8;
-  const int warps_avail = (int)std::min<size_t>(hm.tps_scratch_bytes / per_warp, (size_t)1 << 30);
-  if (warps_avail < kTpsThreads / 32)
-    throw sf_error(SF_ERR_UNSUPPORTED, "thread-per-state scratch not allocated (set the lanes-per-state knob to 1)");
-  p.gscratch = hm.tps_scratch;
+  const size_t need_bytes = tps_scratch_bytes(hm, MODE, p.n);
+  if (!ws || ws_bytes < need_bytes)
+    throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_chem_workspace_size reports (" +
+                                         std::to_string(need_bytes) + " bytes for these states)");
+  // slots of whole 4-warp blocks: a launch never has more warps than the workspace has slots
+  const long long blocks_avail = (long long)(ws_bytes / per_warp) / (kTpsThreads / 32);
+  const long long max_blocks = std::max<long long>(1, (long long)(tps_resident_warps(hm) / (kTpsThreads / 32)));
+  p.gscratch = static_cast<double *>(ws);
   const size_t smem = hm.dm.blob_bytes;
-  CUDA_THROW(cudaFuncSetAttribute(chem_kernel_tps<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)chem_kernel_tps<MODE>, smem);
   const long long need = ((long long)p.n + kTpsThreads - 1) / kTpsThreads;
-  const int grid = (int)std::max<long long>(1, std::min<long long>(need, warps_avail / (kTpsThreads / 32)));
+  const int grid = (int)std::max<long long>(1, std::min(need, std::min(blocks_avail, max_blocks)));
   chem_kernel_tps<MODE><<<grid, kTpsThreads, smem, st>>>(p);
   CUDA_THROW(cudaGetLastError());
   return SF_OK;
 }
 
 template <int MODE>
-int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
+int launch_mode(const HostMech &hm, KParams &p, cudaStream_t st, int G_req, void *ws, size_t ws_bytes)
 {
-  if (G_req == 1) return launch_tps<MODE>(hm, p, st);
+  if (G_req == 1) return launch_tps<MODE>(hm, p, st, ws, ws_bytes);
   const int G = G_req > 0 ? G_req : pick_group(hm.dm);
   const auto &progs = hm.programs_for(G);
   p.m = hm.dm;
@@ -284,7 +290,7 @@ int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
   case 16: kern = chem_kernel<16, MODE>; break;
   default: kern = chem_kernel<32, MODE>; break;
   }
-  CUDA_THROW(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)kern, smem);
   const int blocks_per_sm = std::max(1, (int)(((size_t)smem_max) / smem));
   const long long need = ((long long)p.n + groups - 1) / groups;
   const int grid = (int)std::max<long long>(1, std::min<long long>(need, (long long)nsm * blocks_per_sm));
@@ -296,13 +302,17 @@ int launch_mode(HostMech &hm, KParams &p, cudaStream_t st, int G_req)
 
 }  // namespace
 
-int chem_launch(HostMech &hm, int mode, KParams &p, cudaStream_t st, int G)
+int chem_launch(const HostMech &hm, int mode, KParams &p, cudaStream_t st, int G, void *ws, size_t ws_bytes)
 {
   switch (mode) {
-  case MODE_RATES: return launch_mode<MODE_RATES>(hm, p, st, G);
-  case MODE_SENS: return launch_mode<MODE_SENS>(hm, p, st, G);
-  case MODE_RHS: return p.open ? launch_mode<MODE_RHS_OPEN>(hm, p, st, G) : launch_mode<MODE_RHS>(hm, p, st, G);
-  default: return p.open ? launch_mode<MODE_JAC_OPEN>(hm, p, st, G) : launch_mode<MODE_JAC>(hm, p, st, G);
+  case MODE_RATES: return launch_mode<MODE_RATES>(hm, p, st, G, ws, ws_bytes);
+  case MODE_SENS: return launch_mode<MODE_SENS>(hm, p, st, G, ws, ws_bytes);
+  case MODE_RHS:
+    return p.open ? launch_mode<MODE_RHS_OPEN>(hm, p, st, G, ws, ws_bytes)
+                  : launch_mode<MODE_RHS>(hm, p, st, G, ws, ws_bytes);
+  default:
+    return p.open ? launch_mode<MODE_JAC_OPEN>(hm, p, st, G, ws, ws_bytes)
+                  : launch_mode<MODE_JAC>(hm, p, st, G, ws, ws_bytes);
   }
 }
 
@@ -355,26 +365,7 @@ int sf_mech_set_tuning(sf_mech *mech, int knob, int value)
     t_err = "sf_mech_set_tuning: value out of range for this knob";
     return SF_ERR_INVALID_ARGUMENT;
   }
-  const int old = mech->m.tune[knob];
   mech->m.tune[knob] = value;
-  bool tps = false;
-  for (int k = SF_TUNE_GROUP_RATES; k <= SF_TUNE_GROUP_JAC; ++k) tps |= mech->m.tune[k] == 1;
-  if (tps && ((knob <= SF_TUNE_GROUP_JAC && value == 1) || knob == SF_TUNE_TPS_CTAS)) {
-    // thread-per-state kernels: interleaved scratch for every warp that can be resident, (re)allocated here so
-    // that the batched entry points themselves never allocate
-    try {
-      sfgb::ensure_tps_scratch(mech->m);
-    } catch (sfgb::sf_error &e) {
-      mech->m.tune[knob] = old;
-      t_err = e.what();
-      return e.code;
-    }
-  }
-  if (!tps && mech->m.tps_scratch) {
-    cudaFree(mech->m.tps_scratch);
-    mech->m.tps_scratch = nullptr;
-    mech->m.tps_scratch_bytes = 0;
-  }
   return SF_OK;
 }
 
@@ -446,7 +437,7 @@ int sf_mech_info(const sf_mech *m, int *ns, int *nr, int *counts)
 }
 
 int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const double *rho, const double *Y,
-                              double *out_w, void *stream)
+                              double *out_w, void *workspace, size_t workspace_bytes, void *stream)
 {
   return guard([&] {
     if (!mech || n < 0 || (n > 0 && (!T || !rho || !Y || !out_w))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
@@ -457,13 +448,13 @@ int sf_production_rates_batch(const sf_mech *mech, int n, const double *T, const
     p.Y = Y;
     p.out_w = out_w;
     p.configuration = 0;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RATES, p, (cudaStream_t)stream,
-                       group_of(mech->m, SF_TUNE_GROUP_RATES));
+    return chem_launch(mech->m, MODE_RATES, p, (cudaStream_t)stream, group_of(mech->m, SF_TUNE_GROUP_RATES),
+                       workspace, workspace_bytes);
   });
 }
 
 int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const double *T, const double *Y, int option,
-                        double *out_w, double *out_sens, void *stream)
+                        double *out_w, double *out_sens, void *workspace, size_t workspace_bytes, void *stream)
 {
   return guard([&] {
     if (!mech || n < 0 || (n > 0 && (!T || !rho || !Y || !out_w || !out_sens)))
@@ -477,8 +468,8 @@ int sf_rates_sens_batch(const sf_mech *mech, int n, const double *rho, const dou
     p.option = option;
     p.out_w = out_w;
     p.out_S = out_sens;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_SENS, p, (cudaStream_t)stream,
-                       group_of(mech->m, SF_TUNE_GROUP_SENS));
+    return chem_launch(mech->m, MODE_SENS, p, (cudaStream_t)stream, group_of(mech->m, SF_TUNE_GROUP_SENS),
+                       workspace, workspace_bytes);
   });
 }
 
@@ -508,7 +499,8 @@ static void fill_reactor(KParams &p, const sf_reactor_params *rp)
 }
 
 int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *rp, int n, const double *q,
-                         const double *pressures, double *out_rhs, void *stream)
+                         const double *pressures, double *out_rhs, void *workspace, size_t workspace_bytes,
+                         void *stream)
 {
   return guard([&] {
     if (!mech || n < 0 || (n > 0 && (!q || !out_rhs))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
@@ -518,13 +510,14 @@ int sf_reactor_rhs_batch(const sf_mech *mech, const sf_reactor_params *rp, int n
     p.q = q;
     p.pressures = pressures;
     p.out_rhs = out_rhs;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_RHS, p, (cudaStream_t)stream,
-                       group_of(mech->m, SF_TUNE_GROUP_RHS));
+    return chem_launch(mech->m, MODE_RHS, p, (cudaStream_t)stream, group_of(mech->m, SF_TUNE_GROUP_RHS), workspace,
+                       workspace_bytes);
   });
 }
 
 int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n, const double *q,
-                         const double *pressures, double *out_rhs, double *out_jac, void *stream)
+                         const double *pressures, double *out_rhs, double *out_jac, void *workspace,
+                         size_t workspace_bytes, void *stream)
 {
   return guard([&] {
     if (!mech || n < 0 || (n > 0 && (!q || !out_rhs || !out_jac))) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
@@ -537,9 +530,23 @@ int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int r
     p.option = rates_option;
     p.out_rhs = out_rhs;
     p.out_J = out_jac;
-    return chem_launch(const_cast<HostMech &>(mech->m), MODE_JAC, p, (cudaStream_t)stream,
-                       group_of(mech->m, SF_TUNE_GROUP_JAC));
+    return chem_launch(mech->m, MODE_JAC, p, (cudaStream_t)stream, group_of(mech->m, SF_TUNE_GROUP_JAC), workspace,
+                       workspace_bytes);
   });
+}
+
+size_t sf_chem_workspace_size(const sf_mech *mech, int kind, int n)
+{
+  if (!mech || n <= 0 || kind < SF_CHEM_RATES || kind > SF_CHEM_JAC) return 0;
+  static const int knob[4] = {SF_TUNE_GROUP_RATES, SF_TUNE_GROUP_SENS, SF_TUNE_GROUP_RHS, SF_TUNE_GROUP_JAC};
+  static const int mode[4] = {MODE_RATES, MODE_SENS, MODE_RHS, MODE_JAC};
+  if (group_of(mech->m, knob[kind]) != 1) return 0;
+  try {
+    return tps_scratch_bytes(mech->m, mode[kind], n);
+  } catch (sf_error &e) {
+    t_err = e.what();
+    return 0;
+  }
 }
 
 size_t sf_reactor_jac_host_workspace_size(const sf_mech *mech, const sf_reactor_params *rp, int n)
@@ -547,7 +554,8 @@ size_t sf_reactor_jac_host_workspace_size(const sf_mech *mech, const sf_reactor_
   if (!mech || !rp || n < 0) return 0;
   const size_t neq = (size_t)mech->m.dm.ns + (rp->configuration == 1 ? 1 : 0);
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  return up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8) + up(n * neq * neq * 8);
+  return up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8) + up(n * neq * neq * 8) +
+         sf_chem_workspace_size(mech, SF_CHEM_JAC, n);
 }
 
 int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n,
@@ -563,25 +571,24 @@ int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *rp, 
     if (!workspace || workspace_bytes < sf_reactor_jac_host_workspace_size(mech, rp, n))
       throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_reactor_jac_host_workspace_size reports");
     HostMech &hm = const_cast<HostMech &>(mech->m);
+    // the copy stream and chunk events belong to the mechanism: calls from several threads take turns here (each
+    // event wait captures its own record), their copies sharing the copy stream
+    std::lock_guard<std::mutex> lock(hm.host_batch_mutex);
     const size_t neq = (size_t)hm.dm.ns + (rp->configuration == 1 ? 1 : 0);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     char *w = static_cast<char *>(workspace);
+    const size_t io_bytes = up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8) + up(n * neq * neq * 8);
     double *q = reinterpret_cast<double *>(w);
     double *pr = reinterpret_cast<double *>(w + up(n * neq * 8));
     double *rhs = reinterpret_cast<double *>(w + up(n * neq * 8) + up((size_t)n * 8));
     double *J = reinterpret_cast<double *>(w + up(n * neq * 8) + up((size_t)n * 8) + up(n * neq * 8));
+    void *kws = w + io_bytes;  // the kernel's scratch: every chunk runs on `stream`, one after another
+    const size_t kws_bytes = workspace_bytes - io_bytes;
     cudaStream_t st = (cudaStream_t)stream;
     const int G = group_of(hm, SF_TUNE_GROUP_JAC);
     // chunk: by default the states one wave of the thread-per-state kernel covers (its resident warps), else half
     int chunk = chunk_states;
-    if (chunk <= 0) {
-      if (G == 1 && hm.tps_scratch_bytes) {
-        const size_t per_warp = (size_t)32 * hm.sl.total * 8;
-        chunk = (int)std::min<size_t>((size_t)n, hm.tps_scratch_bytes / per_warp * 32);
-      } else {
-        chunk = (n + 1) / 2;
-      }
-    }
+    if (chunk <= 0) chunk = G == 1 ? (int)std::min<size_t>((size_t)n, tps_resident_warps(hm) * 32) : (n + 1) / 2;
     chunk = std::max(1, std::min(chunk, n));
     const int nchunks = (n + chunk - 1) / chunk;
     if (!hm.copy_stream) CUDA_THROW(cudaStreamCreateWithFlags(&hm.copy_stream, cudaStreamNonBlocking));
@@ -605,7 +612,7 @@ int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *rp, 
       p.option = rates_option;
       p.out_rhs = rhs + a * neq;
       p.out_J = J + a * neq * neq;
-      const int rc = chem_launch(hm, MODE_JAC, p, st, G);
+      const int rc = chem_launch(hm, MODE_JAC, p, st, G, kws, kws_bytes);
       if (rc != SF_OK) return (int)rc;
       CUDA_THROW(cudaEventRecord(hm.events[c], st));
       CUDA_THROW(cudaStreamWaitEvent(hm.copy_stream, hm.events[c], 0));

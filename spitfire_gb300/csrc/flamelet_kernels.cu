@@ -751,6 +751,119 @@ __global__ void __launch_bounds__(64) btddod_solve_kernel(int nf, int ns, const 
   }
 }
 
+// Block-triangular solves with the inverses of a block-diagonal factorization (btddod_matrix_kernels.cpp:386-428):
+//   lower  x_0 = F_0 b_0,               x_i = F_i (b_i - sub_{i-1} o x_{i-1})
+//   upper  x_{nb-1} = F_{nb-1} b_{nb-1}, x_i = F_i (b_i - sup_i o x_{i+1})
+// One warp per flamelet; F_i (column-major inverses, [points][ns*ns]) are streamed into shared memory one block
+// ahead, the vector stays in registers.
+template <int R>
+__global__ void __launch_bounds__(32) btddod_triangle_solve_kernel(int nf, int ns, const int *offz,
+                                                                   const long long *offv, const double *inverses,
+                                                                   const double *values, const double *rhs, double *x,
+                                                                   int upper, const int *active, int double_buffer)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int f = blockIdx.x;
+  if (f >= nf || (active && !active[f])) return;
+  const int z0 = offz[f], nb = offz[f + 1] - z0;
+  const int bs2 = ns * ns;
+  double *sm = reinterpret_cast<double *>(smem);
+  SweepBuffers sb{sm, sm + (double_buffer ? bs2 : 0), double_buffer != 0, bs2};
+  const double *vals = values + offv[f];
+  const double *sub = vals + (size_t)nb * bs2;
+  const double *sup = sub + (size_t)(nb - 1) * ns;
+  const double *b = rhs + (size_t)z0 * ns;
+  double *xs = x + (size_t)z0 * ns;
+  auto blk = [&](int t) { return upper ? nb - 1 - t : t; };
+  auto fsrc = [&](int t) { return inverses + (size_t)(z0 + blk(t)) * bs2; };
+  const int lane = threadIdx.x & 31;
+  double xp[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) xp[s] = 0.;
+  sb.prime(0, fsrc);
+  for (int t = 0; t < nb; ++t) {
+    const double *F = sb.get(t, nb - 1, 1, fsrc);
+    const int i = blk(t);
+    double v[R];
+    vec_load<R>(v, b + (size_t)i * ns, ns);
+    if (t > 0) {
+      const double *cpl = upper ? sup + (size_t)i * ns : sub + (size_t)(i - 1) * ns;
+#pragma unroll
+      for (int s = 0; s < R; ++s) {
+        const int k = lane + 32 * s;
+        if (k < ns) v[s] = v[s] - cpl[k] * xp[s];
+      }
+    }
+    vec_apply<R>(F, ns, v);
+    vec_store<R>(xs + (size_t)i * ns, v, ns);
+#pragma unroll
+    for (int s = 0; s < R; ++s) xp[s] = v[s];
+  }
+}
+
+// Inverse of every ns x ns column-major block of a list (btddod_matrix_kernels.cpp:364-373 factors each block of a
+// block-diagonal matrix): one CTA per block, Gauss-Jordan with partial pivoting as in the block-Thomas
+// factorization. pivots receives each block's pivot order.
+__global__ void __launch_bounds__(kFactorThreads) blockdiag_inverse_kernel(int n_blocks, int ns, const double *blocks,
+                                                                           double *out_inv, int *pivots)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int blkid = blockIdx.x;
+  if (blkid >= n_blocks) return;
+  const int bs2 = ns * ns;
+  FactorShared sh(smem, ns);
+  const double *A = blocks + (size_t)blkid * bs2;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    sh.buf0[r * ns + c] = A[e];
+  }
+  __syncthreads();
+  const double *Z = cta_gj_inverse(sh.buf0, sh.buf1, ns, sh.piv, sh.pinv, sh.ws, sh.used);
+  double *O = out_inv + (size_t)blkid * bs2;
+  for (int e = tid; e < bs2; e += nt) {
+    const int c = e / ns, r = e - c * ns;
+    O[e] = Z[sh.piv[r] * ns + sh.pinv[c]];
+  }
+  for (int k = tid; k < ns; k += nt) pivots[(size_t)blkid * ns + k] = sh.piv[k];
+}
+
+// y_i = B_i x_i for every block of a list (btddod_matrix_kernels.cpp:167-177, and :375-384 with the inverses of a
+// block-diagonal factorization): one thread per row.
+__global__ void blockdiag_matvec_kernel(int n_blocks, int ns, const double *blocks, const double *x, double *y)
+{
+  const long long total = (long long)n_blocks * ns;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long bi = t / ns;
+    const int r = (int)(t - bi * ns);
+    const double *B = blocks + (size_t)bi * ns * ns;
+    const double *xs = x + (size_t)bi * ns;
+    double v = 0.;
+    for (int c = 0; c < ns; ++c) v += B[r + c * ns] * xs[c];
+    y[t] = v;
+  }
+}
+
+// A <- matrix_scale*A + diag_scale*B over the BTDDOD values, B a block diagonal [points][ns*ns]
+// (btddod_matrix_kernels.cpp:430-446): grid (chunks, flamelets), one value per thread per chunk step.
+__global__ void btddod_scale_block_diag_kernel(int nf, int ns, const int *offz, const long long *offv, double *values,
+                                               double ms, const double *bdiag, double ds, const int *active)
+{
+  const int f = blockIdx.y;
+  if (f >= nf || (active && !active[f])) return;
+  const int z0 = offz[f], nb = offz[f + 1] - z0;
+  const long long bs2 = (long long)ns * ns;
+  const long long ne = (long long)ns * (nb * ns + 2 * (nb - 1));
+  double *vals = values + offv[f];
+  const double *bd = bdiag + (size_t)z0 * bs2;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+    double v = __dmul_rn(vals[e], ms);
+    if (e < nb * bs2) v = __dadd_rn(v, __dmul_rn(bd[e], ds));
+    vals[e] = v;
+  }
+}
+
 // y = A x (btddod_matrix_kernels.cpp:121-160): one thread per row of every point of every flamelet.
 __global__ void btddod_matvec_kernel(int n_points, int nf, int ns, const int *offz, const long long *offv,
                                      const double *values, const double *x, double *y, const int *active)
@@ -818,7 +931,7 @@ int launch_points(HostMech &hm, FlmParams &p, bool jac, cudaStream_t st)
   p.groups_per_cta = groups;
   const size_t smem = hm.dm.blob_bytes + per * groups;
   void (*k)(const FlmParams) = jac ? flamelet_point_kernel<32, true> : flamelet_point_kernel<32, false>;
-  CUDA_THROW(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)k, smem);
   const int bps = std::max(1, (int)((size_t)smem_max / smem));
   const int grid = (int)std::max<long long>(1, std::min<long long>(((long long)p.n_points + groups - 1) / groups,
                                                                    (long long)nsm * bps));
@@ -897,9 +1010,27 @@ int launch_solve(int nf, int ns, const int *offz, const long long *offv, const d
   const size_t smem = (size_t)(dbl ? 4 : 2) * ns * ns * 8 + extra;
   if (smem > (size_t)smem_max)
     throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block-Thomas solve");
-  CUDA_THROW(cudaFuncSetAttribute(btddod_solve_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ensure_dynamic_smem((const void *)btddod_solve_kernel<R>, smem);
   btddod_solve_kernel<R><<<nf, 64, smem, st>>>(nf, ns, offz, offv, values, l_values, pivots, rhs, out_x, active,
                                                dbl);
+  return check_launch();
+}
+
+template <int R>
+int launch_triangle(int nf, int ns, const int *offz, const long long *offv, const double *inverses,
+                    const double *values, const double *rhs, double *out_x, int upper, const int *active,
+                    cudaStream_t st)
+{
+  int dev, smem_max;
+  CUDA_THROW(cudaGetDevice(&dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int dbl = (size_t)2 * ns * ns * 8 <= (size_t)smem_max ? 1 : 0;
+  const size_t smem = (size_t)(dbl ? 2 : 1) * ns * ns * 8;
+  if (smem > (size_t)smem_max)
+    throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory triangular solve");
+  ensure_dynamic_smem((const void *)btddod_triangle_solve_kernel<R>, smem);
+  btddod_triangle_solve_kernel<R><<<nf, 32, smem, st>>>(nf, ns, offz, offv, inverses, values, rhs, out_x, upper,
+                                                         active, dbl);
   return check_launch();
 }
 
@@ -909,6 +1040,81 @@ int launch_solve(int nf, int ns, const int *offz, const long long *offv, const d
 using namespace sfgb;
 
 extern "C" {
+
+int sf_btddod_blockdiag_factor_batch(int n_blocks, int ns, const double *blocks, double *out_inverses,
+                                     int *out_pivots, void *stream)
+{
+  if (n_blocks < 0 || ns < 1 || ns > 128 || (n_blocks > 0 && (!blocks || !out_inverses || !out_pivots))) {
+    set_error("sf_btddod_blockdiag_factor_batch: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  if (n_blocks == 0) return SF_OK;
+  const size_t smem = factor_smem_bytes(ns);
+  return guarded([&] {
+    int dev, smem_max;
+    CUDA_THROW(cudaGetDevice(&dev));
+    CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem > (size_t)smem_max)
+      throw sf_error(SF_ERR_UNSUPPORTED, "block size too large for the shared-memory block inverse");
+    ensure_dynamic_smem((const void *)blockdiag_inverse_kernel, smem);
+    blockdiag_inverse_kernel<<<n_blocks, kFactorThreads, smem, (cudaStream_t)stream>>>(n_blocks, ns, blocks,
+                                                                                        out_inverses, out_pivots);
+    return check_launch();
+  });
+}
+
+int sf_btddod_blockdiag_matvec_batch(int n_blocks, int ns, const double *blocks, const double *x, double *out_y,
+                                     void *stream)
+{
+  if (n_blocks < 0 || ns < 1 || (n_blocks > 0 && (!blocks || !x || !out_y))) {
+    set_error("sf_btddod_blockdiag_matvec_batch: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  if (n_blocks == 0) return SF_OK;
+  const long long rows = (long long)n_blocks * ns;
+  const int grid = (int)std::max<long long>(1, std::min<long long>((rows + 255) / 256, 152LL * 16));
+  blockdiag_matvec_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(n_blocks, ns, blocks, x, out_y);
+  return check_launch();
+}
+
+int sf_btddod_triangle_solve_batch(int nf, int ns, const int *offz, const long long *offv, const int *offz_host,
+                                   const double *inverses, const double *values, const double *rhs, double *out_x,
+                                   int upper, const int *active, void *stream)
+{
+  if (nf < 1 || ns < 1 || ns > 128 || !offz || !offv || !inverses || !values || !rhs || !out_x) {
+    set_error("sf_btddod_triangle_solve_batch: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  (void)offz_host;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int up = upper ? 1 : 0;
+  return guarded([&] {
+    if (ns <= 32) return launch_triangle<1>(nf, ns, offz, offv, inverses, values, rhs, out_x, up, active, st);
+    if (ns <= 64) return launch_triangle<2>(nf, ns, offz, offv, inverses, values, rhs, out_x, up, active, st);
+    if (ns <= 96) return launch_triangle<3>(nf, ns, offz, offv, inverses, values, rhs, out_x, up, active, st);
+    return launch_triangle<4>(nf, ns, offz, offv, inverses, values, rhs, out_x, up, active, st);
+  });
+}
+
+int sf_btddod_scale_and_add_block_diagonal_batch(int nf, int ns, const int *offz, const long long *offv,
+                                                 const int *offz_host, double *values, double ms,
+                                                 const double *block_diag, double ds, const int *active,
+                                                 void *stream)
+{
+  if (nf < 1 || ns < 1 || nf > 65535 || !offz || !offv || !offz_host || !values || !block_diag) {
+    set_error("sf_btddod_scale_and_add_block_diagonal_batch: bad argument");
+    return SF_ERR_INVALID_ARGUMENT;
+  }
+  long long max_ne = 0;
+  for (int f = 0; f < nf; ++f) {
+    const long long nb = offz_host[f + 1] - offz_host[f];
+    max_ne = std::max(max_ne, (long long)ns * (nb * ns + 2 * (nb - 1)));
+  }
+  const int chunks = (int)std::max<long long>(1, std::min<long long>((max_ne + 1023) / 1024, 1024));
+  btddod_scale_block_diag_kernel<<<dim3(chunks, nf), 256, 0, (cudaStream_t)stream>>>(nf, ns, offz, offv, values, ms,
+                                                                                     block_diag, ds, active);
+  return check_launch();
+}
 
 int sf_flamelet_stencils(const sf_mech *mech, const double *dz, int nzi, const double *chi, const double *invLe,
                          double *cmaj, double *csub, double *csup, double *mc, double *nc)
@@ -974,12 +1180,19 @@ int sf_flamelet_rhs_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
   });
 }
 
+size_t sf_flamelet_jac_workspace_size(const sf_mech *mech, int eigenvalues)
+{
+  return mech && eigenvalues ? 256 : 0;
+}
+
 int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, const double *state, int rates_option,
                           int scale_and_offset, double prefactor, double diffterm, double *out_expeig,
-                          double *out_values, void *stream)
+                          double *out_values, void *workspace, size_t workspace_bytes, void *stream)
 {
   return guarded([&] {
     if (!mech || !state || !out_values) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad argument");
+    if (out_expeig && (!workspace || workspace_bytes < sf_flamelet_jac_workspace_size(mech, 1)))
+      throw sf_error(SF_ERR_WORKSPACE, "eigenvalue bounds need the workspace sf_flamelet_jac_workspace_size reports");
     if (rates_option < 0 || rates_option > 2)
       throw sf_error(SF_ERR_INVALID_ARGUMENT, "rates option must be 0, 1 or 2");
     if (out_expeig && scale_and_offset)
@@ -1004,18 +1217,19 @@ int sf_flamelet_jac_batch(const sf_mech *mech, const sf_flamelet_batch *fb, cons
       const size_t per = (size_t)(ns * ns + 2 * ns) * 8;
       const int warps = (int)std::min<size_t>(8, (size_t)smem_max / per);
       if (warps < 1) throw sf_error(SF_ERR_UNSUPPORTED, "block too large for the eigenvalue kernel");
-      CUDA_THROW(cudaFuncSetAttribute(flamelet_expeig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(per * warps)));
+      ensure_dynamic_smem((const void *)flamelet_expeig_kernel, per * warps);
       int per_sm = 0;
       CUDA_THROW(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, flamelet_expeig_kernel, 32 * warps,
                                                                per * warps));
       const int grid = (int)std::max<long long>(1, std::min<long long>((long long)nsm * std::max(1, per_sm),
                                                                        ((long long)p.n_points + warps - 1) / warps));
-      CUDA_THROW(cudaMemsetAsync(hm.d_work_counter, 0, sizeof(int), st));
+      // the points are handed out by an atomic counter in the caller's workspace, zeroed on the stream first
+      int *counter = static_cast<int *>(workspace);
+      CUDA_THROW(cudaMemsetAsync(counter, 0, sizeof(int), st));
       flamelet_expeig_kernel<<<grid, 32 * warps, per * warps, st>>>(p.n_points, p.n_flamelets, ns, p.offz, p.offv,
                                                                     out_values, p.cmajor, diffterm, fb->diffterm,
                                                                     fb->active, out_expeig, hm.d_status, warps,
-                                                                    hm.d_work_counter);
+                                                                    counter);
       CUDA_THROW(cudaGetLastError());
     }
     return SF_OK;
@@ -1043,9 +1257,8 @@ int sf_btddod_factor_batch(int nf, int ns, const int *offz, const long long *off
     // Each CTA is bound by its SM's FP64 unit. When every CTA can have an SM of its own, ask for more than half an
     // SM's shared memory so that no two CTAs share one (the block scheduler may otherwise pair them).
     const size_t smem_launch = 2LL * nf <= nsm ? std::max(smem, (size_t)smem_max / 2 + 1024) : smem;
-    CUDA_THROW(cudaFuncSetAttribute(btddod_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_launch));
-    CUDA_THROW(cudaFuncSetAttribute(btddod_middle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_dynamic_smem((const void *)btddod_factor_kernel, smem_launch);
+    ensure_dynamic_smem((const void *)btddod_middle_kernel, smem);
     cudaStream_t st = (cudaStream_t)stream;
     btddod_factor_kernel<<<2 * nf, kFactorThreads, smem_launch, st>>>(nf, ns, offz, offv, values, l_values, pivots,
                                                                       active);

@@ -474,7 +474,7 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
                           : nullptr;
     p.mat_doubles = matrix_doubles(p.neq, p.prec);
     auto kern = p.cfg.open ? integrate_kernel<true> : integrate_kernel<false>;
-    CUDA_THROW(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+    ensure_dynamic_smem((const void *)kern, sh.smem);
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_THROW(cudaMemsetAsync(workspace, 0, 256, st));
     kern<<<sh.grid, 32 * sh.warps, sh.smem, st>>>(p);

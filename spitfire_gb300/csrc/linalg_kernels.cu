@@ -159,12 +159,22 @@ int sf_newton_lu_batch(int n, int m, const double *J, const double *gamma_h, int
   const size_t mm = (size_t)m * m;
   if (precision == 0) {
     const size_t smem = kWarpsPerCta * (mm * 8 + m * 4);
-    cudaFuncSetAttribute(lu64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    try {
+      ensure_dynamic_smem((const void *)lu64_kernel, smem);
+    } catch (sf_error &e) {
+      set_error(e.what());
+      return e.code;
+    }
     lu64_kernel<<<grid_for(n), 32 * kWarpsPerCta, smem, st>>>(n, m, J, gamma_h, out_A, (double *)out_lu, out_piv,
                                                               out_info);
   } else if (precision == 1) {
     const size_t smem = kWarpsPerCta * (mm * 4 + m * 4);
-    cudaFuncSetAttribute(lu32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    try {
+      ensure_dynamic_smem((const void *)lu32_kernel, smem);
+    } catch (sf_error &e) {
+      set_error(e.what());
+      return e.code;
+    }
     lu32_kernel<<<grid_for(n), 32 * kWarpsPerCta, smem, st>>>(n, m, J, gamma_h, out_A, (float *)out_lu, out_piv,
                                                               out_info);
   } else {
@@ -191,7 +201,12 @@ int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const i
   const size_t mm = (size_t)m * m;
   if (precision == 0) {
     const size_t smem = kWarpsPerCta * ((mm + m) * 8 + m * 4);
-    cudaFuncSetAttribute(solve64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    try {
+      ensure_dynamic_smem((const void *)solve64_kernel, smem);
+    } catch (sf_error &e) {
+      set_error(e.what());
+      return e.code;
+    }
     solve64_kernel<<<grid_for(n), 32 * kWarpsPerCta, smem, st>>>(n, m, (const double *)lu, piv, b, out_x);
   } else if (precision == 1) {
     if (!A) {
@@ -200,7 +215,12 @@ int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const i
     }
     const size_t per = mm / 2 + 2 * (size_t)m + 2;
     const size_t smem = kWarpsPerCta * (per * 8 + m * 4);
-    cudaFuncSetAttribute(solve32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    try {
+      ensure_dynamic_smem((const void *)solve32_kernel, smem);
+    } catch (sf_error &e) {
+      set_error(e.what());
+      return e.code;
+    }
     solve32_kernel<<<grid_for(n), 32 * kWarpsPerCta, smem, st>>>(n, m, A, (const float *)lu, piv, refine, b, out_x);
   } else {
     set_error("sf_newton_solve_batch: precision must be 0 or 1");
@@ -215,88 +235,3 @@ int sf_newton_solve_batch(int n, int m, const double *A, const void *lu, const i
 }
 
 }  // extern "C"
-
-// ------------------------------------------------------------------------------------ FP64 pipe peak probe
-// Independent FP64 FMA chains in registers (8 per thread, no memory traffic), for the FP64 roofline denominator:
-// the measured-peaks file of this machine has HBM and bf16 figures only.
-namespace sfgb {
-namespace {
-__global__ void fp64_probe_kernel(int iters, double seed, double *sink, int active_lanes)
-{
-  double a[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) a[k] = seed + k * 1e-3 + threadIdx.x * 1e-7;
-  const double b = 0.999999999, c = 1e-9;
-  if ((int)(threadIdx.x & 31) < active_lanes)
-    for (int i = 0; i < iters; ++i) {
-#pragma unroll
-      for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
-    }
-  double s = 0.;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) s += a[k];
-  if (s == 12345.678) sink[0] = s;  // keeps the chains live
-}
-}  // namespace
-}  // namespace sfgb
-
-namespace {
-// Elapsed milliseconds of one probe launch (8 blocks per SM, 256 threads, `active_lanes` lanes of every warp
-// running 8 independent FMA chains of `iters` steps), after a short warm-up launch.
-int probe_ms(int iters, int active_lanes, double *sink, cudaStream_t st, float *ms, int *blocks, int *threads)
-{
-  int dev, nsm;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  *blocks = nsm * 8;
-  *threads = 256;
-  sfgb::fp64_probe_kernel<<<*blocks, *threads, 0, st>>>(16, 1.0, sink, 32);
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, st);
-  sfgb::fp64_probe_kernel<<<*blocks, *threads, 0, st>>>(iters, 1.0, sink, active_lanes);
-  cudaEventRecord(e1, st);
-  cudaEventSynchronize(e1);
-  cudaEventElapsedTime(ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    set_error(cudaGetErrorString(e));
-    return SF_ERR_CUDA;
-  }
-  return SF_OK;
-}
-}  // namespace
-
-extern "C" int sf_fp64_peak_probe(int iters, double *out_tflops, double *sink, void *stream)
-{
-  if (!out_tflops || !sink || iters < 1) {
-    set_error("sf_fp64_peak_probe: bad argument");
-    return SF_ERR_INVALID_ARGUMENT;
-  }
-  float ms = 0.f;
-  int blocks, threads;
-  const int rc = probe_ms(iters, 32, sink, (cudaStream_t)stream, &ms, &blocks, &threads);
-  if (rc) return rc;
-  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
-  *out_tflops = flops / (ms * 1e-3) / 1e12;
-  return SF_OK;
-}
-
-extern "C" int sf_fp64_issue_probe(int iters, int active_lanes, double *out_warp_instr_per_s, double *sink,
-                                   void *stream)
-{
-  if (!out_warp_instr_per_s || !sink || iters < 1 || active_lanes < 1 || active_lanes > 32) {
-    set_error("sf_fp64_issue_probe: bad argument");
-    return SF_ERR_INVALID_ARGUMENT;
-  }
-  float ms = 0.f;
-  int blocks, threads;
-  const int rc = probe_ms(iters, active_lanes, sink, (cudaStream_t)stream, &ms, &blocks, &threads);
-  if (rc) return rc;
-  const double warp_instr = 8.0 * (double)iters * blocks * (threads / 32);
-  *out_warp_instr_per_s = warp_instr / (ms * 1e-3);
-  return SF_OK;
-}

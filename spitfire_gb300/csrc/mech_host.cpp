@@ -28,8 +28,6 @@ HostMech::~HostMech()
   }
   if (d_blob) cudaFree(d_blob);
   if (d_status) cudaFree(d_status);
-  if (d_work_counter) cudaFree(d_work_counter);
-  if (tps_scratch) cudaFree(tps_scratch);
   for (cudaEvent_t e : events) cudaEventDestroy(e);
   if (copy_stream) cudaStreamDestroy(copy_stream);
 }
@@ -332,9 +330,29 @@ void HostMech::build(const sf_mech_desc *d)
   CUDA_THROW(cudaMemcpy(d_blob, bytes.data(), m.blob_bytes, cudaMemcpyHostToDevice));
   CUDA_THROW(cudaMalloc(&d_status, 16));
   CUDA_THROW(cudaMemset(d_status, 0, 16));
-  CUDA_THROW(cudaMalloc(&d_work_counter, 64));
-  CUDA_THROW(cudaMemset(d_work_counter, 0, 64));
   CUDA_THROW(cudaGetDevice(&device));
+  // every gather program the kernels use, built here so that no evaluation call builds or allocates one
+  for (int G : {1, 8, 16, 32}) build_programs(G);
+}
+
+const HostMech::Programs &HostMech::programs_for(int G) const
+{
+  auto it = programs.find(G);
+  if (it == programs.end()) throw sf_error(SF_ERR_INVALID_ARGUMENT, "no gather program for this lane width");
+  return it->second;
+}
+
+void ensure_dynamic_smem(const void *kernel, size_t bytes)
+{
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, size_t> set;
+  int dev;
+  CUDA_THROW(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cur = set[{kernel, dev}];
+  if (bytes <= cur) return;
+  CUDA_THROW(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
 }
 
 // ------------------------------------------------------------------------------------------ gather programs
@@ -417,10 +435,9 @@ std::vector<GatherItem> schedule(std::vector<Entry> &entries, int G, int *len_ou
 }
 }  // namespace
 
-const HostMech::Programs &HostMech::programs_for(int G)
+void HostMech::build_programs(int G)
 {
-  auto it = programs.find(G);
-  if (it != programs.end()) return it->second;
+  if (programs.count(G)) return;
   const int ns = dm.ns, nr = dm.nr;
   const ScratchLayout &L = sl;
   auto S = [](int idx) { return REF_SCRATCH | (uint32_t)idx; };
@@ -512,7 +529,7 @@ const HostMech::Programs &HostMech::programs_for(int G)
     if (!items.empty()) CUDA_THROW(cudaMemcpy(dptr, items.data(), items.size() * sizeof(GatherItem), cudaMemcpyHostToDevice));
     P.progs[k].items = dptr;
   }
-  return programs.emplace(G, std::move(P)).first->second;
+  programs.emplace(G, std::move(P));
 }
 
 }  // namespace sfgb

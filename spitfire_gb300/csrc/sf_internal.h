@@ -5,6 +5,7 @@
 #include <array>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -45,15 +46,11 @@ struct HostMech {
   std::vector<std::vector<int>> net_entry_of, slot_entry_of;
   void *d_blob = nullptr;
   int *d_status = nullptr;  // device error word of kernels using this mechanism
-  // work counter of the dynamically scheduled kernels (zeroed on the launching stream before each launch; like
-  // the scratch below it serves one stream at a time)
-  int *d_work_counter = nullptr;
   int device = 0;
   int tune[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // launch shapes chosen by the autotuner (sf_tune_knob), 0 = default
-  double *tps_scratch = nullptr;           // interleaved scratch of the thread-per-state kernels
-  size_t tps_scratch_bytes = 0;
   cudaStream_t copy_stream = nullptr;      // host-buffer entry points: device-to-host copies overlapping compute
   std::vector<cudaEvent_t> events;         // their chunk-completion events (created on first use)
+  std::mutex host_batch_mutex;             // serializes the host-buffer calls that share the two above
 
   struct Programs {
     DevProgram progs[4]{};  // 0: w only, 1: w/S_rho/S_T/P/Q, 2: Y block + T row, 3: all species rows (sens)
@@ -62,15 +59,24 @@ struct HostMech {
   std::map<int, Programs> programs;
 
   void build(const sf_mech_desc *d);
-  const Programs &programs_for(int G);
+  const Programs &programs_for(int G) const;  // the gather programs of lane width G (1, 8, 16 or 32), built by build()
   ~HostMech();
+
+ private:
+  void build_programs(int G);
 };
 
 // Launch helpers implemented in the .cu files (return an sf_status code).
 int launch_rates(const HostMech &m, int n, const double *T, const double *rho, const double *Y, double *w,
                  cudaStream_t st);
 void set_error(const std::string &msg);
-void ensure_tps_scratch(HostMech &m);
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current device, once per (kernel, device) and
+// size: cudaFuncSetAttribute is a host-side call the launchers would otherwise repeat on every launch.
+void ensure_dynamic_smem(const void *kernel, size_t bytes);
+// Thread-per-state chemistry kernels: warps that can be resident at once, and the bytes of interleaved scratch a
+// launch of n states takes (at most one slot per resident warp).
+size_t tps_resident_warps(const HostMech &hm);
+size_t tps_scratch_bytes(const HostMech &hm, int mode, long long n);
 
 }  // namespace sfgb
 

@@ -329,6 +329,9 @@ class FlameletBatch:
         self.rates_option = self.setups[0].rates_option
         self.diffterm = 4. * np.array([s.max_dissipation_rate for s in self.setups])
         self.zeros_dof = torch.zeros(self.npts * ns, dtype=torch.float64, device=dev)
+        # the Jacobian call's workspace (the eigenvalue kernel's work counter); a batch runs on one stream
+        self.jac_ws = torch.zeros(max(int(L.sf_flamelet_jac_workspace_size(h, 1)), 8) // 8, dtype=torch.float64,
+                                  device=dev)
 
     # ------------------------------------------------------------------------------------------ operations
     # Every operation takes `active`: None (all flamelets) or a bool tensor [nf]; flamelets outside it are left
@@ -369,7 +372,8 @@ class FlameletBatch:
         try:
             N.check(N.load().sf_flamelet_jac_batch(self.g.handle, C.byref(self.fb), N.ptr(state), self.rates_option,
                                                    int(scale_and_offset), float(prefactor), float(diffterm),
-                                                   N.ptr(expeig), N.ptr(self.values), N.stream_handle()))
+                                                   N.ptr(expeig), N.ptr(self.values), N.ptr(self.jac_ws),
+                                                   self.jac_ws.numel() * 8, N.stream_handle()))
         finally:
             self.fb.active = None
             self.fb.diffterm = None
