@@ -9,7 +9,7 @@ complete-combustion profile; spitfire_gb300.workloads.gri_states). One step = on
   e2e        states/s through the public API with host buffers: every step copies the states host->device (pinned)
              and the RHS + Jacobian device->host, inside the timed region
   roofline   the kernel is FP64-pipe bound: achieved = executed FP64 flops per state (counted by ncu, see
-             profiles/) x states / kernel time, peak = FP64 FMA throughput measured live by sf_fp64_peak_probe
+             profiles/) x states / kernel time, peak = FP64 FMA throughput measured live by bench_probes.cu
   cpu_baseline / --impl reference: the oracle (C++ restatement of Griffon, OpenMP over all host cores) on the
              same states
 
@@ -52,7 +52,7 @@ N_REACTORS = 8192
 N_FLAMELETS = 64
 N_ADJOINT = 2048
 # Per GRI state of each Jacobian kernel the autotuner can choose, from ncu on the profiling cases
-# (python -m spitfire_gb300.profile_cases jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA),
+# (python bench.py --profile-case jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA),
 # warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states) and DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum / states; the 8192-state case of the lane-group kernel keeps part of
 # its Jacobians in L2 at the end, so its figure is a lower bound).
@@ -526,6 +526,227 @@ def bench_adjoint(spec, rank, stream, cpu):
     return res
 
 
+# ---------------------------------------------------------------------------------------------- FP64 probes
+# bench_probes.cu (beside this file) holds the FP64 throughput probes, compiled on their own into _build/: they are
+# measurement code, not part of the library.
+_PROBES = None
+
+
+def build_probes():
+    """Compile bench_probes.cu for sm_103a into _build/libbench_probes.so (skipped when up to date)."""
+    import hashlib
+    from spitfire_gb300 import build as B
+    src = os.path.join(ROOT, 'bench_probes.cu')
+    out_dir = os.path.join(ROOT, '_build')
+    lib = os.path.join(out_dir, 'libbench_probes.so')
+    stamp = lib + '.stamp'
+    h = hashlib.sha256(open(src, 'rb').read() + ' '.join(B.ARCH).encode() + os.uname().machine.encode()).hexdigest()
+    if os.path.exists(lib) and os.path.exists(stamp) and open(stamp).read() == h:
+        return lib
+    os.makedirs(out_dir, exist_ok=True)
+    subprocess.check_call([B.nvcc(), '-shared', '-Xcompiler', '-fPIC', '-O3', '-lineinfo', *B.ARCH, src,
+                           '-o', lib + '.tmp'])
+    os.replace(lib + '.tmp', lib)
+    with open(stamp, 'w') as f:
+        f.write(h)
+    return lib
+
+
+def _probes():
+    global _PROBES
+    if _PROBES is None:
+        import ctypes as C
+        L = C.CDLL(build_probes())
+        L.bench_fp64_fma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p,
+                                     C.c_void_p]
+        L.bench_fp64_dmma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        _PROBES = L
+    return _PROBES
+
+
+def fp64_fma_probe(iters, active_lanes=32):
+    """(TFLOP/s of the active lanes, warp FP64 instructions/s) of register FMA chains on every SM."""
+    import ctypes as C
+    import torch
+    sink = torch.zeros(1, dtype=torch.float64, device='cuda')
+    tf, wi = C.c_double(), C.c_double()
+    rc = _probes().bench_fp64_fma(int(iters), int(active_lanes), C.byref(tf), C.byref(wi), sink.data_ptr(),
+                                  torch.cuda.current_stream().cuda_stream)
+    if rc:
+        raise RuntimeError(f'bench_fp64_fma failed ({rc})')
+    return tf.value, wi.value
+
+
+def fp64_dmma_probe(iters, which=0):
+    """TFLOP/s of FP64 mma.sync (which 0: m8n8k4, 1: m16n8k16) with independent accumulators on every SM."""
+    import ctypes as C
+    import torch
+    sink = torch.zeros(1, dtype=torch.float64, device='cuda')
+    tf = C.c_double()
+    rc = _probes().bench_fp64_dmma(int(iters), int(which), C.byref(tf), sink.data_ptr(),
+                                   torch.cuda.current_stream().cuda_stream)
+    if rc:
+        raise RuntimeError(f'bench_fp64_dmma failed ({rc})')
+    return tf.value
+
+
+# ---------------------------------------------------------------------------------------------- profiling cases
+# Small, self-contained runs of each kernel family for ncu and quick checks:  python bench.py --profile-case <case>
+#   jac        isochoric RHS + Jacobian of 8192 GRI-3.0 states (chem_kernel MODE_JAC), 3 launches
+#   jac_tps    the same with the thread-per-state kernel (chem_kernel_tps MODE_JAC) at 2 resident 4-warp blocks
+#              per SM, on 38912 states (one warp batch per resident warp), 2 launches
+#   rates_rhs  production rates (chem_kernel_tps MODE_RATES) and the isochoric right-hand side (MODE_RHS) of 38912
+#              states, thread per state at 2 resident 4-warp blocks per SM, 2 launches each
+#   integrate_2048  2048 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s with the
+#              autotuner's shape (Griffon scratch in global slots, 6 warps per block)
+#   integrate  256 isobaric reactors of the batched-ignition distribution to ignition or 0.1 s (integrate_kernel)
+#   flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
+#              block-Thomas factorization, solve and matvec
+#   adjoint    64 reactors of the adjoint distribution recorded to 1 ms, then the batched adjoint
+#   fp64issue  warp-level FP64 FMA instructions per second with 1, 2, 4, 8, 16 and 32 active lanes per warp
+#   dmma       FP64 mma.sync (m8n8k4, m16n8k16) throughput beside the DFMA pipe's
+def _spec():
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    return ChemicalMechanismSpec.bundled('methane-gri30')
+
+
+def case_jac():
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    q = torch.tensor(W.isochoric_state(W.gri_states(spec, 8192)), device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(3):
+        spec.griffon.reactor_jac_batch(P, q, 0)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_jac_tps():
+    import torch
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    AT.set_tuning(spec, 'tps_ctas', 2)
+    AT.set_tuning(spec, 'group_jac', 1)
+    n = torch.cuda.get_device_properties(0).multi_processor_count * 2 * 4 * 32
+    q = torch.tensor(W.isochoric_state(W.gri_states(spec, n)), device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(2):
+        spec.griffon.reactor_jac_batch(P, q, 0)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_rates_rhs():
+    import torch
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    spec = _spec()
+    AT.set_tuning(spec, 'tps_ctas', 2)
+    AT.set_tuning(spec, 'group_rates', 1)
+    AT.set_tuning(spec, 'group_rhs', 1)
+    n = torch.cuda.get_device_properties(0).multi_processor_count * 2 * 4 * 32
+    d = W.gri_states(spec, n)
+    g = spec.griffon
+    q = torch.tensor(W.isochoric_state(d), device='cuda')
+    T = torch.tensor(d['T'], device='cuda')
+    rho = torch.tensor(d['rho'], device='cuda')
+    Y = torch.tensor(d['Y'], device='cuda')
+    P = reactor_params('isochoric')
+    for _ in range(2):
+        g.production_rates_batch(T, rho, Y)
+    for _ in range(2):
+        g.reactor_rhs_batch(P, q)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_integrate():
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec = _spec()
+    d = W.ignition_batch(spec, 256, seed=1003)
+    BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                          stop_at_time=0.1)
+    return spec
+
+
+def case_integrate_2048():
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec = _spec()
+    AT.set_tuning(spec, 'integrate_scratch', 1)
+    AT.set_tuning(spec, 'integrate_warps', 6)
+    d = W.ignition_batch(spec, 2048, seed=1003)
+    BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
+                                          stop_at_time=0.1)
+    return spec
+
+
+def case_flamelet():
+    import torch
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.flamelet import FlameletBatch
+    spec = _spec()
+    setups = W.slfm_flamelet_setups(spec, 8, seed=1004, nz_range=(64, 120))
+    b = FlameletBatch(setups)
+    x = b.initial_state()
+    y = b.rhs(x)
+    b.jacobian(x, eig=True, diffterm_per_flamelet=b.diffterm_tensor())
+    b.factor()
+    b.solve(y)
+    b.matvec(x)
+    torch.cuda.synchronize()
+    return spec
+
+
+def case_adjoint():
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.adjoint import ReactorAdjoint
+    spec = _spec()
+    d = W.adjoint_batch(spec, 64, seed=1005)
+    adj = ReactorAdjoint(spec, 'isobaric')
+    tr = adj.forward(d['q0'], pressures=d['p'], t_end=1.e-3)
+    g = adj.backward(tr)
+    assert bool(np.isfinite(g['theta'].cpu().numpy()).all())
+    return spec
+
+
+def case_fp64issue():
+    for lanes in (1, 2, 4, 8, 16, 32):
+        tf, wi = fp64_fma_probe(4000, lanes)
+        print(f'active lanes {lanes:2d}: {wi:.4e} warp FP64 FMA instructions/s, {tf:.3f} TFLOP/s of useful lanes')
+    return None
+
+
+def case_dmma():
+    tf, _ = fp64_fma_probe(20000, 32)
+    print(f'FP64 FMA (DFMA pipe), all lanes: {tf:.3f} TFLOP/s')
+    for which, name in ((0, 'm8n8k4'), (1, 'm16n8k16')):
+        print(f'FP64 mma.sync {name}: {fp64_dmma_probe(2000 if which == 0 else 500, which):.3f} TFLOP/s')
+    return None
+
+
+PROFILE_CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs,
+                 'integrate_2048': case_integrate_2048, 'integrate': case_integrate, 'flamelet': case_flamelet,
+                 'adjoint': case_adjoint, 'fp64issue': case_fp64issue, 'dmma': case_dmma}
+
+
+def run_profile_case(name):
+    import numpy as np  # noqa: F401  (the cases use it)
+    from spitfire_gb300 import build
+    build.build()
+    spec = PROFILE_CASES[name]()
+    status = spec.griffon.device_status() if spec is not None else 0
+    print(f'{name}: done, device status {status}')
+    return 0 if status == 0 else 1
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle C++ restatement of Griffon on the host cores (the reference's own code path
     cannot run on the GPU machine: it is not present there)."""
@@ -563,7 +784,10 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    ap.add_argument('--profile-case', choices=sorted(PROFILE_CASES), help='run one profiling case and exit')
     args = ap.parse_args()
+    if args.profile_case:
+        sys.exit(run_profile_case(args.profile_case))
     rank, world, local = dist_env()
     if args.impl == 'reference':
         if world > 1:
@@ -675,19 +899,16 @@ def main():
     del ws
 
     # ---------------- roofline (FP64 pipe)
-    sink = torch.zeros(1, dtype=torch.float64, device=dev)
-    import ctypes as C
-    peak = C.c_double()
-    N.check(N.load().sf_fp64_peak_probe(20000, C.byref(peak), N.ptr(sink), N.stream_handle()))
+    peak_tflops, issue_peak = fp64_fma_probe(20000, 32)
     dense = griffon_dense_flops(spec)
     algo = kern['flops']
-    roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': peak.value,
-            'peak_source': 'measured live by sf_fp64_peak_probe (FP64 FMA chains on every SM); the measured-peaks '
-                           'file has no FP64 figure',
+    roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': peak_tflops,
+            'peak_source': 'measured live by bench_probes.cu bench_fp64_fma (FP64 FMA chains on every SM); the '
+                           'measured-peaks file has no FP64 figure',
             'kernel': kern['kernel']}
     if algo:
         roof['achieved'] = algo * N_STATES / (ms * 1e-3) / 1e12
-        roof['frac'] = roof['achieved'] / peak.value
+        roof['frac'] = roof['achieved'] / peak_tflops
         roof['flops_per_state'] = algo
     else:
         roof['achieved'] = None
@@ -695,13 +916,11 @@ def main():
     # DRAM bytes of one launch: the ncu figure per state times the states of a launch
     roof['traffic'] = kern['dram_bytes'] * N_STATES if kern.get('dram_bytes') else None
     roof['traffic_source'] = 'ncu dram__bytes_read.sum + dram__bytes_write.sum per state on the profiling case ' \
-                             '(python -m spitfire_gb300.profile_cases jac_tps | jac), scaled to the launch'
-    issue = C.c_double()
-    N.check(N.load().sf_fp64_issue_probe(4000, 32, C.byref(issue), N.ptr(sink), N.stream_handle()))
+                             '(python bench.py --profile-case jac_tps | jac), scaled to the launch'
     if kern['warp_instr']:
         ach_issue = kern['warp_instr'] * N_STATES / (ms * 1e-3)
         roof['fp64_issue'] = {'unit': 'warp FP64 instructions/s', 'per_state': kern['warp_instr'],
-                              'achieved': ach_issue, 'peak': issue.value, 'frac': ach_issue / issue.value,
+                              'achieved': ach_issue, 'peak': issue_peak, 'frac': ach_issue / issue_peak,
                               'note': 'GB300 charges FP64 per warp instruction whatever the active lanes; this is '
                                       'the pipe-occupancy roofline, the TFLOP/s one above counts useful lanes'}
     roof['griffon_dense_flops_per_state'] = dense

@@ -1,0 +1,154 @@
+// FP64 throughput probes of bench.py: the roofline denominators for the FP64 kernels (the measured-peaks file of
+// this pool holds HBM and bf16 figures only). Not part of the library: bench.py compiles this file on its own
+// (bench.build_probes) and loads it with ctypes.
+//
+//   bench_fp64_fma    independent register FMA chains (8 per thread, no memory traffic) on every SM, with
+//                     `active_lanes` (1..32) lanes of every warp working: FP64 FMA throughput, and warp-level FP64
+//                     instructions per second (equal rates for every lane count mean FP64 work is charged per warp
+//                     instruction, whatever the number of active lanes)
+//   bench_fp64_dmma   the same with the legacy FP64 tensor path, mma.sync .f64 (m8n8k4: 512 flops per warp
+//                     instruction; m16n8k16: 4096), independent accumulators per warp: whether the FP64 MMA pipe
+//                     beats the DFMA pipe for the small dense block updates of the LU and Gauss-Jordan kernels
+//
+// Each launch covers 8 blocks of 256 threads per SM after a short warm-up launch, timed with CUDA events on the
+// caller's stream (which the call synchronizes). Every loop is register-only with a fixed trip count.
+#include <cuda_runtime.h>
+
+namespace {
+
+__global__ void fma_probe_kernel(int iters, double seed, double *sink, int active_lanes)
+{
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + k * 1e-3 + threadIdx.x * 1e-7;
+  const double b = 0.999999999, c = 1e-9;
+  if ((int)(threadIdx.x & 31) < active_lanes)
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+  double s = 0.;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == 12345.678) sink[0] = s;  // keeps the chains live
+}
+
+// m8n8k4: A one double per lane, B one, C/D two; eight independent accumulators per warp.
+__global__ void dmma_m8n8k4_kernel(int iters, double seed, double *sink)
+{
+  const double a = 1e-3 * (seed + threadIdx.x * 1e-7), b = 1e-3 * (0.999 - threadIdx.x * 1e-9);
+  double c[8][2];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = k * 1e-6;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                   : "+d"(c[k][0]), "+d"(c[k][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
+  if (s == 12345.678) sink[0] = s;
+}
+
+// m16n8k16: A eight doubles per lane, B four, C/D four; four independent accumulators per warp.
+__global__ void dmma_m16n8k16_kernel(int iters, double seed, double *sink)
+{
+  const double a = 1e-4 * (seed + threadIdx.x * 1e-7), b = 1e-4 * (0.999 - threadIdx.x * 1e-9);
+  double c[4][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) c[k][j] = (k + j) * 1e-6;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      asm volatile("mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+                   "{%4,%4,%4,%4,%4,%4,%4,%4}, {%5,%5,%5,%5}, {%0,%1,%2,%3};"
+                   : "+d"(c[k][0]), "+d"(c[k][1]), "+d"(c[k][2]), "+d"(c[k][3])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s += c[k][0] + c[k][1] + c[k][2] + c[k][3];
+  if (s == 12345.678) sink[0] = s;
+}
+
+template <class L>
+int timed(cudaStream_t st, L launch, float *ms)
+{
+  launch(16);  // warm-up
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return 1;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return 1;
+  }
+  cudaEventRecord(e0, st);
+  launch(-1);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+void shape(int *blocks, int *threads)
+{
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  *blocks = nsm * 8;
+  *threads = 256;
+}
+
+}  // namespace
+
+extern "C" {
+
+// TFLOP/s of the active lanes and warp-level FP64 instructions per second.
+int bench_fp64_fma(int iters, int active_lanes, double *out_tflops, double *out_warp_instr_per_s, double *sink,
+                   void *stream)
+{
+  if (iters < 1 || active_lanes < 1 || active_lanes > 32 || !out_tflops || !out_warp_instr_per_s || !sink) return 2;
+  int blocks, threads;
+  shape(&blocks, &threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  float ms = 0.f;
+  const int rc = timed(st, [&](int it) {
+    fma_probe_kernel<<<blocks, threads, 0, st>>>(it < 0 ? iters : it, 1.0, sink, it < 0 ? active_lanes : 32);
+  }, &ms);
+  if (rc) return rc;
+  const double warp_instr = 8.0 * (double)iters * blocks * (threads / 32);
+  *out_warp_instr_per_s = warp_instr / (ms * 1e-3);
+  *out_tflops = 2.0 * warp_instr * active_lanes / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+// TFLOP/s of FP64 mma.sync, shape 0 = m8n8k4, 1 = m16n8k16.
+int bench_fp64_dmma(int iters, int which, double *out_tflops, double *sink, void *stream)
+{
+  if (iters < 1 || (which != 0 && which != 1) || !out_tflops || !sink) return 2;
+  int blocks, threads;
+  shape(&blocks, &threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  float ms = 0.f;
+  const int rc = timed(st, [&](int it) {
+    const int n = it < 0 ? iters : it;
+    if (which == 0)
+      dmma_m8n8k4_kernel<<<blocks, threads, 0, st>>>(n, 1.0, sink);
+    else
+      dmma_m16n8k16_kernel<<<blocks, threads, 0, st>>>(n, 1.0, sink);
+  }, &ms);
+  if (rc) return rc;
+  const double per_instr = which == 0 ? 2.0 * 8 * 8 * 4 : 2.0 * 16 * 8 * 16;
+  const double chains = which == 0 ? 8.0 : 4.0;
+  const double flops = per_instr * chains * (double)iters * blocks * (threads / 32);
+  *out_tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+}  // extern "C"

@@ -524,7 +524,7 @@ void rates_sens(const Mech &m, double T, double rho, double mmw, const double *y
   const int ns = m.ns, nsp1 = ns + 1;
   const double invT = 1. / T, logT = std::log(T), invM = 1. / mmw, ct = rho * invM;
   const double invRu = 1. / m.Ru;
-  std::vector<double> g(ns), dB(ns), dRdY(ns), dCdY(ns);
+  std::vector<double> g(ns), dB(ns), dRdY(ns), dCdY(ns), dqdY(ns);
   gibbs(m, T, g.data(), dB.data());
   for (int i = 0; i < ns; ++i) w[i] = 0.;
   for (int i = 0; i < nsp1 * nsp1; ++i) S[i] = 0.;
@@ -675,16 +675,16 @@ void rates_sens(const Mech &m, double T, double rho, double mmw, const double *y
     const double q = Rnet * Ctbaf;
     const double dqdrho = dRdrho * Ctbaf + (tbaf ? dCdrho * Rnet : 0.);
     const double dqdT = dRdT * Ctbaf + (tbaf ? dCdT * Rnet : 0.);
+    // dq/dY once per reaction (rates_sensitivities_exact.cpp:1001-1010), then scattered to each net species
+    for (int s = 0; s < ns - 1; ++s) dqdY[s] = dRdY[s] * Ctbaf + (tbaf ? dCdY[s] * Rnet : 0.);
     for (size_t i = 0; i < x.net.size(); ++i) {
       const int idx = x.net[i];
       const double f = -x.net_nu[i] * x.net_mw[i];
       w[idx] += f * q;
       S[idx] += f * dqdrho;
       S[idx + nsp1] += f * dqdT;
-      for (int s = 0; s < ns - 1; ++s) {
-        const double dq = dRdY[s] * Ctbaf + (tbaf ? dCdY[s] * Rnet : 0.);
-        S[idx + 2 * nsp1 + nsp1 * s] += f * dq;
-      }
+      double *Sc = S + idx + 2 * nsp1;
+      for (int s = 0; s < ns - 1; ++s) Sc[nsp1 * s] += f * dqdY[s];
     }
   }
 }

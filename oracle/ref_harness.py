@@ -23,7 +23,7 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get('SPITFIRE_REFERENCE', '/root/reference')
+REF_ROOT = os.environ.get('SPITFIRE_REFERENCE')  # the reference checkout (tests/golden/make_golden.py sets it)
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -49,6 +49,8 @@ def load_reference():
     """Import the reference modules; returns a namespace with griffon, odesolve, HomogeneousReactor, Flamelet, ..."""
     if _loaded:
         return _loaded['ns']
+    if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, 'src', 'spitfire')):
+        raise FileNotFoundError('set SPITFIRE_REFERENCE to a checkout of the reference Spitfire')
     src = os.path.join(REF_ROOT, 'src', 'spitfire')
     for pkg in ('spitfire', 'spitfire.time', 'spitfire.chemistry', 'spitfire.griffon'):
         m = types.ModuleType(pkg)

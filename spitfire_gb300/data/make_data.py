@@ -38,4 +38,6 @@ def convert(src_dir):
 
 
 if __name__ == '__main__':
-    convert(sys.argv[1] if len(sys.argv) > 1 else '/root/reference/tests/test_mechanisms')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python -m spitfire_gb300.data.make_data <reference checkout>/tests/test_mechanisms')
+    convert(sys.argv[1])

@@ -44,7 +44,7 @@ the reference's Python modules, loaded by oracle/ref_harness.py). The fixtures p
   reference_<name>_gold.pkl  byte copies of the reference's pickled gold libraries
                        (tests/tabulation/<name>/gold.pkl): the reader of reference-written libraries is tested on them
 
-Usage:  python tests/golden/make_golden.py [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
+Usage:  python tests/golden/make_golden.py --reference PATH [kernels] [ignition] [gold] [flamelets] [open] [nonadiabatic]
                                            [transient] [structure] [unstrained] [dropin] [libraries]
 """
 import json
@@ -59,8 +59,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 sys.path.insert(0, os.path.join(ROOT, 'tests'))
-REF = os.environ.get('SPITFIRE_REFERENCE', '/root/reference')
-MECHS = os.path.join(REF, 'tests', 'test_mechanisms')
+REF = None     # the reference checkout: --reference PATH, or SPITFIRE_REFERENCE
+MECHS = None
 
 
 def seeded_states(spec, n, seed):
@@ -661,7 +661,16 @@ def libraries():
 
 
 if __name__ == '__main__':
-    what = sys.argv[1:] or ['kernels', 'ignition', 'gold', 'flamelets']
+    args = sys.argv[1:]
+    if '--reference' in args:
+        i = args.index('--reference')
+        os.environ['SPITFIRE_REFERENCE'] = args[i + 1]
+        del args[i:i + 2]
+    REF = os.environ.get('SPITFIRE_REFERENCE')
+    if not REF or not os.path.isdir(os.path.join(REF, 'tests', 'test_mechanisms')):
+        sys.exit('give the reference checkout: --reference PATH (or set SPITFIRE_REFERENCE)')
+    MECHS = os.path.join(REF, 'tests', 'test_mechanisms')
+    what = args or ['kernels', 'ignition', 'gold', 'flamelets']
     if 'flamelets' in what:
         slfm_gold()
         flamelets()
