@@ -49,11 +49,12 @@ def btddod_row_err(a, b, nzi, ns):
     return float((num / np.maximum(den, 1e-300)).max())
 
 
-def vec_err(a, b, ns):
-    """Per-variable relative error of point-major vectors: |a - b| over the largest |b| of that variable."""
+def vec_err(a, b, ns, floor=1e-300):
+    """Per-variable relative error of point-major vectors: |a - b| over the largest |b| of that variable (at least
+    `floor`)."""
     a = np.asarray(a).reshape(-1, ns)
     b = np.asarray(b).reshape(-1, ns)
-    return float((np.abs(a - b).max(0) / np.maximum(np.abs(b).max(0), 1e-300)).max())
+    return float((np.abs(a - b).max(0) / np.maximum(np.abs(b).max(0), floor)).max())
 
 
 def eig_err(e, ref, op, state):
