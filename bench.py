@@ -166,7 +166,7 @@ def _ignite_one(args):
         _ignite_one.og = g
     r = I.integrate(I.ReactorProblem(g, 'isobaric', pressure=p), q0, delta_temperature_ignition=400.,
                     stop_at_time=0.1)
-    return r['t'], r['status'], r['steps']
+    return r['t'], r['status'], r['steps'], r['t_interp']
 
 
 def _worker_init(root):
@@ -190,7 +190,7 @@ def cpu_ignitions(q0, p, n_sample, seconds=30.0):
                 break
         dt = time.perf_counter() - t0
         pool.terminate()
-    return len(res) / dt, cores, [r[0] for r in res], [r[1] for r in res], dt
+    return len(res) / dt, cores, [r[0] for r in res], [r[1] for r in res], dt, [r[3] for r in res]
 
 
 def _flamelet_one(args):
@@ -322,6 +322,7 @@ def bench_ignition(spec, rank, stream, cpu):
     e1.synchronize()
     ms = max_over_ranks(e0.elapsed_time(e1))
     tau = out['t'].cpu().numpy()
+    tau_i = out['t_interp'].cpu().numpy()
     status = out['status'].cpu().numpy()
     steps = out['counts'][:, 0].cpu().numpy()
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -330,6 +331,7 @@ def bench_ignition(spec, rank, stream, cpu):
            'status_counts': {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
            'steps': {'min': int(steps.min()), 'median': float(np.median(steps)), 'max': int(steps.max())},
            'device_status': spec.griffon.device_status(),
+           'tau_interpolated': _tau_interp_summary(tau, tau_i, status),
            'autotune': {'chosen': {'placement': PLACEMENT[best[0]], 'warps_per_block': best[1]},
                         'candidates_ms_1024_reactors': {f'{PLACEMENT[k[0]]}/{k[1]}w': v for k, v in cand.items()}}}
     # comparison point: the plain single-state GPU form (one thread per reactor, same step logic) on the same batch
@@ -359,16 +361,185 @@ def bench_ignition(spec, rank, stream, cpu):
                               'tau_rel_err_vs_fp64_median': float(np.median(rel32))}
     if cpu:
         n_s = 256
-        rate, cores, t_cpu, st_cpu, dt = cpu_ignitions(d['q0'], d['p'], n_s, seconds=30.)
+        rate, cores, t_cpu, st_cpu, dt, ti_cpu = cpu_ignitions(d['q0'], d['p'], n_s, seconds=30.)
         k = len(t_cpu)
         both = [i for i in range(k) if st_cpu[i] == 2 and status[i] == 2]
         rel = [abs(tau[i] - t_cpu[i]) / t_cpu[i] for i in both]
+        rel_i = [abs(tau_i[i] - ti_cpu[i]) / ti_cpu[i] for i in both if ti_cpu[i] is not None]
+        res['tau_interpolated']['rel_err_vs_oracle_max'] = max(rel_i) if rel_i else None
         res['cpu_baseline'] = {'value': rate, 'unit': 'ignitions/s', 'cores': cores, 'kind': 'port',
                                'sample': f'oracle integrator (ESDIRK64 + Newton + PI restated, C++ kernels) on the '
                                          f'first {k} reactors, spawned pool, {dt:.1f} s'}
         res['tau_rel_err_vs_oracle'] = {'reactors_compared': len(both), 'max': max(rel) if rel else None,
                                         'status_mismatches': int(sum(st_cpu[i] != status[i] for i in range(k)))}
     return res
+
+
+N_H2 = 4096
+
+
+def bench_h2(rank, stream, cpu):
+    """The small-mechanism workload: h2-burke isochoric RHS + analytical Jacobian on 4096 seeded states (T ~ U(800,
+    2500) K, 1 atm, Y = 0.5 Dir(0.5) over the nine named species + 0.5 N2), L2 flushed between steps; and one ESDIRK64
+    ignition of stoichiometric H2/air (H2:O2:N2 = 2:1:3.76) from 1200 K at 1 atm to t = 1e-3 s, isochoric and
+    isobaric, against the oracle integrator."""
+    import numpy as np
+    import torch
+    import integrate as I
+    import oracle as orc
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    from spitfire_gb300.reactors import BatchIntegrator
+    spec = ChemicalMechanismSpec.bundled('h2-burke')
+    g = spec.griffon
+    dev = torch.device('cuda', torch.cuda.current_device())
+    d = W.h2_states(spec, N_H2, seed=1001 + rank)
+    qh = W.isochoric_state(d)
+    q = torch.tensor(qh, device=dev)
+    neq = q.shape[1]
+    P = reactor_params('isochoric')
+    tuned = AT.tune_chemistry(spec, qh, kinds=('jac',))
+    rhs = torch.empty_like(q)
+    J = torch.empty((N_H2, neq * neq), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        g.reactor_jac_batch(P, q, 0, out_rhs=rhs, out_jac=J)
+    for _ in range(5):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(20):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = max_over_ranks(statistics.mean(times))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    hbm, hbm_src = measured_peaks()
+    per_state = (neq + neq + neq * neq) * 8
+    ach = per_state * N_H2 / (ms * 1e-3) / 1e9
+    res = {'workload': f'h2-burke (11 species, 27 reactions) isochoric RHS + analytical Jacobian, {N_H2} states',
+           'value': world * N_H2 / (ms * 1e-3), 'unit': 'states/s', 'ms': ms,
+           'l2': 'flushed between steps (256 MB write outside the timed events)',
+           'autotune': {'group_jac': tuned['group_jac'][0]},
+           'roofline': {'bound': 'hbm', 'algorithmic_bytes_per_state': per_state, 'achieved': ach, 'peak': hbm,
+                        'unit': 'GB/s', 'frac': ach / hbm, 'peak_source': hbm_src,
+                        'note': '4096 states are 5.5 MB of output: one launch of a few microseconds, so the time '
+                                'is launch and ramp-up latency, not bandwidth'}}
+    # the plain single-state GPU form on the same states
+    from spitfire_gb300 import _native as N
+    wsp = torch.empty(N.load().sf_reactor_jac_plain_workspace_size(g.handle, N_H2) // 8 + 1, dtype=torch.float64,
+                      device=dev)
+    plain_ms = sorted(_timed(lambda: g.reactor_jac_plain_batch(P, q, workspace=wsp), stream) for _ in range(3))[1]
+    res['plain_gpu_form'] = {'value': world * N_H2 / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
+                             'speedup_batched_over_plain': plain_ms / ms}
+    # one stoichiometric H2/air ignition from 1200 K at 1 atm to t = 1e-3 s
+    X = np.zeros(spec.n_species)
+    X[spec.species_index('H2')], X[spec.species_index('O2')], X[spec.species_index('N2')] = 2., 1., 3.76
+    Y = X * spec.molecular_weights
+    Y /= Y.sum()
+    og = orc.OracleGriffon()
+    spec._populate_griffon(og)
+    orc.set_threads(1)
+    ign = {}
+    for conf in ('isochoric', 'isobaric'):
+        if conf == 'isobaric':
+            q0 = np.hstack([[1200.], Y[:-1]])[None, :]
+        else:
+            rho = 101325. / (Y / spec.molecular_weights).sum() / (8314.46261815324 * 1200.)
+            q0 = np.hstack([[rho, 1200.], Y[:-1]])[None, :]
+        bi = BatchIntegrator(spec, conf, pressure=101325.)
+        bi.run(q0, stop_at_time=1.e-3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = bi.run(q0, stop_at_time=1.e-3)
+        torch.cuda.synchronize()
+        gpu_s = time.perf_counter() - t0
+        qf = out['q'].cpu().numpy()[0]
+        steps = int(out['counts'][0, 0].item())
+        prob = I.ReactorProblem(og, conf, pressure=101325.)
+        t0 = time.perf_counter()
+        r = I.integrate(prob, q0[0], stop_at_time=1.e-3)
+        cpu_s = time.perf_counter() - t0
+        Ti = 1 if conf == 'isochoric' else 0
+        ign[conf] = {'gpu_seconds': gpu_s, 'steps': steps, 'T_end': float(qf[Ti]),
+                     'oracle_steps': int(r['steps']), 'oracle_seconds_1core': cpu_s,
+                     'T_end_rel_err_vs_oracle': float(abs(qf[Ti] - r['state'][Ti]) / r['state'][Ti]),
+                     'note': 'one reactor is one warp on one SM: a latency figure, not a throughput one'}
+    res['ignition_1200K_to_1ms'] = ign
+    if cpu:
+        og2 = orc.OracleGriffon()
+        spec._populate_griffon(og2)
+        cores = os.cpu_count()
+        orc.set_threads(cores)
+        P2 = reactor_params('isochoric')
+        yin = np.zeros(spec.n_species)
+        P2.inflow_Y = orc._p(yin)
+        og2.reactor_jac_batch(P2, qh[:256], 0)
+        t0 = time.perf_counter()
+        done = 0
+        while time.perf_counter() - t0 < 5.:
+            og2.reactor_jac_batch(P2, qh, 0)
+            done += N_H2
+        dt = time.perf_counter() - t0
+        res['cpu_baseline'] = {'value': done / dt, 'unit': 'states/s', 'cores': cores, 'kind': 'port',
+                               'sample': f'{done} h2-burke isochoric RHS+Jacobian evaluations (passes over the '
+                                         f'{N_H2} benchmark states) in {dt:.1f} s'}
+    del flush, J, wsp
+    torch.cuda.empty_cache()
+    return res
+
+
+def _flamelet_time_split(setups):
+    """A second, instrumented solve of the same batch: the GPU time of each batched operation (CUDA events around
+    every call of the solvers) against the wall time; the rest is host-side control (masks, norms, convergence
+    tests and the synchronizations they need)."""
+    import torch
+    from spitfire_gb300.flamelet import FlameletBatch
+    b = FlameletBatch(setups)
+    rec = {}
+    for name in ('rhs', 'jacobian', 'factor', 'solve', 'scale_and_add_diagonal'):
+        f = getattr(b, name)
+
+        def wrap(*a, _f=f, _n=name, **kw):
+            key = _n + ('_eig' if kw.get('eig') else '')
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = _f(*a, **kw)
+            e1.record()
+            rec.setdefault(key, []).append((e0, e1))
+            return r
+        setattr(b, name, wrap)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.compute_steady_state()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ops = {k: {'calls': len(v), 'seconds': sum(a.elapsed_time(e) for a, e in v) * 1e-3} for k, v in rec.items()}
+    gpu = sum(o['seconds'] for o in ops.values())
+    return {'wall_s': wall, 'batched_ops_s': gpu, 'host_control_s': wall - gpu, 'ops': ops,
+            'note': 'instrumented second solve; kernels between the timed operations (torch masks, norms) count as '
+                    'host control'}
+
+
+def _tau_interp_summary(tau, tau_i, status):
+    """How far the step-end ignition delays (the reference's measure) sit from the Hermite-interpolated crossing."""
+    import numpy as np
+    ign = (status == 2) & np.isfinite(tau_i)
+    rel = (tau[ign] - tau_i[ign]) / tau_i[ign]
+    return {'reactors': int(ign.sum()),
+            'step_end_minus_interpolated_rel': {'median': float(np.median(rel)) if rel.size else None,
+                                                'max': float(rel.max()) if rel.size else None},
+            'note': 'the delay as the end of the accepted step that first has T > T0 + 400 K (the reference\'s '
+                    'measure, reactors.py:774-790) against the time the cubic Hermite interpolant over that step '
+                    'crosses T0 + 400 K'}
 
 
 def bench_flamelet(spec, rank, stream, cpu):
@@ -436,6 +607,7 @@ def bench_flamelet(spec, rank, stream, cpu):
         'factor': {'bound': 'fp64 (critical path: the longest flamelet)', 'flops_per_point': 2. * ns ** 3,
                    'achieved_tflops': fac_flops / (k['factor_ms'] * 1e-3) / 1e12}}
     res['kernels'] = k
+    res['time_split'] = _flamelet_time_split(setups)
     if cpu:
         idx = list(range(0, N_FLAMELETS, 4))
         done, cores, dt = cpu_flamelets(setups, idx, seconds=60.)
@@ -560,6 +732,7 @@ def _probes():
         L.bench_fp64_fma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p,
                                      C.c_void_p]
         L.bench_fp64_dmma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        L.bench_store.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_double), C.c_void_p]
         _PROBES = L
     return _PROBES
 
@@ -590,6 +763,18 @@ def fp64_dmma_probe(iters, which=0):
     return tf.value
 
 
+def store_probe(t, pattern):
+    """GB/s of kernel stores into the tensor t (CUDA, or pinned CPU memory written over the host link)."""
+    import ctypes as C
+    import torch
+    gbs = C.c_double()
+    rc = _probes().bench_store(C.c_void_p(t.data_ptr()), t.numel() * t.element_size(), int(pattern), C.byref(gbs),
+                               torch.cuda.current_stream().cuda_stream)
+    if rc:
+        raise RuntimeError(f'bench_store failed ({rc})')
+    return gbs.value
+
+
 # ---------------------------------------------------------------------------------------------- profiling cases
 # Small, self-contained runs of each kernel family for ncu and quick checks:  python bench.py --profile-case <case>
 #   jac        isochoric RHS + Jacobian of 8192 GRI-3.0 states (chem_kernel MODE_JAC), 3 launches
@@ -605,6 +790,8 @@ def fp64_dmma_probe(iters, which=0):
 #   adjoint    64 reactors of the adjoint distribution recorded to 1 ms, then the batched adjoint
 #   fp64issue  warp-level FP64 FMA instructions per second with 1, 2, 4, 8, 16 and 32 active lanes per warp
 #   dmma       FP64 mma.sync (m8n8k4, m16n8k16) throughput beside the DFMA pipe's
+#   sysmem     kernel stores into device memory and into pinned host memory (coalesced, and the thread-per-state
+#              Jacobian pattern), beside cudaMemcpy device-to-host of the same 1.5 GB
 def _spec():
     from spitfire_gb300.mechanism import ChemicalMechanismSpec
     return ChemicalMechanismSpec.bundled('methane-gri30')
@@ -732,9 +919,28 @@ def case_dmma():
     return None
 
 
+def case_sysmem():
+    import torch
+    n = 1536 * 1024 * 1024 // 8
+    dev = torch.empty(n, dtype=torch.float64, device='cuda')
+    host = torch.empty(n, dtype=torch.float64).pin_memory()
+    for pattern, name in ((0, 'coalesced'), (1, 'thread-per-state blocks')):
+        print(f'stores, {name}: device memory {store_probe(dev, pattern):.1f} GB/s, pinned host memory '
+              f'{store_probe(host, pattern):.1f} GB/s')
+    host.copy_(dev, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    host.copy_(dev, non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    print(f'cudaMemcpy device-to-host (pinned): {n * 8 / (e0.elapsed_time(e1) * 1e-3) / 1e9:.1f} GB/s')
+    return None
+
+
 PROFILE_CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs,
                  'integrate_2048': case_integrate_2048, 'integrate': case_integrate, 'flamelet': case_flamelet,
-                 'adjoint': case_adjoint, 'fp64issue': case_fp64issue, 'dmma': case_dmma}
+                 'adjoint': case_adjoint, 'fp64issue': case_fp64issue, 'dmma': case_dmma, 'sysmem': case_sysmem}
 
 
 def run_profile_case(name):
@@ -748,31 +954,45 @@ def run_profile_case(name):
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the oracle C++ restatement of Griffon on the host cores (the reference's own code path
-    cannot run on the GPU machine: it is not present there)."""
+    """--impl reference: the reference's CPU path for this workload on the host cores, as the oracle port (its C++
+    restatement of Griffon, measured here at the reference's own speed; the reference's sources are not on the GPU
+    box). Every step evaluates all 65536 states' RHS + Jacobian with OpenMP over all host cores."""
     if rank != 0:
         return
     import numpy as np
+    import oracle as orc
     from spitfire_gb300 import workloads as W
+    from spitfire_gb300._desc import reactor_params
     from spitfire_gb300.mechanism import ChemicalMechanismSpec
     spec = ChemicalMechanismSpec.bundled('methane-gri30')
     d = W.gri_states(spec, N_STATES)
     q = W.isochoric_state(d)
+    og = orc.OracleGriffon()
+    spec._populate_griffon(og)
+    cores = os.cpu_count()
+    orc.set_threads(cores)
+    P = reactor_params('isochoric')
+    yin = np.zeros(spec.n_species)
+    P.inflow_Y = orc._p(yin)
     per = []
-    base = None
     for k in range(args.warmup + args.steps):
-        b = cpu_baseline(spec, q, seconds=max(1.0, 20.0 / max(args.steps, 1)))
+        t0 = time.perf_counter()
+        og.reactor_jac_batch(P, q, 0)
+        dt = time.perf_counter() - t0
         if k >= args.warmup:
-            per.append(b['value'])
-            base = b
-    v = statistics.mean(per)
+            per.append(dt)
+    ms = 1e3 * statistics.mean(per)
+    v = N_STATES / (ms * 1e-3)
     line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'states/s', 'n_gpus': world,
-            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * N_STATES / v,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic (seeded GRI-3.0 states)',
             'config': {'workload': f'GRI-3.0 isochoric RHS + analytical Jacobian, {N_STATES} states',
                        'l2': 'n/a (CPU)'},
-            'cpu_baseline': {**base, 'value': v},
+            'cpu_baseline': {'value': v, 'unit': 'states/s', 'cores': cores, 'kind': 'port',
+                             'sample': f'every step: all {N_STATES} states, OpenMP over {cores} host threads; the '
+                                       f'port runs at 0.99x the unmodified reference Griffon single-threaded on the '
+                                       f'same GRI states'},
             'e2e': {'value': v, 'unit': 'states/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
 
@@ -934,6 +1154,7 @@ def main():
     del J, J_h
     torch.cuda.empty_cache()
     cpu = rank == 0 and world == 1 and not args.no_cpu
+    small = bench_h2(rank, stream, cpu)
     ignition = bench_ignition(spec, rank, stream, cpu)
     flamelet = bench_flamelet(spec, rank, stream, cpu)
     adjoint = bench_adjoint(spec, rank, stream, cpu)
@@ -950,7 +1171,7 @@ def main():
                          'candidates_ms': {str(k): v for k, v in tuned['group_jac'][1].items()}},
             'plain_gpu_form': {'value': N_STATES / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
                                'speedup_batched_over_plain': plain_ms / ms},
-            'newton': newton, 'ignition': ignition, 'flamelet': flamelet, 'adjoint': adjoint}
+            'newton': newton, 'h2_small': small, 'ignition': ignition, 'flamelet': flamelet, 'adjoint': adjoint}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(spec, qh)
     if rank == 0:

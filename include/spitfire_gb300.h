@@ -295,6 +295,12 @@ typedef struct sf_integrate_params {
   const double *feed_temperature_table;
   int feed_points;
   double feed_t0, feed_dt, feed_jac_t0;
+  /* Optional output of sf_integrate_batch / sf_integrate_record_batch with delta_temperature_ignition > 0: DEVICE
+   * [n], the time at which T first reaches T0 + delta, from the cubic Hermite interpolant of T over the accepted
+   * step that crossed it (end values and the right-hand side's dT/dt at both ends; the first crossing in the step).
+   * NaN where T never reaches it. No reference counterpart: the reference's delay is the end time of that step
+   * (reactors.py:774-790, the integrators' out_t), which this refines without changing the steps. NULL: none. */
+  double *ignition_time_interp;
 } sf_integrate_params;
 
 /* Per-reactor outcome codes written to out_status. */
@@ -378,6 +384,9 @@ typedef struct sf_flamelet_batch {
    * flamelet's interior points. */
   const double *T_convection, *h_convection, *T_radiation, *h_radiation;
   int use_scaled_heat_loss;
+  const double *prefactor;  /* DEVICE [n_flamelets] or NULL: each flamelet's own prefactor of the scale_and_offset
+                               form of sf_flamelet_jac_batch (prefactor * J - I, e.g. gamma * dt of its own time
+                               step), in place of the scalar argument */
 } sf_flamelet_batch;
 
 /* Flamelet residual for every flamelet of the batch (flamelet_kernels.cpp:1039-1218). */

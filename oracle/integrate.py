@@ -84,7 +84,8 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
               max_nonlinear_iter=20, maximum_steps_per_jacobian=1, stop_at_time=None, delta_temperature_ignition=None,
               minimum_allowable_residual=1.e-12, stop_at_steady=None, max_attempts=1000000, save_each_step=False,
               stop_criteria=None, post_step_clip=True):
-    """Returns dict(state, t, steps, newton_iters, jac_setups, failed_steps, status[, times, states]).
+    """Returns dict(state, t, steps, newton_iters, jac_setups, failed_steps, status, t_interp[, times, states]);
+    t_interp: with delta_temperature_ignition, the Hermite-interpolated first crossing of T0 + delta (None if none).
 
     prob gives rhs(q, t) and either jac(q) (dense; LAPACK LU of dt*gamma*J - I) or linear_setup(q, prefactor) and
     linear_solve(r) (its own factorization of prefactor*J - I), and either Tidx (one temperature scaled by 1e3) or
@@ -113,6 +114,7 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
     times = [0.] if save_each_step else None
     states = [state.copy()] if save_each_step else None
     attempts = 0
+    t_interp = None  # first crossing of T0 + delta, Hermite-interpolated over the crossing step
     while True:
         attempts += 1
         if attempts > max_attempts:
@@ -160,11 +162,15 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
         # ---- governor (integrator.py:540-640)
         recent = dt
         if np.all(np.isfinite(dstate)):
+            T_start = state[prob.Tidx] if T0 is not None else None
             state = state + dstate
-            t = t + dt
-            nsteps += 1
             if post_step_clip:
                 state[state < 0.] = 0.  # post_step_callback (reactors.py:506-508, flamelet.py:1119-1121)
+            if T0 is not None and t_interp is None and state[prob.Tidx] > T0 + delta_temperature_ignition:
+                t_interp = hermite_crossing(t, dt, T_start, state[prob.Tidx], k[0][prob.Tidx], k[5][prob.Tidx],
+                                            T0 + delta_temperature_ignition)
+            t = t + dt
+            nsteps += 1
             if save_each_step:
                 times.append(t)
                 states.append(state.copy())
@@ -222,11 +228,33 @@ def integrate(prob, q0, first_time_step=1.e-6, max_time_step=1.e6, transient_tol
         if not cont:
             break
     out = dict(state=state, t=t, steps=nsteps, newton_iters=nnewton, jac_setups=njac, failed_steps=nfail,
-               status=status)
+               status=status, t_interp=t_interp)
     if save_each_step:
         out['times'] = np.array(times)
         out['states'] = np.array(states)
     return out
+
+
+def hermite_crossing(t0, h, y0, y1, d0, d1, thr):
+    """First time in [t0, t0 + h] at which the cubic Hermite interpolant (end values y0 <= thr < y1, end derivatives
+    d0, d1) reaches thr: the first of 16 equal sub-intervals with a crossing, then 48 bisections. The GPU integrator
+    refines its ignition delay the same way (a project-defined measure; the reference reports the step end)."""
+    def p(s):
+        s2, s3 = s * s, s * s * s
+        return (2. * s3 - 3. * s2 + 1.) * y0 + (s3 - 2. * s2 + s) * h * d0 + (3. * s2 - 2. * s3) * y1 + \
+            (s3 - s2) * h * d1
+    lo, hi = 0., 1.
+    for j in range(1, 17):
+        if p(j / 16.) >= thr:
+            lo, hi = (j - 1) / 16., j / 16.
+            break
+    for _ in range(48):
+        mid = 0.5 * (lo + hi)
+        if p(mid) >= thr:
+            hi = mid
+        else:
+            lo = mid
+    return t0 + hi * h
 
 
 def ignition_delay(prob, q0, delta=400., **kw):

@@ -49,7 +49,8 @@ class SfIntegrateParams(C.Structure):
                 ('minimum_allowable_residual', C.c_double), ('stop_at_steady', C.c_double),
                 ('linear_precision', C.c_int), ('refine_sweeps', C.c_int), ('rates_option', C.c_int),
                 ('max_attempts', C.c_int), ('feed_temperature_table', _dp), ('feed_points', C.c_int),
-                ('feed_t0', C.c_double), ('feed_dt', C.c_double), ('feed_jac_t0', C.c_double)]
+                ('feed_t0', C.c_double), ('feed_dt', C.c_double), ('feed_jac_t0', C.c_double),
+                ('ignition_time_interp', _dp)]
 
 
 class SfFlameletBatch(C.Structure):
@@ -58,7 +59,7 @@ class SfFlameletBatch(C.Structure):
                 ('cmajor', _dp), ('csub', _dp), ('csup', _dp), ('mcoeff', _dp), ('ncoeff', _dp), ('chi', _dp),
                 ('include_enthalpy_flux', C.c_int), ('include_variable_cp', C.c_int), ('diffterm', _dp),
                 ('active', _ip), ('T_convection', _dp), ('h_convection', _dp), ('T_radiation', _dp),
-                ('h_radiation', _dp), ('use_scaled_heat_loss', C.c_int)]
+                ('h_radiation', _dp), ('use_scaled_heat_loss', C.c_int), ('prefactor', _dp)]
 
 
 def reactor_params(configuration='isobaric', heat_transfer='adiabatic', open_=False, pressure=101325.,

@@ -115,6 +115,32 @@ __device__ bool warp_hmatrix_below(double *A, int n, double cutoff, double *dg)
   return true;
 }
 
+// The same test for the unreduced upper Hessenberg block H[lo..hi, lo..hi] of a QR iterate: every eigenvalue of
+// the block has real part below `cutoff` if its comparison matrix (diag(cutoff - h_ii), -|h_ij| elsewhere, zero
+// below the subdiagonal) is a nonsingular M-matrix. A Hessenberg LU without pivoting eliminates one row per
+// column, so the test keeps one row vector (r: hi + 1 doubles of shared work, lanes over columns) and costs
+// O(m^2) for a block of m rows, against O(m^2) per double-shift QR sweep over the block.
+__device__ bool warp_hess_hmatrix_below(const double *H, int n, int lo, int hi, double cutoff, double *r)
+{
+  const int lane = threadIdx.x & 31;
+  for (int j = lo + lane; j <= hi; j += 32) r[j] = j == lo ? cutoff - H[lo + lo * n] : -fabs(H[lo + j * n]);
+  __syncwarp();
+  for (int k = lo; k <= hi; ++k) {
+    const double dgk = cutoff - H[k + k * n];
+    const double p = r[k];
+    if (!(dgk > 0.) || !(p > 1e-10 * dgk)) return false;  // the same values in every lane: a warp-uniform exit
+    if (k == hi) break;
+    const double l = -fabs(H[(k + 1) + k * n]) / p;  // multiplier of row k + 1 (its only entry below the pivot)
+    __syncwarp();
+    for (int j = k + 1 + lane; j <= hi; j += 32) {
+      const double m = j == k + 1 ? cutoff - H[(k + 1) + (k + 1) * n] : -fabs(H[(k + 1) + j * n]);
+      r[j] = m - l * r[j];
+    }
+    __syncwarp();
+  }
+  return true;
+}
+
 // Upper bound of the real parts of the eigenvalues by Gershgorin's theorem applied to rows and to columns.
 __device__ double warp_gershgorin_bound(const double *A, int n)
 {
@@ -241,6 +267,10 @@ __device__ __forceinline__ int warp_find_lo(double *H, int n, int hi)
 // Largest real part of the eigenvalues of the n x n matrix A (destroyed; A is balanced first). work: 2n doubles
 // of shared memory. If cutoff is given and the balanced matrix's Gershgorin bound is <= cutoff, the function
 // returns that bound instead of running QR (every eigenvalue is then known to have real part <= cutoff).
+// With a cutoff the QR iteration also stops early: after every second sweep on an unreduced block, the block is
+// tested with warp_hess_hmatrix_below, and a block whose eigenvalues are all proven left of the cutoff is set aside
+// without computing them. The returned maximum then covers only the eigenvalues computed, so it is exact whenever
+// it exceeds the cutoff, and at most the cutoff otherwise, which is all max(lambda_max - cutoff, 0) needs.
 // Returns false if the QR iteration did not converge within its budget (the largest real part of the diagonal
 // found so far is returned then).
 __device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_max, double cutoff = -INFINITY)
@@ -279,6 +309,12 @@ __device__ bool warp_max_real_eig(double *A, int n, double *work, double *out_ma
       const double disc = tr * tr - det;
       vmax = fmax(vmax, disc >= 0. ? tr + sqrt(disc) : tr);
       hi -= 2;
+      iter = 0;
+      continue;
+    }
+    // the early exit: a block whose eigenvalues all lie left of the cutoff is done
+    if (cutoff > -INFINITY && (iter & 1) && warp_hess_hmatrix_below(H, n, lo, hi, cutoff, work)) {
+      hi = lo - 1;
       iter = 0;
       continue;
     }

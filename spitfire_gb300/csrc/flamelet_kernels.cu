@@ -34,6 +34,7 @@ struct FlmParams {
   int scale_offset;
   int rates_option;
   double prefactor;
+  const double *prefactors;  // device [nf] or null: each flamelet's own prefactor of scale_offset
   double *eflux_store;  // if set: the enthalpy-flux diagonal correction is stored here (per point) instead
   const int *active;    // device [nf] or null: flamelets with active[f] == 0 are skipped
   // nonadiabatic flamelets: convection / radiation temperature and coefficient per interior point (null: adiabatic)
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
   NoJ noj;
   for (int pt = blockIdx.x * p.groups_per_cta + gid; pt < p.n_points; pt += gridDim.x * p.groups_per_cta) {
     const int f = find_flamelet(p.offz, p.n_flamelets, pt);
+    const double pref = p.prefactors ? p.prefactors[f] : p.prefactor;
     if (p.active && !p.active[f]) continue;
     const int z0 = p.offz[f], nzi = p.offz[f + 1] - z0;
     const int iz = pt - z0;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
       // block of this point in the flamelet's BTDDOD value array
       double *vals = p.out_values + p.offv[f];
       double *blk = vals + (size_t)iz * ns * ns;
-      BlockWriter bw{blk, ns, p.cmajor + (size_t)pt * ns, p.scale_offset, p.prefactor};
+      BlockWriter bw{blk, ns, p.cmajor + (size_t)pt * ns, p.scale_offset, pref};
       double *rhs_tmp = scr + L.total;
       reactor_eval<G, true, default_unroll(G), false>(m, b, L, scr, grp, st, p.pressure, cfg, p.pg, rhs_tmp, bw);
       if (p.eflux) {
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
         const double f1 = 0.5 * chi / cp * dTdZ * dcpdZ;
         grp.sync();
         if (lane == 0) {
-          const double corr = (p.scale_offset ? p.prefactor : 1.) * f1 / cp * cps;
+          const double corr = (p.scale_offset ? pref : 1.) * f1 / cp * cps;
           if (p.eflux_store)
             p.eflux_store[(size_t)pt * ns] = corr;
           else
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(256) flamelet_point_kernel(const FlmParams p)
       }
       // off-diagonals: sub row iz (iz >= 1) and super row iz (iz <= nzi-2) (flamelet_kernels.cpp:1383-1394)
       const long long sub_off = (long long)nzi * ns * ns, sup_off = sub_off + (long long)(nzi - 1) * ns;
-      const double sc = p.scale_offset ? p.prefactor : 1.;
+      const double sc = p.scale_offset ? pref : 1.;
       for (int q = lane; q < ns; q += G) {
         if (iz >= 1) vals[sub_off + (long long)(iz - 1) * ns + q] = sc * p.csub[(size_t)pt * ns + q];
         if (iz <= nzi - 2) vals[sup_off + (long long)iz * ns + q] = sc * p.csup[(size_t)pt * ns + q];
@@ -973,6 +975,7 @@ void fill(FlmParams &p, const sf_flamelet_batch *fb)
   p.eflux = fb->include_enthalpy_flux;
   p.vcp = fb->include_variable_cp;
   p.active = fb->active;
+  p.prefactors = fb->prefactor;
 }
 
 template <class F>

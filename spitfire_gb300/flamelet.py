@@ -362,13 +362,19 @@ class FlameletBatch:
     def jacobian(self, state, scale_and_offset=False, prefactor=0., eig=False, diffterm=0., diffterm_per_flamelet=None,
                  active=None):
         """BTDDOD Jacobian values into self.values; with eig also the eigenvalue bound per row, using
-        diffterm_per_flamelet (CUDA FP64 [nf]) when given, else the scalar diffterm."""
+        diffterm_per_flamelet (CUDA FP64 [nf]) when given, else the scalar diffterm. prefactor: a number, or a CUDA
+        FP64 tensor [nf] with each flamelet's own prefactor of the scale_and_offset form."""
         torch = _torch()
         expeig = torch.empty(self.npts * self.ns, dtype=torch.float64, device=state.device) if eig else None
         m = self._mask(active)
         self.fb.active = C.cast(m.data_ptr(), C.POINTER(C.c_int)) if m is not None else None
         self.fb.diffterm = C.cast(diffterm_per_flamelet.data_ptr(), C.POINTER(C.c_double)) \
             if diffterm_per_flamelet is not None else None
+        per = torch.is_tensor(prefactor)
+        if per:
+            self._pref_keep = prefactor.to(dtype=torch.float64).contiguous()
+            self.fb.prefactor = C.cast(self._pref_keep.data_ptr(), C.POINTER(C.c_double))
+            prefactor = 0.
         try:
             N.check(N.load().sf_flamelet_jac_batch(self.g.handle, C.byref(self.fb), N.ptr(state), self.rates_option,
                                                    int(scale_and_offset), float(prefactor), float(diffterm),
@@ -377,6 +383,7 @@ class FlameletBatch:
         finally:
             self.fb.active = None
             self.fb.diffterm = None
+            self.fb.prefactor = None
         return (self.values, expeig) if eig else self.values
 
     def diffterm_tensor(self, diffusion_factor=4.):
@@ -682,7 +689,6 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
     host = state.cpu().numpy()
     times = [[0.] for _ in range(nf)]
     states = [[host[a:e].copy()] for (a, e) in seg]
-    onehot = torch.eye(nf, dtype=torch.bool, device=dev)
     G, A, B, BH = _ESDIRK_GAMMA, _ESDIRK_A, _ESDIRK_B, _ESDIRK_BH
     k = [torch.zeros_like(state) for _ in range(6)]
     coerce = stop_at_time is not None
@@ -697,9 +703,9 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
         if coerce:
             dt = np.where(run & (t + dt > stop_at_time), stop_at_time - t, dt)
         need = run & eval_setup
-        for f in np.flatnonzero(need):
-            b.jacobian(state, scale_and_offset=True, prefactor=float(dt[f] * G), active=onehot[f])
         if need.any():
+            # one launch for every flamelet that needs a setup, each with its own prefactor gamma * dt
+            b.jacobian(state, scale_and_offset=True, prefactor=torch.from_numpy(dt * G).to(dev), active=mask(need))
             b.factor(active=mask(need))
             jac_setups[need] += 1
         setup_count[run] += 1
@@ -744,7 +750,8 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
             new = state + dstate
             new = torch.where(new < 0., torch.zeros_like(new), new)
             state = torch.where(b.expand(mask(acc)), new, state)
-        host = state.cpu().numpy()
+        # the states reach the host only for the recorded trajectory or a stop criterion
+        host = state.cpu().numpy() if (save_each_step or stop_criteria is not None) else None
         for f in np.flatnonzero(run):
             recent = dt[f]
             if fin[f]:
@@ -789,6 +796,7 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
                 status[f] = 3
             if not cont:
                 run[f] = False
+    host = state.cpu().numpy()
     out = []
     for f in range(nf):
         if save_each_step:

@@ -146,6 +146,7 @@ class BatchIntegrator:
         dev = torch.device('cuda', torch.cuda.current_device())
         return dict(q=torch.empty((n, neq), dtype=torch.float64, device=dev),
                     t=torch.empty(n, dtype=torch.float64, device=dev),
+                    t_interp=torch.full((n,), float('nan'), dtype=torch.float64, device=dev),
                     counts=torch.empty((n, 4), dtype=torch.int32, device=dev),
                     status=torch.empty(n, dtype=torch.int32, device=dev),
                     ws=torch.empty(self.workspace_bytes(n) // 4 + 1, dtype=torch.int32, device=dev))
@@ -156,6 +157,9 @@ class BatchIntegrator:
     def launch(self, q0, pressures, out, ip, record=None):
         L = N.load()
         n = q0.shape[0]
+        # the Hermite-interpolated first crossing of T0 + delta beside the step-end delay
+        ip.ignition_time_interp = C.cast(out['t_interp'].data_ptr(), C.POINTER(C.c_double)) \
+            if ip.delta_temperature_ignition > 0. else None
         if record is None:
             N.check(L.sf_integrate_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0),
                                          N.ptr(pressures), N.ptr(out['q']), N.ptr(out['t']), N.ptr(out['counts']),
@@ -172,8 +176,9 @@ class BatchIntegrator:
         """Integrate every row of q0 (isobaric [T, Y_0..Y_{ns-2}] or isochoric [rho, T, Y...]).
 
         Returns dict of CUDA tensors: q (final states), t (final times; the ignition delay when
-        delta_temperature_ignition is given), counts [n, 4] (accepted steps, Newton iterations, Jacobian setups,
-        failed steps), status (see STATUS_NAMES)."""
+        delta_temperature_ignition is given), t_interp (with delta_temperature_ignition: the time T first reaches
+        T0 + delta on the cubic Hermite interpolant of the crossing step, NaN if never), counts [n, 4] (accepted
+        steps, Newton iterations, Jacobian setups, failed steps), status (see STATUS_NAMES)."""
         torch = _torch()
         q0 = self.g._dev(q0)
         pr = self.g._dev(pressures) if pressures is not None else None

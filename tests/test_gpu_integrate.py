@@ -59,6 +59,7 @@ def test_batched_ignition_matches_oracle(cuda):
     bi = BatchIntegrator(spec, 'isobaric')
     out = bi.run(d['q0'], pressures=d['p'], delta_temperature_ignition=400., stop_at_time=0.1)
     tau = out['t'].cpu().numpy()
+    ti = out['t_interp'].cpu().numpy()
     st = out['status'].cpu().numpy()
     cnt = out['counts'].cpu().numpy()
     for i in range(16):
@@ -67,6 +68,12 @@ def test_batched_ignition_matches_oracle(cuda):
         assert st[i] == r['status'], i
         assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
         assert abs(tau[i] - r['t']) / r['t'] <= 1e-6, (i, tau[i], r['t'])
+        # the Hermite-interpolated delay: the oracle's, and inside the crossing step (no later than its end)
+        if r['t_interp'] is None:
+            assert np.isnan(ti[i]), i
+        else:
+            assert abs(ti[i] - r['t_interp']) / r['t_interp'] <= 1e-6, (i, ti[i], r['t_interp'])
+            assert ti[i] <= tau[i] * (1. + 1e-12), i
 
 
 def test_fp32_lu_variant_error_is_small(cuda):

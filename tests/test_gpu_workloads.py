@@ -37,6 +37,7 @@ def test_low_temperature_ignition_band_matches_oracle(cuda):
                                                 stop_at_time=0.1)
     tau, st = out['t'].cpu().numpy(), out['status'].cpu().numpy()
     cnt, qf = out['counts'].cpu().numpy(), out['q'].cpu().numpy()
+    ti = out['t_interp'].cpu().numpy()
     statuses = []
     for i in range(n):
         r = I.integrate(I.ReactorProblem(og, 'isobaric', pressure=d['p'][i]), d['q0'][i],
@@ -45,6 +46,10 @@ def test_low_temperature_ignition_band_matches_oracle(cuda):
         assert st[i] == r['status'], (i, st[i], r['status'])
         assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
         assert abs(tau[i] - r['t']) / r['t'] <= 1e-6, (i, tau[i], r['t'])
+        if r['t_interp'] is None:
+            assert np.isnan(ti[i]), i
+        else:
+            assert abs(ti[i] - r['t_interp']) / r['t_interp'] <= 1e-6, i
         ref = r['state']
         assert abs(qf[i, 0] - ref[0]) / ref[0] < 1e-6, i
         assert np.max(np.abs(qf[i, 1:] - ref[1:])) / np.max(np.abs(ref[1:])) < 1e-6, i

@@ -51,9 +51,11 @@ class CpuBatch:
         return out
 
     def jacobian(self, state, scale_and_offset=False, prefactor=0., active=None):
+        # prefactor: a number, or one per flamelet (as FlameletBatch.jacobian takes it)
         x = state.numpy()
         for f in self._on(active):
-            self._J[f] = self.ops[f].jac(x[self._seg(f)], scale_and_offset=scale_and_offset, prefactor=prefactor)
+            pf = float(prefactor[f]) if torch.is_tensor(prefactor) else prefactor
+            self._J[f] = self.ops[f].jac(x[self._seg(f)], scale_and_offset=scale_and_offset, prefactor=pf)
 
     def factor(self, active=None):
         for f in self._on(active):
