@@ -1005,6 +1005,8 @@ def main():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--profile-case', choices=sorted(PROFILE_CASES), help='run one profiling case and exit')
+    ap.add_argument('--headline-only', action='store_true',
+                    help='measure the headline workload (value, e2e, roofline) and skip the further blocks')
     args = ap.parse_args()
     if args.profile_case:
         sys.exit(run_profile_case(args.profile_case))
@@ -1149,15 +1151,17 @@ def main():
     roof['hbm'] = {'algorithmic_bytes': hbm_bytes, 'achieved_gbs': hbm_bytes / (ms * 1e-3) / 1e9}
 
     # ---------------- further workloads
-    gh = torch.tensor(d['gamma_h'], dtype=torch.float64, device=dev)
-    newton = bench_newton(q, rhs, J, gh, stream)
-    del J, J_h
-    torch.cuda.empty_cache()
     cpu = rank == 0 and world == 1 and not args.no_cpu
-    small = bench_h2(rank, stream, cpu)
-    ignition = bench_ignition(spec, rank, stream, cpu)
-    flamelet = bench_flamelet(spec, rank, stream, cpu)
-    adjoint = bench_adjoint(spec, rank, stream, cpu)
+    extra = {}
+    if not args.headline_only:
+        gh = torch.tensor(d['gamma_h'], dtype=torch.float64, device=dev)
+        extra['newton'] = bench_newton(q, rhs, J, gh, stream)
+        del J, J_h
+        torch.cuda.empty_cache()
+        extra['h2_small'] = bench_h2(rank, stream, cpu)
+        extra['ignition'] = bench_ignition(spec, rank, stream, cpu)
+        extra['flamelet'] = bench_flamelet(spec, rank, stream, cpu)
+        extra['adjoint'] = bench_adjoint(spec, rank, stream, cpu)
 
     line = {'metric': METRIC, 'value': value, 'unit': 'states/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
@@ -1171,7 +1175,7 @@ def main():
                          'candidates_ms': {str(k): v for k, v in tuned['group_jac'][1].items()}},
             'plain_gpu_form': {'value': N_STATES / (plain_ms * 1e-3), 'unit': 'states/s', 'ms': plain_ms,
                                'speedup_batched_over_plain': plain_ms / ms},
-            'newton': newton, 'h2_small': small, 'ignition': ignition, 'flamelet': flamelet, 'adjoint': adjoint}
+            **extra}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(spec, qh)
     if rank == 0:
