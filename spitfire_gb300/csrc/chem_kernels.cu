@@ -41,9 +41,6 @@ struct KParams {
   double *out_w, *out_S, *out_rhs, *out_J;
   int groups_per_cta;
   double *gscratch;  // thread-per-state kernels: interleaved per-warp scratch in global memory
-  // thread-per-state Jacobians: device addresses of pinned host outputs the warp copies its finished block to
-  double *host_rhs, *host_J;
-  int host_vec2;     // both copies are 16-byte aligned
   // open reactors: feed
   int open;
   double tau, rho_in, Tin;
@@ -169,20 +166,6 @@ __global__ void __launch_bounds__(256) chem_kernel(const KParams p)
     eval_state<G, MODE>(p, m, b, L, scr, grp, pg, cfg, st);
 }
 
-// Copy `count` doubles with the 32 lanes of a warp, in 16-byte pairs where both addresses allow it.
-__device__ __forceinline__ void copy_block(const double *src, double *dst, size_t count, int lane, int vec2)
-{
-  if (vec2 && ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
-    const double2 *s2 = reinterpret_cast<const double2 *>(src);
-    double2 *d2 = reinterpret_cast<double2 *>(dst);
-    const size_t pairs = count >> 1;
-    for (size_t e = lane; e < pairs; e += 32) d2[e] = s2[e];
-    if ((count & 1) && lane == 0) dst[count - 1] = src[count - 1];
-  } else {
-    for (size_t e = lane; e < count; e += 32) dst[e] = src[e];
-  }
-}
-
 // Thread per state: the 32 lanes of a warp evaluate 32 states in lockstep (the same mechanism, so the same
 // instruction stream), each FP64 instruction carrying 32 useful lanes. Scratch is interleaved per warp in global
 // memory (L2/HBM); the mechanism blob is in shared memory, read by all lanes at once.
@@ -206,17 +189,6 @@ __global__ void __launch_bounds__(128) chem_kernel_tps(const KParams p)
   for (int base = wg * 32; base < p.n; base += nwg * 32) {
     const int st = base + lane;
     if (st < p.n) eval_state<1, MODE>(p, m, b, L, scr, grp, pg, cfg, st);
-    if (jac_mode(MODE) && MODE != MODE_SENS && p.host_J) {
-      // the warp's 32 states are one contiguous block of the outputs: copy it to host memory with coalesced
-      // stores, so that the results cross the host link while other warps still compute
-      __syncwarp();
-      const int neq = p.configuration == 1 ? m.ns + 1 : m.ns;
-      const int cnt = min(32, p.n - base);
-      copy_block(p.out_J + (size_t)base * neq * neq, p.host_J + (size_t)base * neq * neq, (size_t)cnt * neq * neq,
-                 lane, p.host_vec2);
-      copy_block(p.out_rhs + (size_t)base * neq, p.host_rhs + (size_t)base * neq, (size_t)cnt * neq, lane,
-                 p.host_vec2 && ((cnt * neq) & 1) == 0 && (neq & 1) == 0);
-    }
   }
 }
 
@@ -563,24 +535,6 @@ int sf_reactor_jac_batch(const sf_mech *mech, const sf_reactor_params *rp, int r
   });
 }
 
-// Device address of host memory the device can write directly (a pinned, mapped allocation), or false.
-static bool host_addressable(void *host, double **dev)
-{
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
-  void *d = nullptr;
-  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
-    cudaGetLastError();
-    return false;
-  }
-  *dev = static_cast<double *>(d);
-  return true;
-}
-
 size_t sf_chem_workspace_size(const sf_mech *mech, int kind, int n)
 {
   if (!mech || n <= 0 || kind < SF_CHEM_RATES || kind > SF_CHEM_JAC) return 0;
@@ -632,26 +586,6 @@ int sf_reactor_jac_host_batch(const sf_mech *mech, const sf_reactor_params *rp, 
     const size_t kws_bytes = workspace_bytes - io_bytes;
     cudaStream_t st = (cudaStream_t)stream;
     const int G = group_of(hm, SF_TUNE_GROUP_JAC);
-    // Outputs in pinned host memory the device can address, with the thread-per-state kernel: one launch, each warp
-    // copying its finished block of states to the host (coalesced), so the copies overlap the rest of the kernel.
-    double *dev_jac_host = nullptr, *dev_rhs_host = nullptr;
-    if (G == 1 && chunk_states <= 0 && host_addressable(out_jac_host, &dev_jac_host) &&
-        host_addressable(out_rhs_host, &dev_rhs_host)) {
-      CUDA_THROW(cudaMemcpyAsync(q, q_host, n * neq * 8, cudaMemcpyHostToDevice, st));
-      if (pressures_host) CUDA_THROW(cudaMemcpyAsync(pr, pressures_host, (size_t)n * 8, cudaMemcpyHostToDevice, st));
-      KParams p{};
-      fill_reactor(p, rp);
-      p.n = n;
-      p.q = q;
-      p.pressures = pressures_host ? pr : nullptr;
-      p.option = rates_option;
-      p.out_rhs = rhs;
-      p.out_J = J;
-      p.host_rhs = dev_rhs_host;
-      p.host_J = dev_jac_host;
-      p.host_vec2 = ((reinterpret_cast<uintptr_t>(dev_jac_host) | reinterpret_cast<uintptr_t>(J)) & 15) == 0;
-      return chem_launch(hm, MODE_JAC, p, st, G, kws, kws_bytes);
-    }
     // chunk: by default the states one wave of the thread-per-state kernel covers (its resident warps), else half
     int chunk = chunk_states;
     if (chunk <= 0) chunk = G == 1 ? (int)std::min<size_t>((size_t)n, tps_resident_warps(hm) * 32) : (n + 1) / 2;

@@ -267,9 +267,8 @@ def test_open_reactor_rhs_jac(cuda, name, configuration, heat, group):
 
 @pytest.mark.parametrize('group', [0, 1])
 def test_host_buffer_jacobians_match_device_path(cuda, group):
-    """sf_reactor_jac_host_batch (host states in, host results out: chunked with overlapped copies, or, for pinned
-    outputs and the thread-per-state kernel, one launch whose warps copy their finished blocks to the host) gives
-    the device entry point's results bit for bit, for pinned and pageable buffers, aligned or not, and several chunk
+    """sf_reactor_jac_host_batch (host states in, host results out, chunked with overlapped copies) gives the
+    device entry point's results bit for bit, for pinned and pageable buffers (aligned or not) and several chunk
     sizes."""
     import torch
     from spitfire_gb300 import autotune as AT
@@ -296,7 +295,7 @@ def test_host_buffer_jacobians_match_device_path(cuda, group):
         g.reactor_jac_host_batch(P, np.ascontiguousarray(qh), rn, Jn, chunk_states=1234)
         torch.cuda.synchronize()
         assert np.array_equal(rn, r_ref) and np.array_equal(Jn, J_ref)
-        # pinned outputs at an 8-byte offset (the warps' copies to host memory then go one double at a time)
+        # pinned outputs at an 8-byte offset into their allocations
         rb = torch.empty(n * neq + 1, dtype=torch.float64).pin_memory()
         Jb = torch.empty(n * neq * neq + 1, dtype=torch.float64).pin_memory()
         rv, Jv = rb[1:].view(n, neq), Jb[1:].view(n, neq * neq)
