@@ -286,15 +286,18 @@ typedef struct sf_integrate_params {
   int refine_sweeps;                /* refinement sweeps for linear_precision 1 */
   int rates_option;                 /* 0 dense exact (default), 2 sparse exact */
   int max_attempts;                 /* cap on step attempts (accepted + failed) per reactor */
-  /* Open reactors (params->open) with a time-dependent feed temperature: when feed_temperature_table is non-NULL
-   * (DEVICE pointer to feed_points >= 2 values at integration-local times feed_t0 + j feed_dt), the feed
-   * temperature is its piecewise-linear interpolant, held constant beyond the ends, in place of
-   * params->inflow_temperature. As in the reference (reactors.py:279-282, :335-338, :538-592), each right-hand side
-   * takes the feed at its own time and each Jacobian the feed of the most recent right-hand side, or the feed at
-   * feed_jac_t0 before the first one. NULL: the constant params->inflow_temperature. */
-  const double *feed_temperature_table;
-  int feed_points;
-  double feed_t0, feed_dt, feed_jac_t0;
+  /* Time-dependent reactor parameters (reactors.py:253-341): when time_table is non-NULL (DEVICE
+   * [time_points][time_width], time_points >= 2, values at integration-local times time_t0 + j time_dt), each
+   * parameter whose sf_time_param bit is set in time_columns is the table's interpolant (cubic Lagrange on four
+   * table points, held constant beyond the ends) in place of its value in sf_reactor_params. The columns hold the
+   * set parameters in the order of their bits, the ns feed mass fractions of SF_TIME_FEED_Y last. As in the
+   * reference's closures (reactors.py:279-282, :335-341, :538-592), each right-hand side takes the parameters at
+   * its own time and each Jacobian those of the most recent right-hand side, or those at time_jac_t0 before the
+   * first one. The feed density has no column: the reference evaluates it once, at t = 0. Mass-transfer columns
+   * act on open reactors only, heat-transfer ones on diathermal reactors only. NULL: none. */
+  const double *time_table;
+  int time_points, time_width, time_columns;
+  double time_t0, time_dt, time_jac_t0;
   /* Optional output of sf_integrate_batch / sf_integrate_record_batch with delta_temperature_ignition > 0: DEVICE
    * [n], the time at which T first reaches T0 + delta, from the cubic Hermite interpolant of T over the accepted
    * step that crossed it (end values and the right-hand side's dT/dt at both ends; the first crossing in the step).
@@ -302,6 +305,17 @@ typedef struct sf_integrate_params {
    * (reactors.py:774-790, the integrators' out_t), which this refines without changing the steps. NULL: none. */
   double *ignition_time_interp;
 } sf_integrate_params;
+
+/* Parameters a time table of sf_integrate_params may hold, as bits of time_columns. */
+enum sf_time_param {
+  SF_TIME_FEED_T = 1,      /* feed temperature */
+  SF_TIME_MIXING_TAU = 2,  /* mixing (residence) time */
+  SF_TIME_CONV_T = 4,      /* convection (fluid) temperature */
+  SF_TIME_CONV_H = 8,      /* convection coefficient */
+  SF_TIME_RAD_T = 16,      /* radiation (surface) temperature */
+  SF_TIME_RAD_EPS = 32,    /* radiative emissivity */
+  SF_TIME_FEED_Y = 64      /* feed mass fractions (ns columns) */
+};
 
 /* Per-reactor outcome codes written to out_status. */
 enum sf_integrate_status {

@@ -28,21 +28,47 @@ STATUS = {'done': 1, 'ignited': 2, 'steady': 3, 'max_steps': 4, 'nan': 5, 'no_ig
 
 
 class ReactorProblem:
-    """Closed reactor RHS/Jacobian closures (reactors.py:538-592) over the oracle Griffon."""
+    """Reactor RHS/Jacobian closures (reactors.py:538-592) over the oracle Griffon. Diathermal reactors take
+    convection_temperature, radiation_temperature, convection_coefficient, radiative_emissivity and
+    surface_area_to_volume; any of the first four may be a function of time. As in the reference
+    (_update_heat_transfer_parameters, reactors.py:324-328), every right-hand side evaluation refreshes them at its
+    own time and the Jacobian uses the values the most recent right-hand side left (those at t = 0 before the
+    first one, reactors.py:275-278)."""
 
-    def __init__(self, og, configuration, pressure=101325., heat='adiabatic'):
+    HEAT = (('convection_temperature', 'fluid_temperature'), ('radiation_temperature', 'surface_temperature'),
+            ('convection_coefficient', 'h_convection'), ('radiative_emissivity', 'eps_radiation'))
+
+    def __init__(self, og, configuration, pressure=101325., heat='adiabatic', convection_temperature=300.,
+                 radiation_temperature=300., convection_coefficient=0., radiative_emissivity=0.,
+                 surface_area_to_volume=1.):
         import oracle as orc
         from spitfire_gb300._desc import reactor_params
         self.og = og
         self.configuration = configuration
         self.pressure = pressure
-        self.P = reactor_params(configuration, heat, pressure=pressure)
+        self.P = reactor_params(configuration, heat, pressure=pressure, surface_area_to_volume=surface_area_to_volume)
+        self._funcs = {}
+        given = dict(convection_temperature=convection_temperature, radiation_temperature=radiation_temperature,
+                     convection_coefficient=convection_coefficient, radiative_emissivity=radiative_emissivity)
+        for name, field in self.HEAT:
+            v = given[name]
+            if callable(v):
+                self._funcs[field] = v
+            setattr(self.P, field, v(0.) if callable(v) else v)
         self._yin = np.zeros(og.n_species)
         self.P.inflow_Y = orc._p(self._yin)
         self.Tidx = 0 if configuration == 'isobaric' else 1
         self.pres = np.array([pressure]) if configuration == 'isobaric' else None
 
+    def _update(self, t):
+        for field, f in self._funcs.items():
+            if field == 'inflow_Y':
+                self._yin[:] = np.asarray(f(t), dtype=np.float64)
+            else:
+                setattr(self.P, field, f(t))
+
     def rhs(self, q, t=0.):
+        self._update(t)
         return self.og.reactor_rhs_batch(self.P, q[None, :], pressures=self.pres)[0]
 
     def jac(self, q):
@@ -52,28 +78,27 @@ class ReactorProblem:
 
 
 class OpenReactorProblem(ReactorProblem):
-    """Open (mass-exchange) reactor: a feed of temperature `feed_temperature` (a number or a function of time), mass
-    fractions `feed_Y`, density `feed_density` (isochoric) and mixing time `tau`. As in the reference's closures
-    (reactors.py:538-592 with _update_mass_transfer_parameters, :335-338) every right-hand side evaluation refreshes
-    the feed temperature at its own time, and the Jacobian uses the values the most recent right-hand side left
-    (those at t = 0 before the first one, reactors.py:279-282)."""
+    """Open (mass-exchange) reactor: a feed of temperature `feed_temperature`, mass fractions `feed_Y`, density
+    `feed_density` (isochoric) and mixing time `tau`. The feed temperature, mass fractions and mixing time may be
+    functions of time: as in the reference's closures (reactors.py:538-592 with _update_mass_transfer_parameters,
+    :330-333) every right-hand side evaluation refreshes them at its own time, and the Jacobian uses the values the
+    most recent right-hand side left (those at t = 0 before the first one, reactors.py:275-282). A feed density
+    function is evaluated once, at t = 0, and never refreshed, as in the reference."""
 
     def __init__(self, og, configuration, feed_temperature, feed_Y, tau, pressure=101325., heat='adiabatic',
-                 feed_density=0.):
+                 feed_density=0., **heat_params):
         import oracle as orc
-        super().__init__(og, configuration, pressure=pressure, heat=heat)
+        super().__init__(og, configuration, pressure=pressure, heat=heat, **heat_params)
         self.P.open = 1
-        self.P.tau = tau
-        self.P.inflow_density = feed_density
-        self._yin = np.asarray(feed_Y, dtype=np.float64).copy()
+        at0 = lambda v: v(0.) if callable(v) else v
+        self.P.tau = at0(tau)
+        self.P.inflow_density = at0(feed_density)
+        self._yin = np.asarray(at0(feed_Y), dtype=np.float64).copy()
         self.P.inflow_Y = orc._p(self._yin)
-        self._tf = feed_temperature
-        self.P.inflow_temperature = feed_temperature(0.) if callable(feed_temperature) else feed_temperature
-
-    def rhs(self, q, t=0.):
-        if callable(self._tf):
-            self.P.inflow_temperature = self._tf(t)
-        return super().rhs(q)
+        self.P.inflow_temperature = at0(feed_temperature)
+        for field, v in (('inflow_temperature', feed_temperature), ('tau', tau), ('inflow_Y', feed_Y)):
+            if callable(v):
+                self._funcs[field] = v
 
 
 C = A.sum(axis=1)  # stage times t + c_s dt

@@ -48,9 +48,14 @@ class SfIntegrateParams(C.Structure):
                 ('stop_at_time', C.c_double), ('delta_temperature_ignition', C.c_double),
                 ('minimum_allowable_residual', C.c_double), ('stop_at_steady', C.c_double),
                 ('linear_precision', C.c_int), ('refine_sweeps', C.c_int), ('rates_option', C.c_int),
-                ('max_attempts', C.c_int), ('feed_temperature_table', _dp), ('feed_points', C.c_int),
-                ('feed_t0', C.c_double), ('feed_dt', C.c_double), ('feed_jac_t0', C.c_double),
-                ('ignition_time_interp', _dp)]
+                ('max_attempts', C.c_int), ('time_table', _dp), ('time_points', C.c_int),
+                ('time_width', C.c_int), ('time_columns', C.c_int), ('time_t0', C.c_double),
+                ('time_dt', C.c_double), ('time_jac_t0', C.c_double), ('ignition_time_interp', _dp)]
+
+# bits of SfIntegrateParams.time_columns (enum sf_time_param), in column order
+TIME_PARAMS = [('feed_temperature', 1), ('mixing_tau', 2), ('convection_temperature', 4),
+               ('convection_coefficient', 8), ('radiation_temperature', 16), ('radiative_emissivity', 32),
+               ('feed_mass_fractions', 64)]
 
 
 class SfFlameletBatch(C.Structure):

@@ -89,27 +89,58 @@ struct IterMatrix {
   }
 };
 
-// Feed temperature of an open reactor at integration-local time t: the table's 4-point (cubic) Lagrange interpolant,
-// else the constant. At a spacing of the first time step the interpolation error, O(h^4 T''''), is far below the
-// rounding of the temperature, so the right-hand side sees the feed function itself.
-__device__ __forceinline__ double feed_temperature_at(const IntParams &p, double t)
+// Time-dependent reactor parameters at integration-local time t: every column of the time table is its 4-point
+// (cubic) Lagrange interpolant in time, held constant beyond the table's ends. At a spacing of the first time step
+// the interpolation error, fourth order in the spacing, is far below the rounding of the values, so the right-hand
+// side sees the parameter functions themselves. Sets the parameters of time_columns in cf; the feed mass fractions
+// go to ybuf (ns doubles of the warp's shared memory), which cf.yin then points to.
+__device__ __noinline__ void apply_time_params(const IntParams &p, ReactorCfg &cf, double t, double *ybuf, int ns)
 {
   const sf_integrate_params &ip = p.ip;
-  const double *tab = ip.feed_temperature_table;
-  if (!tab) return p.cfg.Tin;
-  const double u = (t - ip.feed_t0) / ip.feed_dt;
-  const int last = ip.feed_points - 1;
-  if (!(u > 0.)) return tab[0];
-  if (u >= (double)last) return tab[last];
-  int i = (int)u;
-  // stencil i-1 .. i+2, shifted inside the table at its ends
-  const int i0 = i < 1 ? 0 : (i + 2 > last ? last - 3 : i - 1);
-  const double x = u - (double)i0;  // position within the stencil, nodes at 0, 1, 2, 3
-  const double x0 = x, x1 = x - 1., x2 = x - 2., x3 = x - 3.;
-  const double w0 = -x1 * x2 * x3 * (1. / 6.), w1 = x0 * x2 * x3 * 0.5, w2 = -x0 * x1 * x3 * 0.5,
-               w3 = x0 * x1 * x2 * (1. / 6.);
-  if (last < 3) return tab[i] + (u - (double)i) * (tab[i + 1] - tab[i]);
-  return w0 * tab[i0] + w1 * tab[i0 + 1] + w2 * tab[i0 + 2] + w3 * tab[i0 + 3];
+  const double *tab = ip.time_table;
+  const int W = ip.time_width, last = ip.time_points - 1;
+  const double u = (t - ip.time_t0) / ip.time_dt;
+  // stencil rows r0 .. r0 + rows - 1 with weights w (a single row beyond the ends)
+  int r0 = 0, rows = 1;
+  double w[4] = {1., 0., 0., 0.};
+  if (!(u > 0.)) {
+    r0 = 0;
+  } else if (u >= (double)last) {
+    r0 = last;
+  } else if (last < 3) {
+    r0 = (int)u;
+    rows = 2;
+    w[1] = u - (double)r0;
+    w[0] = 1. - w[1];
+  } else {
+    const int i = (int)u;
+    r0 = i < 1 ? 0 : (i + 2 > last ? last - 3 : i - 1);  // stencil shifted inside the table at its ends
+    rows = 4;
+    const double x0 = u - (double)r0, x1 = x0 - 1., x2 = x0 - 2., x3 = x0 - 3.;
+    w[0] = -x1 * x2 * x3 * (1. / 6.);
+    w[1] = x0 * x2 * x3 * 0.5;
+    w[2] = -x0 * x1 * x3 * 0.5;
+    w[3] = x0 * x1 * x2 * (1. / 6.);
+  }
+  auto val = [&](int c) {
+    double v = 0.;
+    for (int k = 0; k < rows; ++k) v += w[k] * tab[(size_t)(r0 + k) * W + c];
+    return v;
+  };
+  const int m = ip.time_columns;
+  int c = 0;
+  if (m & SF_TIME_FEED_T) cf.Tin = val(c++);
+  if (m & SF_TIME_MIXING_TAU) cf.tau = val(c++);
+  if (m & SF_TIME_CONV_T) cf.Tc = val(c++);
+  if (m & SF_TIME_CONV_H) cf.hc = val(c++);
+  if (m & SF_TIME_RAD_T) cf.Tr = val(c++);
+  if (m & SF_TIME_RAD_EPS) cf.eps = val(c++);
+  if ((m & SF_TIME_FEED_Y) && ybuf) {
+    __syncwarp();
+    for (int k = threadIdx.x & 31; k < ns; k += 32) ybuf[k] = val(c + k);
+    __syncwarp();
+    cf.yin = ybuf;
+  }
 }
 
 __device__ __forceinline__ double warp_max(double v)
@@ -155,6 +186,8 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
   double *dinv = after + (p.prec == 1 ? lu32_doubles + neq : 0) + (neq + 1) / 2 + 1;
   float *rf = xf + neq;
   const int Tidx = p.cfg.configuration == 1 ? 1 : 0;
+  // feed mass fractions of a time table: the last ns doubles of the warp's shared region
+  double *ybuf = (p.ip.time_table && (p.ip.time_columns & SF_TIME_FEED_Y)) ? base + p.per_warp - m.ns : nullptr;
   NoJ noj;
 
   for (;;) {
@@ -169,7 +202,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
     // reactor options with the feed temperature of the current evaluation; t_rhs: time of the most recent
     // right-hand side, whose feed the next Jacobian uses
     ReactorCfg cf = p.cfg;
-    double t_rhs = ip.feed_jac_t0;
+    double t_rhs = ip.time_jac_t0;
     double t = 0., dt = ip.first_time_step;
     double tau_interp = nan("");  // first crossing of T0 + delta, Hermite-interpolated
     bool setup = true;
@@ -183,7 +216,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
       if (coerce && t + dt > ip.stop_at_time) dt = ip.stop_at_time - t;
       if (setup) {
         IterMatrix im{A, neq, dt * kGamma};
-        if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs);
+        if (p.ip.time_table) apply_time_params(p, cf, t_rhs, ybuf, m.ns);
         reactor_eval<32, true, kIntegratorUnroll, OPEN>(m, b, L, scr, grp, y, pres, cf, p.pg, f, im);
         __syncwarp();
         if (p.prec == 1) {
@@ -212,14 +245,16 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
         for (int i = lane; i < neq; i += 32) slot[2 + i] = y[i];
       }
       // ---------------- one ESDIRK64 step (methods.py:502-612)
-      if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs = t);
+      t_rhs = t;
+      if (p.ip.time_table) apply_time_params(p, cf, t_rhs, ybuf, m.ns);
       reactor_eval<32, false, kIntegratorUnroll, OPEN>(m, b, L, scr, grp, y, pres, cf, p.pg, k, noj);
       for (int i = lane; i < neq; i += 32) Y[i] = y[i];
       __syncwarp();
       bool nl_ok = true;
       for (int s = 1; s < 6; ++s) {
         const double *kprev = k + (s - 1) * neq;
-        if (OPEN) cf.Tin = feed_temperature_at(p, t_rhs = t + c_c[s] * dt);
+        t_rhs = t + c_c[s] * dt;
+        if (p.ip.time_table) apply_time_params(p, cf, t_rhs, ybuf, m.ns);
         for (int i = lane; i < neq; i += 32) {
           double pr = 0.;
           for (int j = s - 1; j >= 0; --j) pr += c_a[s][j] * k[j * neq + i];  // a_s,s-1 k_s-1 + ... + a_s1 k_1
@@ -372,12 +407,14 @@ __global__ void __launch_bounds__(256) integrate_kernel(const IntParams p)
 
 // Shared memory per warp. global_scratch: the Griffon scratch lives in a global slot; global_matrix: the iteration
 // matrix and the FP32 factors too, leaving the vectors and pivots in shared memory.
-size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scratch, bool global_matrix)
+size_t per_warp_doubles(const HostMech &hm, int neq, int prec, bool global_scratch, bool global_matrix,
+                        bool feed_y_table = false)
 {
   const size_t n2 = (size_t)neq * neq;
   return (global_matrix ? 0 : n2) + 12 * (size_t)neq + (global_scratch ? 0 : hm.sl.total) +
          (prec == 1 ? (global_matrix ? 0 : (n2 + 1) / 2) + (size_t)neq : 0) + ((size_t)neq + 1) / 2 + 2 +
-         (size_t)neq;  // the last: reciprocals of U's diagonal
+         (size_t)neq +                           // reciprocals of U's diagonal
+         (feed_y_table ? (size_t)hm.dm.ns : 0);  // interpolated feed mass fractions
 }
 
 size_t matrix_doubles(int neq, int prec)
@@ -392,7 +429,7 @@ struct IntShape {
 };
 
 // Warps per block and grid of the persistent launch (autotuned knobs, else as many warps as fit)
-IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n)
+IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n, bool feed_y_table = false)
 {
   int dev, smem_max, nsm;
   CUDA_THROW(cudaGetDevice(&dev));
@@ -400,7 +437,7 @@ IntShape integrate_shape(const HostMech &hm, int neq, int prec, int n)
   CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   IntShape s{};
   const bool gs = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] >= 1, gm = hm.tune[SF_TUNE_INTEGRATE_SCRATCH] == 2;
-  s.per_warp = per_warp_doubles(hm, neq, prec, gs, gm);
+  s.per_warp = per_warp_doubles(hm, neq, prec, gs, gm, feed_y_table);
   const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
   int fit = (int)std::min<size_t>(8, avail / (s.per_warp * 8));
   if (fit < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the shared-memory integrator");
@@ -427,9 +464,14 @@ size_t sf_integrate_workspace_size(const sf_mech *mech, const sf_reactor_params 
   try {
     const HostMech &hm = mech->m;
     const int neq = params->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
-    // both linear precisions: the larger of the two scratch needs
-    const IntShape a = integrate_shape(hm, neq, 0, n < 1 ? 1 : n), b = integrate_shape(hm, neq, 1, n < 1 ? 1 : n);
-    return 256 + std::max(a.scratch_bytes + a.mat_bytes, b.scratch_bytes + b.mat_bytes);
+    // both linear precisions, with or without a feed mass-fraction table: the largest scratch need
+    size_t most = 0;
+    for (int prec = 0; prec <= 1; ++prec)
+      for (int fy = 0; fy <= 1; ++fy) {
+        const IntShape a = integrate_shape(hm, neq, prec, n < 1 ? 1 : n, fy != 0);
+        most = std::max(most, a.scratch_bytes + a.mat_bytes);
+      }
+    return 256 + most;
   } catch (...) {
     return 256;
   }
@@ -448,8 +490,19 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     if (rp->open) {
       if (!rp->inflow_Y || !(rp->tau > 0.))
         throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs feed mass fractions and a positive mixing time");
-      if (ip->feed_temperature_table ? (ip->feed_points < 2 || !(ip->feed_dt > 0.)) : !(rp->inflow_temperature > 0.))
+      const bool t_table = ip->time_table && (ip->time_columns & SF_TIME_FEED_T);
+      if (!t_table && !(rp->inflow_temperature > 0.))
         throw sf_error(SF_ERR_INVALID_ARGUMENT, "open reactor needs a feed temperature (constant or table)");
+    }
+    if (ip->time_table) {
+      const int m = ip->time_columns;
+      int width = 0;
+      for (int bit = 1; bit <= SF_TIME_RAD_EPS; bit <<= 1) width += (m & bit) ? 1 : 0;
+      if (m & SF_TIME_FEED_Y) width += mech->m.dm.ns;
+      if (m & ~127) throw sf_error(SF_ERR_INVALID_ARGUMENT, "unknown bit in time_columns");
+      if (ip->time_points < 2 || !(ip->time_dt > 0.) || ip->time_width < width)
+        throw sf_error(SF_ERR_INVALID_ARGUMENT, "time table needs >= 2 points, a positive spacing and a column for "
+                                                "every parameter of time_columns");
     }
     if (ip->linear_precision != 0 && ip->linear_precision != 1)
       throw sf_error(SF_ERR_INVALID_ARGUMENT, "linear_precision must be 0 or 1");
@@ -484,7 +537,6 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.cfg.Tin = rp->inflow_temperature;
     p.cfg.yin = rp->inflow_Y;
     p.ip = *ip;
-    if (!rp->open) p.ip.feed_temperature_table = nullptr;
     if (p.ip.maximum_time_step_count <= 0) p.ip.maximum_time_step_count = 2147483647;
     p.n = n;
     p.neq = rp->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
@@ -499,7 +551,8 @@ static int integrate_impl(const sf_mech *mech, const sf_reactor_params *rp, cons
     p.queue = static_cast<unsigned int *>(workspace);
     p.rec = record;
     p.rec_cap = record_cap;
-    const IntShape sh = integrate_shape(hm, p.neq, p.prec, n);
+    const IntShape sh = integrate_shape(hm, p.neq, p.prec, n,
+                                        ip->time_table && (ip->time_columns & SF_TIME_FEED_Y));
     if (workspace_bytes < 256 + sh.scratch_bytes + sh.mat_bytes)
       throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_integrate_workspace_size reports");
     p.per_warp = sh.per_warp;

@@ -17,7 +17,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
-from ._desc import SfIntegrateParams, reactor_params
+from ._desc import TIME_PARAMS, SfIntegrateParams, reactor_params
 
 STATUS_NAMES = {0: 'running', 1: 'done', 2: 'ignited', 3: 'steady', 4: 'max_steps', 5: 'nan', 6: 'no_ignition',
                 7: 'record_full'}
@@ -36,10 +36,13 @@ class BatchIntegrator:
     """Batched ESDIRK64 integration of reactors that share a mechanism, configuration, heat transfer and feed.
 
     heat_transfer 'diathermal' takes convection_temperature, radiation_temperature, convection_coefficient,
-    radiative_emissivity and surface_area_to_volume (constants). mass_transfer 'open' takes mixing_tau, the feed
-    mass fractions feed_mass_fractions (ns values), feed_density (isochoric) and feed_temperature: a number, or a
-    function of time evaluated on a table that the device interpolates linearly (reactors.py:335-338 evaluates it at
-    each right-hand side; the table spacing is the first time step, at most FEED_TABLE_MAX_POINTS points)."""
+    radiative_emissivity and surface_area_to_volume. mass_transfer 'open' takes mixing_tau, the feed mass fractions
+    feed_mass_fractions (ns values), feed_density (isochoric) and feed_temperature. Each of convection_temperature,
+    radiation_temperature, convection_coefficient, radiative_emissivity, mixing_tau, feed_temperature and
+    feed_mass_fractions may be a function of time (absolute time; an array of ns values for the mass fractions),
+    as in the reference (reactors.py:253-341): it is evaluated on a table of integration times that the device
+    interpolates, and every right-hand side takes the parameters at its own time, every Jacobian those of the most
+    recent right-hand side. A feed_density function is evaluated once, at t = 0, as the reference does."""
 
     def __init__(self, mech, configuration='isobaric', heat_transfer='adiabatic', pressure=101325.,
                  linear_precision=0, refine_sweeps=2, rates_option=0, mass_transfer='closed', mixing_tau=None,
@@ -54,6 +57,8 @@ class BatchIntegrator:
         self.g = mech.griffon
         self.configuration = configuration
         self.open = mass_transfer == 'open'
+        value0 = lambda v: v(0.) if callable(v) else v
+        self._time_funcs = {}  # parameter name -> function of absolute time
         kw = {}
         if heat_transfer == 'diathermal':
             for name, v in (('convection_temperature', convection_temperature),
@@ -64,27 +69,30 @@ class BatchIntegrator:
                 if v is None:
                     raise ValueError(f'diathermal reactors need {name}')
                 if callable(v):
-                    raise NotImplementedError(f'a time-dependent {name} is not on the GPU path')
-            kw = dict(fluid_temperature=convection_temperature, surface_temperature=radiation_temperature,
-                      h_convection=convection_coefficient, eps_radiation=radiative_emissivity,
-                      surface_area_to_volume=surface_area_to_volume)
-        self._feed_T = None
+                    if name == 'surface_area_to_volume':
+                        raise ValueError('surface_area_to_volume is a constant (the reactor shape)')
+                    self._time_funcs[name] = v
+            kw = dict(fluid_temperature=float(value0(convection_temperature)),
+                      surface_temperature=float(value0(radiation_temperature)),
+                      h_convection=float(value0(convection_coefficient)),
+                      eps_radiation=float(value0(radiative_emissivity)),
+                      surface_area_to_volume=float(surface_area_to_volume))
         self._feed_Y = None
         if self.open:
             if mixing_tau is None or feed_temperature is None or feed_mass_fractions is None:
                 raise ValueError('open reactors need mixing_tau, feed_temperature and feed_mass_fractions')
             if configuration == 'isochoric' and feed_density is None:
                 raise ValueError('open isochoric reactors need feed_density')
-            for name, v in (('mixing_tau', mixing_tau), ('feed_mass_fractions', feed_mass_fractions),
-                            ('feed_density', feed_density)):
+            for name, v in (('mixing_tau', mixing_tau), ('feed_temperature', feed_temperature),
+                            ('feed_mass_fractions', feed_mass_fractions)):
                 if callable(v):
-                    raise NotImplementedError(f'a time-dependent {name} is not on the GPU path')
-            self._feed_Y = self.g._dev(np.asarray(feed_mass_fractions, dtype=np.float64).reshape(-1))
+                    self._time_funcs[name] = v
+            self._feed_Y = self.g._dev(np.asarray(value0(feed_mass_fractions), dtype=np.float64).reshape(-1))
             if self._feed_Y.numel() != mech.n_species:
                 raise ValueError('feed_mass_fractions needs one value per species')
-            self._feed_T = feed_temperature
-            kw.update(inflow_temperature=300. if callable(feed_temperature) else float(feed_temperature),
-                      inflow_density=float(feed_density or 0.), tau=float(mixing_tau),
+            # the reference evaluates a feed density function once, at t = 0 (reactors.py:280, never updated)
+            kw.update(inflow_temperature=float(value0(feed_temperature)),
+                      inflow_density=float(value0(feed_density) or 0.), tau=float(value0(mixing_tau)),
                       inflow_Y_ptr=self._feed_Y.data_ptr())
         self.params = reactor_params(configuration, heat_transfer, self.open, pressure=pressure, **kw)
         self.linear_precision = linear_precision
@@ -93,15 +101,37 @@ class BatchIntegrator:
         self._graph = None
         self._table = None
 
+    def _time_table(self, ta):
+        """[len(ta), width] values of the time-dependent parameters at absolute times ta, columns in the order of
+        their sf_time_param bits; and the bit mask."""
+        ns = self.mech.n_species
+        cols, mask = [], 0
+        for name, bit in TIME_PARAMS:
+            f = self._time_funcs.get(name)
+            if f is None:
+                continue
+            mask |= bit
+            if name == 'feed_mass_fractions':
+                cols.append(np.array([np.asarray(f(x), dtype=np.float64).reshape(ns) for x in ta]))
+                continue
+            try:
+                vals = np.asarray(f(ta), dtype=np.float64)
+                if vals.shape != ta.shape:
+                    raise ValueError
+            except Exception:
+                vals = np.array([float(f(x)) for x in ta])
+            cols.append(vals[:, None])
+        return np.ascontiguousarray(np.hstack(cols)), mask
+
     def controls(self, stop_at_time=None, delta_temperature_ignition=None, stop_at_steady=None,
                  first_time_step=1.e-6, max_time_step=1.e6, transient_tolerance=1.e-10, nonlinear_tolerance=1.e-12,
                  minimum_time_step_count=40, maximum_time_step_count=None, max_nonlinear_iter=20,
                  maximum_steps_per_jacobian=1, minimum_allowable_residual=1.e-12, max_attempts=500000,
                  time_offset=0., first_jacobian_feed_time=0., feed_horizon=1.):
-        """Integration controls. time_offset: the reactors' current time (a feed function is evaluated at
-        time_offset + integration time). first_jacobian_feed_time: the absolute time whose feed the first Jacobian
-        takes (0 for a new reference reactor). feed_horizon: integration time a feed table covers when stop_at_time
-        is not given."""
+        """Integration controls. time_offset: the reactors' current time (a parameter function is evaluated at
+        time_offset + integration time). first_jacobian_feed_time: the absolute time whose parameters the first
+        Jacobian takes (0 for a new reference reactor). feed_horizon: integration time a parameter table covers when
+        stop_at_time is not given."""
         ip = SfIntegrateParams()
         ip.first_time_step = first_time_step
         ip.max_time_step = max_time_step
@@ -119,25 +149,21 @@ class BatchIntegrator:
         ip.refine_sweeps = self.refine_sweeps
         ip.rates_option = self.rates_option
         ip.max_attempts = max_attempts
-        ip.feed_jac_t0 = float(first_jacobian_feed_time) - float(time_offset)
-        if self.open and callable(self._feed_T):
+        ip.time_jac_t0 = float(first_jacobian_feed_time) - float(time_offset)
+        if self._time_funcs:
             horizon = stop_at_time if stop_at_time is not None else feed_horizon
-            t_lo = min(0., ip.feed_jac_t0)
+            t_lo = min(0., ip.time_jac_t0)
             n = int(min(FEED_TABLE_MAX_POINTS,
                         max(FEED_TABLE_MIN_POINTS, np.ceil((horizon - t_lo) / first_time_step) + 1)))
             tl = np.linspace(t_lo, horizon, n)
-            ta = tl + float(time_offset)
-            try:
-                vals = np.asarray(self._feed_T(ta), dtype=np.float64)
-                if vals.shape != ta.shape:
-                    raise ValueError
-            except Exception:
-                vals = np.array([float(self._feed_T(x)) for x in ta])
-            self._table = self.g._dev(vals)
-            ip.feed_temperature_table = C.cast(C.c_void_p(self._table.data_ptr()), C.POINTER(C.c_double))
-            ip.feed_points = n
-            ip.feed_t0 = float(tl[0])
-            ip.feed_dt = float(tl[1] - tl[0])
+            tab, mask = self._time_table(tl + float(time_offset))
+            self._table = self.g._dev(tab)
+            ip.time_table = C.cast(C.c_void_p(self._table.data_ptr()), C.POINTER(C.c_double))
+            ip.time_points = n
+            ip.time_width = tab.shape[1]
+            ip.time_columns = mask
+            ip.time_t0 = float(tl[0])
+            ip.time_dt = float(tl[1] - tl[0])
         return ip
 
     def allocate(self, n):
@@ -300,8 +326,10 @@ def _join_trajectories(lib1, lib2, first_and_last_only=False):
 
 class HomogeneousReactor:
     """Drop-in for spitfire.chemistry.reactors.HomogeneousReactor (reactors.py:27-794): closed or open (mass
-    exchange with a feed), adiabatic, isothermal or diathermal, isobaric or isochoric. Time-dependent parameters are
-    supported for the feed temperature (tabulated for the device); the other parameters are constants."""
+    exchange with a feed), adiabatic, isothermal or diathermal, isobaric or isochoric. The convection and radiation
+    temperatures, convection coefficient, emissivity, mixing time, feed temperature and feed mass fractions may be
+    functions of time, tabulated for the device (see BatchIntegrator); a feed density function is evaluated at
+    t = 0, as the reference does."""
 
     def __init__(self, mech_spec, initial_mixture, configuration, heat_transfer, mass_transfer,
                  convection_temperature=None, radiation_temperature=None, convection_coefficient=None,

@@ -264,3 +264,67 @@ def test_plain_integrator_form_matches_reference_and_oracle(cuda):
         assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
         assert abs(tau[i] - r['t']) / r['t'] <= 1e-6, (i, tau[i], r['t'])
     assert spec.griffon.device_status() == 0
+
+
+def _time_dependent_params(spec, yin):
+    """Functions of time for every parameter the reference lets vary (reactors.py:253-341)."""
+    yn2 = np.zeros(spec.n_species)
+    yn2[spec.species_index('N2')] = 1.
+    w = 2. * np.pi
+    return dict(feed_temperature=lambda t: 900. + 200. * np.sin(w * t / 2.e-3),
+                mixing_tau=lambda t: 2.e-3 * (1. + 0.5 * np.sin(w * t / 3.e-3)),
+                feed_mass_fractions=lambda t: (1. - 0.25 * (1. - np.cos(w * t / 4.e-3))) * yin +
+                0.25 * (1. - np.cos(w * t / 4.e-3)) * yn2,
+                convection_temperature=lambda t: 500. + 2.e4 * t,
+                convection_coefficient=lambda t: 20. * (1. + 200. * t),
+                radiation_temperature=lambda t: 600. - 50. * np.sin(w * t / 2.5e-3),
+                radiative_emissivity=lambda t: 0.5 + 0.2 * np.sin(w * t / 3.5e-3))
+
+
+@pytest.mark.parametrize('configuration', ['isobaric', 'isochoric'])
+def test_time_dependent_parameters_match_oracle(cuda, configuration):
+    """Open, diathermal GRI-3.0 reactors whose feed temperature, feed mass fractions, mixing time, convection and
+    radiation temperatures, convection coefficient and emissivity all vary in time (and, isochoric, whose feed
+    density is a function the reference evaluates at t = 0 only): the batched integrator against the oracle's
+    restatement of the reference's closures, reactor by reactor (status and accepted steps equal, final state
+    within 1e-6), and the drop-in HomogeneousReactor with the same functions."""
+    import integrate as I
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.reactors import BatchIntegrator, HomogeneousReactor
+    spec, og = pair('methane-gri30')
+    n = 4
+    d = W.ignition_batch(spec, n, seed=93, T_range=(1150., 1400.))
+    yin = np.array(d['q0'][0, 1:].tolist() + [1. - d['q0'][0, 1:].sum()])
+    q0 = d['q0']
+    if configuration == 'isochoric':
+        mw = spec.molecular_weights
+        Yf = np.hstack([q0[:, 1:], 1. - q0[:, 1:].sum(1, keepdims=True)])
+        rho = 101325. / (8314.46261815324 * q0[:, 0] * (Yf / mw).sum(1))
+        q0 = np.hstack([rho[:, None], q0])
+    fn = _time_dependent_params(spec, yin)
+    rho_in = lambda t: 0.4 + 100. * t  # evaluated at t = 0 only, as the reference does
+    bi = BatchIntegrator(spec, configuration, 'diathermal', pressure=101325., mass_transfer='open',
+                         feed_density=rho_in, surface_area_to_volume=30., **fn)
+    out = bi.run(q0, stop_at_time=5.e-3)
+    qg, st, cnt = out['q'].cpu().numpy(), out['status'].cpu().numpy(), out['counts'].cpu().numpy()
+    for i in range(n):
+        prob = I.OpenReactorProblem(og, configuration, fn['feed_temperature'], fn['feed_mass_fractions'],
+                                    fn['mixing_tau'], pressure=101325., heat='diathermal', feed_density=rho_in,
+                                    convection_temperature=fn['convection_temperature'],
+                                    radiation_temperature=fn['radiation_temperature'],
+                                    convection_coefficient=fn['convection_coefficient'],
+                                    radiative_emissivity=fn['radiative_emissivity'], surface_area_to_volume=30.)
+        r = I.integrate(prob, q0[i], stop_at_time=5.e-3)
+        assert st[i] == r['status'], i
+        assert cnt[i, 0] == r['steps'], (i, cnt[i], r['steps'])
+        assert np.max(np.abs(qg[i] - r['state']) / np.maximum(np.abs(r['state']), 1e-3)) <= 1e-6, i
+    # the drop-in reactor: the same functions through HomogeneousReactor, against the batch's first reactor
+    mix = spec.stream('TPY', (float(d['T0'][0]), 101325., {s: float(v) for s, v in zip(spec.species_names, d['Y'][0])}))
+    hr = HomogeneousReactor(spec, mix, configuration=configuration, heat_transfer='diathermal',
+                            mass_transfer='open', feed_density=rho_in,
+                            shape_dimension_dict={'shape': 'cube', 'char. length': 0.2}, **fn)  # 30 1/m
+    lib = hr.integrate_to_time(5.e-3)
+    assert hr.last_counts['steps'] == cnt[0, 0], (hr.last_counts, cnt[0])
+    Ti = 1 if configuration == 'isochoric' else 0
+    assert abs(lib['temperature'][-1] - qg[0, Ti]) / qg[0, Ti] < 1e-9
+    assert spec.griffon.device_status() == 0
