@@ -10,9 +10,18 @@
 //                     instruction; m16n8k16: 4096), independent accumulators per warp: whether the FP64 MMA pipe
 //                     beats the DFMA pipe for the small dense block updates of the LU and Gauss-Jordan kernels
 //
-// Each launch covers 8 blocks of 256 threads per SM after a short warm-up launch, timed with CUDA events on the
-// caller's stream (which the call synchronizes). Every loop is register-only with a fixed trip count.
+//   bench_store       stores from the SMs into a buffer, device memory or pinned host memory reached over the host
+//                     link (the device address of a pinned allocation comes from cudaHostGetDevicePointer, and the
+//                     call refuses host memory without one): pattern 0 coalesced (consecutive lanes, consecutive
+//                     doubles), pattern 1 the thread-per-state Jacobian writer's (each lane fills its own 2916-double
+//                     block sequentially, the 32 lanes of a warp 23 KB apart)
+//
+// Each FP64 launch covers 8 blocks of 256 threads per SM after a short warm-up launch, timed with CUDA events on the
+// caller's stream (which the call synchronizes). Every loop is register-only with a fixed trip count, or, for the
+// stores, bounded by the buffer size the caller passes.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 namespace {
 
@@ -74,6 +83,22 @@ __global__ void dmma_m16n8k16_kernel(int iters, double seed, double *sink)
 #pragma unroll
   for (int k = 0; k < 4; ++k) s += c[k][0] + c[k][1] + c[k][2] + c[k][3];
   if (s == 12345.678) sink[0] = s;
+}
+
+// pattern 0: grid-stride over doubles; pattern 1: lane-owned blocks of `block` doubles written in order.
+__global__ void store_kernel(double *dst, long long n, int pattern, int block)
+{
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nt = (long long)gridDim.x * blockDim.x;
+  if (pattern == 0) {
+    for (long long i = tid; i < n; i += nt) dst[i] = (double)i;
+  } else {
+    const long long nblocks = n / block;
+    for (long long b = tid; b < nblocks; b += nt) {
+      double *o = dst + b * block;
+      for (int k = 0; k < block; ++k) o[k] = (double)k;
+    }
+  }
 }
 
 template <class L>
@@ -148,6 +173,41 @@ int bench_fp64_dmma(int iters, int which, double *out_tflops, double *sink, void
   const double chains = which == 0 ? 8.0 : 4.0;
   const double flops = per_instr * chains * (double)iters * blocks * (threads / 32);
   *out_tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+// GB/s of stores into `buffer` (bytes, a device allocation or a pinned host allocation).
+int bench_store(void *buffer, long long bytes, int pattern, double *out_gbs, void *stream)
+{
+  if (!buffer || bytes < 8 || (pattern != 0 && pattern != 1) || !out_gbs) return 2;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, buffer) != cudaSuccess) return 3;
+  double *dst = nullptr;
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+    dst = static_cast<double *>(buffer);
+  } else if (attr.type == cudaMemoryTypeHost) {
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, buffer, 0) != cudaSuccess || !d) return 4;
+    dst = static_cast<double *>(d);
+  } else {
+    return 5;  // pageable host memory: not written from the device here
+  }
+  const int block = 2916;
+  const long long n = pattern == 0 ? bytes / 8 : (bytes / 8 / block) * block;
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t st = (cudaStream_t)stream;
+  // pattern 1: one lane per block, 8 resident warps of 4-warp blocks per SM, as the Jacobian kernel runs
+  const int threads = pattern == 0 ? 256 : 128;
+  const int blocks = pattern == 0 ? nsm * 8 : nsm * 2;
+  float ms = 0.f;
+  const int rc = timed(st, [&](int it) {
+    store_kernel<<<blocks, threads, 0, st>>>(dst, it < 0 ? n : std::min<long long>(n, (long long)block * 64),
+                                             pattern, block);
+  }, &ms);
+  if (rc) return rc;
+  *out_gbs = (double)n * 8 / (ms * 1e-3) / 1e9;
   return 0;
 }
 
