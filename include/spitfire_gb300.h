@@ -481,6 +481,48 @@ int sf_btddod_scale_and_add_block_diagonal_batch(int n_flamelets, int ns, const 
                                                  double *values, double matrix_scale, const double *block_diag,
                                                  double diag_scale, const int *active, void *stream);
 
+/* Steady flamelet solvers for every flamelet of a batch, each with its own iteration count, line search, Jacobian
+ * reuse and (psitc) pseudo-time steps and restarts: Flamelet.steady_solve_newton (flamelet.py:1352-1485) and
+ * Flamelet.steady_solve_psitc (flamelet.py:1487-1703), which a Python caller runs one flamelet at a time. Both
+ * replace the per-flamelet solver loop of Flamelet.compute_steady_state (flamelet.py:1705-1778) for a batch.
+ * Every vector operation, norm and per-flamelet decision runs on the device; the call synchronizes `stream` a few
+ * times per iteration to read whether any flamelet still iterates, needs a new Jacobian, cuts its step or
+ * restarts. state: DEVICE [points][ns] in/out, the initial guess on entry; on return each flamelet's last iterate,
+ * clamped at 0 (as the reference's solvers return it). active: DEVICE int [n_flamelets] or NULL; inactive
+ * flamelets are not iterated (their state is still clamped) and report converged 0. fb->active, fb->prefactor and
+ * fb->diffterm are ignored. Norms are the reference's: the infinity norm of the residual with the temperature rows
+ * divided by 1e3. out_converged, out_iterations: DEVICE int [n_flamelets]; out_min_ds (psitc, DEVICE
+ * [n_flamelets] or NULL): the smallest pseudo-time step of each flamelet where it stopped (the reference's psitc
+ * returns it and compute_steady_state starts its ESDIRK fallback from 1e-2 of it). Factors and Jacobians live in
+ * the workspace (sf_flamelet_steady_workspace_size bytes, DEVICE, 256-byte aligned); a call uses it alone.
+ *
+ * Newton: damped Newton with a Jacobian reused until a line search cut; the line search halves the step (at most
+ * 12 times, while alpha > 1e-3) while the new residual norm exceeds max_factor_line_search times the old one. A
+ * flamelet fails on a non-finite step or residual, a residual above max_allowed_residual, or a state value below
+ * min_allowable_state_var; it converges when its residual norm is <= tolerance within max_iterations. */
+size_t sf_flamelet_steady_workspace_size(const sf_mech *mech, const sf_flamelet_batch *fb);
+int sf_flamelet_steady_newton_batch(const sf_mech *mech, const sf_flamelet_batch *fb, double *state,
+                                    const int *active, double tolerance, int max_iterations,
+                                    double max_factor_line_search, double max_allowed_residual,
+                                    double min_allowable_state_var, int rates_option, int *out_converged,
+                                    int *out_iterations, void *workspace, size_t workspace_bytes, void *stream);
+/* psitc: pseudo-transient continuation, (ds^-1 I - J) dx = r with a per-row pseudo-time step ds refreshed with every
+ * Jacobian: ds <- min(ds_safety / (expeig + 1e-16), ds_ramp * ds, ds_max), expeig the eigenvalue bound of
+ * sf_flamelet_jac_batch with diffterm[f] (DEVICE [n_flamelets], the reference's diffusion_factor * max(chi) of each
+ * flamelet), and on a flamelet's first Jacobian (or every one with global_ds) the flamelet's smallest ds on all its
+ * rows. The Jacobian is refreshed after 8 uses or while the residual norm exceeds 1e-2, and after a line search
+ * cut. A failure (non-finite step or residual, residual above max_allowed_residual, state below
+ * min_allowable_state_var) restarts the flamelet from its initial guess with ds_init divided by ds_init_decrease
+ * (adaptive_restart), until a failure at restart depth > max_recursion_depth ends it unconverged. */
+int sf_flamelet_steady_psitc_batch(const sf_mech *mech, const sf_flamelet_batch *fb, double *state,
+                                   const int *active, const double *diffterm, double tolerance, int max_iterations,
+                                   double min_allowable_state_var, double ds_init, double ds_init_decrease,
+                                   int global_ds, double ds_safety, double ds_ramp, double ds_max,
+                                   double max_factor_line_search, double max_allowed_residual,
+                                   int max_recursion_depth, int adaptive_restart, int rates_option,
+                                   int *out_converged, int *out_iterations, double *out_min_ds, void *workspace,
+                                   size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,6 +79,14 @@ def _declare(L):
     L.sf_btddod_triangle_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _ip, _vp, _vp]
     L.sf_btddod_scale_and_add_block_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                                                C.c_double, _vp, _vp]
+    L.sf_flamelet_steady_workspace_size.argtypes = [_vp, C.POINTER(SfFlameletBatch)]
+    L.sf_flamelet_steady_workspace_size.restype = C.c_size_t
+    _d = C.c_double
+    L.sf_flamelet_steady_newton_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _vp, _d, _ip, _d, _d, _d,
+                                                  _ip, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.sf_flamelet_steady_psitc_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _vp, _vp, _d, _ip, _d, _d, _d,
+                                                 _ip, _d, _d, _d, _d, _d, _ip, _ip, _ip, _vp, _vp, _vp, _vp,
+                                                 C.c_size_t, _vp]
 
 
 # Entry points declared in include/spitfire_gb300.h (the C-ABI test checks the library exports all of them).
@@ -96,7 +104,8 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_mech_layout', 'sf_btddod_blockdiag_factor_batch',
             'sf_btddod_blockdiag_matvec_batch', 'sf_btddod_triangle_solve_batch',
             'sf_btddod_scale_and_add_block_diagonal_batch', 'sf_chem_workspace_size',
-            'sf_flamelet_jac_workspace_size']
+            'sf_flamelet_jac_workspace_size', 'sf_flamelet_steady_workspace_size',
+            'sf_flamelet_steady_newton_batch', 'sf_flamelet_steady_psitc_batch']
 
 
 def load(path=None):

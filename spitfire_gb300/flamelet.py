@@ -447,10 +447,61 @@ class FlameletBatch:
         return per_flamelet[self.dof_flamelet]
 
     # ------------------------------------------------------------------------------------------ solvers
+    def _steady_ws(self):
+        torch = _torch()
+        if getattr(self, '_steady_wsb', None) is None:
+            nb = int(N.load().sf_flamelet_steady_workspace_size(self.g.handle, C.byref(self.fb)))
+            self._steady_wsb = torch.empty((nb + 7) // 8, dtype=torch.float64, device=self.values.device)
+        return self._steady_wsb
+
+    def _steady_common(self, state, active):
+        torch = _torch()
+        dev = state.device
+        state = state.clone().contiguous()
+        m = None if active is None else active.to(dtype=torch.int32).contiguous()
+        conv = torch.empty(self.nf, dtype=torch.int32, device=dev)
+        it = torch.empty(self.nf, dtype=torch.int32, device=dev)
+        return state, m, conv, it, self._steady_ws()
+
     def steady_solve_newton(self, state, active=None, tolerance=1.e-6, max_iterations=10,
                             max_factor_line_search=1.5, max_allowed_residual=1.e6, min_allowable_state_var=-1.e-6):
-        """Batched restatement of Flamelet.steady_solve_newton (flamelet.py:1352-1485). Returns (state,
-        converged[nf] bool, iterations[nf]). The factors of a flamelet stay in place until it needs new ones."""
+        """Flamelet.steady_solve_newton (flamelet.py:1352-1485) for every flamelet of the batch at once, on the
+        native batched solver (sf_flamelet_steady_newton_batch). Returns (state, converged[nf] bool,
+        iterations[nf])."""
+        state, m, conv, it, ws = self._steady_common(state, active)
+        N.check(N.load().sf_flamelet_steady_newton_batch(
+            self.g.handle, C.byref(self.fb), N.ptr(state), N.ptr(m), float(tolerance), int(max_iterations),
+            float(max_factor_line_search), float(max_allowed_residual), float(min_allowable_state_var),
+            int(self.rates_option), N.ptr(conv), N.ptr(it), N.ptr(ws), ws.numel() * 8, N.stream_handle()))
+        return state, conv.bool(), it.long()
+
+    def steady_solve_psitc(self, initial, active=None, tolerance=1.e-6, max_iterations=400,
+                           min_allowable_state_var=-1.e-6, ds_init=1., ds_init_decrease=4., diffusion_factor=4.,
+                           global_ds=False, ds_safety=0.1, ds_ramp=1.1, ds_max=1.e4, max_factor_line_search=1.5,
+                           max_allowed_residual=1.e6, max_recursion_depth=20, adaptive_restart=True):
+        """Flamelet.steady_solve_psitc (flamelet.py:1487-1703) for every flamelet of the batch at once, with its
+        restart from the initial guess after a failure, on the native batched solver
+        (sf_flamelet_steady_psitc_batch). Returns (state, converged[nf] bool, iterations[nf]) and leaves each
+        flamelet's smallest pseudo-time step where it stopped in last_psitc_min_ds."""
+        torch = _torch()
+        state, m, conv, it, ws = self._steady_common(initial, active)
+        dterm = self.diffterm_tensor(diffusion_factor)
+        mds = torch.empty(self.nf, dtype=torch.float64, device=state.device)
+        N.check(N.load().sf_flamelet_steady_psitc_batch(
+            self.g.handle, C.byref(self.fb), N.ptr(state), N.ptr(m), N.ptr(dterm), float(tolerance),
+            int(max_iterations), float(min_allowable_state_var), float(ds_init), float(ds_init_decrease),
+            int(bool(global_ds)), float(ds_safety), float(ds_ramp), float(ds_max), float(max_factor_line_search),
+            float(max_allowed_residual), int(max_recursion_depth), int(bool(adaptive_restart)),
+            int(self.rates_option), N.ptr(conv), N.ptr(it), N.ptr(mds), N.ptr(ws), ws.numel() * 8,
+            N.stream_handle()))
+        self.last_psitc_min_ds = mds
+        return state, conv.bool(), it.long()
+
+    def steady_solve_newton_host(self, state, active=None, tolerance=1.e-6, max_iterations=10,
+                                 max_factor_line_search=1.5, max_allowed_residual=1.e6, min_allowable_state_var=-1.e-6):
+        """The same solver as steady_solve_newton with its control loop on the host, over the batch's own
+        operations (rhs, jacobian, factor, solve, norms): the native solver's arithmetic step by step, kept to check
+        it against. Returns (state, converged[nf] bool, iterations[nf])."""
         torch = _torch()
         dev = state.device
         nf = self.nf
@@ -503,13 +554,14 @@ class FlameletBatch:
         conv = run & ~failed & (res <= tolerance) & (it <= max_iterations)
         return state, conv, it
 
-    def steady_solve_psitc(self, initial, active=None, tolerance=1.e-6, max_iterations=400,
-                           min_allowable_state_var=-1.e-6, ds_init=1., ds_init_decrease=4., diffusion_factor=4.,
-                           global_ds=False, ds_safety=0.1, ds_ramp=1.1, ds_max=1.e4, max_factor_line_search=1.5,
-                           max_allowed_residual=1.e6, max_recursion_depth=20, adaptive_restart=True):
-        """Batched restatement of Flamelet.steady_solve_psitc (flamelet.py:1487-1703), including its restart from the
+    def steady_solve_psitc_host(self, initial, active=None, tolerance=1.e-6, max_iterations=400,
+                                min_allowable_state_var=-1.e-6, ds_init=1., ds_init_decrease=4., diffusion_factor=4.,
+                                global_ds=False, ds_safety=0.1, ds_ramp=1.1, ds_max=1.e4, max_factor_line_search=1.5,
+                                max_allowed_residual=1.e6, max_recursion_depth=20, adaptive_restart=True):
+        """The same solver as steady_solve_psitc with its control loop on the host, including the restart from the
         initial guess with ds_init / ds_init_decrease after a failure (a flamelet gives up once a failure happens
-        at restart depth > max_recursion_depth, or at once without adaptive_restart)."""
+        at restart depth > max_recursion_depth, or at once without adaptive_restart); kept to check the native
+        solver against."""
         torch = _torch()
         dev = initial.device
         nf, ns = self.nf, self.ns
@@ -535,7 +587,10 @@ class FlameletBatch:
             need = go & eval_j
             if bool(need.any()):
                 _, expeig = self.jacobian(state, eig=True, diffterm_per_flamelet=dterm, active=need)
-                new_ds = torch.minimum(torch.minimum(ds_safety / (expeig + 1.e-16), ds_ramp * ds),
+                # a true division, as numpy's ds_safety / (expeig + 1e-16) in the reference (torch evaluates
+                # scalar / tensor as scalar * reciprocal(tensor), two roundings)
+                safe = torch.div(torch.full_like(expeig, float(ds_safety)), expeig + 1.e-16)
+                new_ds = torch.minimum(torch.minimum(safe, ds_ramp * ds),
                                        torch.full_like(ds, ds_max))
                 first = need & ((it == 1) | global_ds)
                 mn = torch.full((nf,), float('inf'), dtype=torch.float64, device=dev).scatter_reduce(

@@ -472,3 +472,36 @@ def test_adiabatic_ignition_transient_matches_reference(cuda):
     assert t[-1] == 2.e-3
     np.testing.assert_allclose(lib['temperature'][-1], g['ign_T'][-1], rtol=1e-6)
     assert m.griffon.device_status() == 0
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_native_steady_solvers_match_host_loop(cuda, name):
+    """sf_flamelet_steady_newton_batch / sf_flamelet_steady_psitc_batch against the same solvers with their control
+    loop on the host (FlameletBatch.steady_solve_*_host): both run the same device operations in the same order,
+    so states, convergence flags, iteration counts and the last pseudo-time steps agree bit for bit, with a run
+    mask, with failures that restart psitc (a low max_allowed_residual) and with a restart depth that gives up."""
+    import torch
+    from spitfire_gb300.flamelet import FlameletBatch
+    d, spec, og, setups = _setups(name)
+    setups[0].initial_state = d[name + '_ic'].copy()
+    b = FlameletBatch(setups)
+    init = b.initial_state()
+    mask = torch.tensor([True, False, True], device=init.device)
+    for kw in (dict(tolerance=1.e-6, max_iterations=38), dict(tolerance=1.e-6, max_iterations=38, active=mask),
+               dict(tolerance=1.e-6, max_iterations=5, max_factor_line_search=1.01)):
+        a = b.steady_solve_newton(init, **kw)
+        h = b.steady_solve_newton_host(init, **kw)
+        assert torch.equal(a[1], h[1]) and torch.equal(a[2], h[2]), (kw, a[1:], h[1:])
+        assert torch.equal(a[0], h[0]), kw
+    for kw in (dict(tolerance=1.e-6, max_iterations=400), dict(tolerance=1.e-6, max_iterations=400, active=~mask),
+               dict(tolerance=1.e-6, max_iterations=60, max_allowed_residual=30., max_recursion_depth=2),
+               dict(tolerance=1.e-6, max_iterations=60, global_ds=True, ds_init=10.),
+               dict(tolerance=1.e-6, max_iterations=60, max_allowed_residual=30., adaptive_restart=False)):
+        a = b.steady_solve_psitc(init, **kw)
+        mds_a = b.last_psitc_min_ds.clone()
+        h = b.steady_solve_psitc_host(init, **kw)
+        mds_h = b.last_psitc_min_ds.clone()
+        assert torch.equal(a[1], h[1]) and torch.equal(a[2], h[2]), (kw, a[1:], h[1:])
+        assert torch.equal(a[0], h[0]), kw
+        assert torch.equal(mds_a, mds_h), (kw, mds_a, mds_h)
+    assert spec.griffon.device_status() == 0
