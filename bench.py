@@ -738,6 +738,7 @@ def _probes():
         L.bench_fp64_fma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p,
                                      C.c_void_p]
         L.bench_fp64_dmma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        L.bench_fp64_mixed.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
         L.bench_store.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_double), C.c_void_p]
         _PROBES = L
     return _PROBES
@@ -766,6 +767,18 @@ def fp64_dmma_probe(iters, which=0):
                                    torch.cuda.current_stream().cuda_stream)
     if rc:
         raise RuntimeError(f'bench_fp64_dmma failed ({rc})')
+    return tf.value
+
+
+def fp64_mixed_probe(iters):
+    """TFLOP/s of a launch whose even warps run DFMA chains and odd warps FP64 m8n8k4 MMAs (equal flops)."""
+    import ctypes as C
+    import torch
+    sink = torch.zeros(1, dtype=torch.float64, device='cuda')
+    tf = C.c_double()
+    rc = _probes().bench_fp64_mixed(int(iters), C.byref(tf), sink.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    if rc:
+        raise RuntimeError(f'bench_fp64_mixed failed ({rc})')
     return tf.value
 
 
@@ -922,6 +935,7 @@ def case_dmma():
     print(f'FP64 FMA (DFMA pipe), all lanes: {tf:.3f} TFLOP/s')
     for which, name in ((0, 'm8n8k4'), (1, 'm16n8k16')):
         print(f'FP64 mma.sync {name}: {fp64_dmma_probe(2000 if which == 0 else 500, which):.3f} TFLOP/s')
+    print(f'half the warps DFMA, half m8n8k4 (equal flops): {fp64_mixed_probe(16000):.3f} TFLOP/s')
     return None
 
 

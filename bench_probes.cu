@@ -9,6 +9,8 @@
 //   bench_fp64_dmma   the same with the legacy FP64 tensor path, mma.sync .f64 (m8n8k4: 512 flops per warp
 //                     instruction; m16n8k16: 4096), independent accumulators per warp: whether the FP64 MMA pipe
 //                     beats the DFMA pipe for the small dense block updates of the LU and Gauss-Jordan kernels
+//   bench_fp64_mixed  even warps run the DFMA chains, odd warps the m8n8k4 MMAs, with equal flops per warp: about
+//                     the DFMA rate if the two share one FP64 unit, about twice it if they issue side by side
 //
 //   bench_store       stores from the SMs into a buffer, device memory or pinned host memory reached over the host
 //                     link (the device address of a pinned allocation comes from cudaHostGetDevicePointer, and the
@@ -82,6 +84,40 @@ __global__ void dmma_m16n8k16_kernel(int iters, double seed, double *sink)
   double s = 0.;
 #pragma unroll
   for (int k = 0; k < 4; ++k) s += c[k][0] + c[k][1] + c[k][2] + c[k][3];
+  if (s == 12345.678) sink[0] = s;
+}
+
+// Even warps: 8 DFMA chains for 8*iters instructions (512 flops per warp per iteration); odd warps: 8 m8n8k4 MMAs
+// every 8th iteration (4096 flops each time), the same flops per warp.
+__global__ void mixed_probe_kernel(int iters, double seed, double *sink)
+{
+  double s = 0.;
+  if (((threadIdx.x >> 5) & 1) == 0) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = seed + k * 1e-3 + threadIdx.x * 1e-7;
+    const double b = 0.999999999, c = 1e-9;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+  } else {
+    const double a = 1e-3 * (seed + threadIdx.x * 1e-7), b = 1e-3 * (0.999 - threadIdx.x * 1e-9);
+    double c[8][2];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = k * 1e-6;
+    for (int i = 0; i < iters / 8; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(c[k][0]), "+d"(c[k][1])
+                     : "d"(a), "d"(b));
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
+  }
   if (s == 12345.678) sink[0] = s;
 }
 
@@ -172,6 +208,23 @@ int bench_fp64_dmma(int iters, int which, double *out_tflops, double *sink, void
   const double per_instr = which == 0 ? 2.0 * 8 * 8 * 4 : 2.0 * 16 * 8 * 16;
   const double chains = which == 0 ? 8.0 : 4.0;
   const double flops = per_instr * chains * (double)iters * blocks * (threads / 32);
+  *out_tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+// TFLOP/s of the mixed DFMA / MMA launch (iters a multiple of 8).
+int bench_fp64_mixed(int iters, double *out_tflops, double *sink, void *stream)
+{
+  if (iters < 8 || iters % 8 || !out_tflops || !sink) return 2;
+  int blocks, threads;
+  shape(&blocks, &threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  float ms = 0.f;
+  const int rc = timed(st, [&](int it) {
+    mixed_probe_kernel<<<blocks, threads, 0, st>>>(it < 0 ? iters : it, 1.0, sink);
+  }, &ms);
+  if (rc) return rc;
+  const double flops = 512.0 * (double)iters * blocks * (threads / 32);
   *out_tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
 }
