@@ -365,6 +365,30 @@ int sf_rate_param_adjoint_batch(const sf_mech *mech, const sf_reactor_params *pa
                                 const double *q, const double *pressures, const double *w, double *out_grad,
                                 void *stream);
 
+/* Outputs of sf_adjoint_batch. SF_ADJ_T_END: the temperature at the end of the recorded integration.
+ * SF_ADJ_TAU_S: the smoothed ignition delay, the ESDIRK64 quadrature of the time spent below T0 + 400 K,
+ *   tau_s = sum_n h_n sum_s b_s g(T_ns),  g(T) = 1 - 1 / (1 + exp(-(T - T0 - 400 K) / 20 K)). */
+enum sf_adjoint_output { SF_ADJ_T_END = 0, SF_ADJ_TAU_S = 1 };
+/* Gradients of recorded closed adiabatic integrations (sf_integrate_record_batch) by the discrete adjoint of their
+ * ESDIRK64 step sequences: for every reactor and output, d/d ln A_r and d/d E_a,r of every reaction (forward, or
+ * high-pressure for falloff, Arrhenius coefficients; E_a in J/kmol) and d/d q0. Backwards over the recorded steps,
+ * all reactors at once: stage Jacobians at the recorded stages, the transposed stage systems
+ * (I - h gamma J_s^T) w_s = c_s with c_s = h b_s lam' + h sum_{l>s} a_ls Ybar_l + h gamma qd_s, Ybar_s = J_s^T w_s +
+ * qd_s, lam = lam' + sum_s Ybar_s (lam' the adjoint with the entries the step's clamp of negative values acted on
+ * zeroed, qd_s the quadrature term of tau_s), and the parameter adjoint sum_s w_s^T df/dtheta (Y_s).
+ * trajectory DEVICE [n][capacity_steps][2 + 6 neq] and counts DEVICE [n][4] as sf_integrate_record_batch wrote
+ * them; pressures DEVICE [n] (isobaric; NULL = params->pressure); T0 DEVICE [n], each reactor's initial
+ * temperature (needed by SF_ADJ_TAU_S, else may be NULL); output_kinds HOST [n_outputs] (1..8 of
+ * sf_adjoint_output). out_grad_theta DEVICE [n][n_outputs][2 n_reactions] (d/d ln A_r at 2r, d/d E_a,r at 2r+1,
+ * reactions in the order the mechanism was described), out_grad_q0 DEVICE [n][n_outputs][neq] or NULL; both
+ * overwritten. The call reads the step counts back once (a synchronization of `stream`). workspace: DEVICE,
+ * sf_adjoint_workspace_size bytes. No reference counterpart (the reference computes no sensitivities). */
+size_t sf_adjoint_workspace_size(const sf_mech *mech, const sf_reactor_params *params, int n, int n_outputs);
+int sf_adjoint_batch(const sf_mech *mech, const sf_reactor_params *params, int n, const double *trajectory,
+                     int capacity_steps, const int *counts, const double *pressures, const double *T0,
+                     int n_outputs, const int *output_kinds, double *out_grad_theta, double *out_grad_q0,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
 /* ------------------------------------------------------------------------------------------------ flamelets */
 /* Stencil coefficients (flamelet_kernels.cpp:31-48); host pointers, host computation (setup only). */
 int sf_flamelet_stencils(const sf_mech *mech, const double *dz, int nzi, const double *chi,

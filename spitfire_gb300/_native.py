@@ -79,6 +79,10 @@ def _declare(L):
     L.sf_btddod_triangle_solve_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _ip, _vp, _vp]
     L.sf_btddod_scale_and_add_block_diagonal_batch.argtypes = [_ip, _ip, _vp, _vp, _vp, _vp, C.c_double, _vp,
                                                                C.c_double, _vp, _vp]
+    L.sf_adjoint_workspace_size.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _ip]
+    L.sf_adjoint_workspace_size.restype = C.c_size_t
+    L.sf_adjoint_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _ip, _vp, _vp, _vp, _ip, _vp, _vp, _vp,
+                                   _vp, C.c_size_t, _vp]
     L.sf_flamelet_steady_workspace_size.argtypes = [_vp, C.POINTER(SfFlameletBatch)]
     L.sf_flamelet_steady_workspace_size.restype = C.c_size_t
     _d = C.c_double
@@ -105,7 +109,8 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_btddod_blockdiag_matvec_batch', 'sf_btddod_triangle_solve_batch',
             'sf_btddod_scale_and_add_block_diagonal_batch', 'sf_chem_workspace_size',
             'sf_flamelet_jac_workspace_size', 'sf_flamelet_steady_workspace_size',
-            'sf_flamelet_steady_newton_batch', 'sf_flamelet_steady_psitc_batch']
+            'sf_flamelet_steady_newton_batch', 'sf_flamelet_steady_psitc_batch', 'sf_adjoint_workspace_size',
+            'sf_adjoint_batch']
 
 
 def load(path=None):

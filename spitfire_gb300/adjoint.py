@@ -42,6 +42,7 @@ _A = np.array([[0., 0., 0., 0., 0., 0.],
 _B = _A[5].copy()
 DT_IGN = 400.
 WIDTH = 20.
+OUTPUT_KINDS = {'T_end': 0, 'tau_s': 1}  # sf_adjoint_output
 
 
 def _torch():
@@ -135,8 +136,40 @@ class ReactorAdjoint:
 
     # ------------------------------------------------------------------------------------------------ backward
     def backward(self, traj, outputs=('T_end', 'tau_s')):
-        """Gradients of the outputs of every reactor. Returns dict(theta=[n, n_out, n_reactions, 2] (d/d ln A,
-        d/d E_a) in file order, q0=[n, n_out, neq] (gradients with respect to the initial state))."""
+        """Gradients of the outputs of every reactor, by the native backward sweep (sf_adjoint_batch). Returns
+        dict(theta=[n, n_out, n_reactions, 2] (d/d ln A, d/d E_a) in file order, q0=[n, n_out, neq] (gradients with
+        respect to the initial state))."""
+        torch = _torch()
+        kinds = []
+        for name in outputs:
+            if name not in OUTPUT_KINDS:
+                raise ValueError(f'unknown output {name}')
+            kinds.append(OUTPUT_KINDS[name])
+        n, neq, nr, O = traj.q0.shape[0], self.neq, self.nr, len(outputs)
+        dev = traj.q0.device
+        theta_int = torch.empty((n, O, 2 * nr), dtype=torch.float64, device=dev)
+        q0g = torch.empty((n, O, neq), dtype=torch.float64, device=dev)
+        L = N.load()
+        if n:
+            nb = int(L.sf_adjoint_workspace_size(self.g.handle, C.byref(self.params), n, O))
+            ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=dev)
+            kk = (C.c_int * O)(*kinds)
+            T0 = traj.T0.contiguous()
+            N.check(L.sf_adjoint_batch(self.g.handle, C.byref(self.params), n, N.ptr(traj.rec), traj.rec.shape[1],
+                                       N.ptr(traj.counts), N.ptr(traj.pressures), N.ptr(T0), O,
+                                       C.cast(kk, C.c_void_p), N.ptr(theta_int), N.ptr(q0g), N.ptr(ws), nb,
+                                       N.stream_handle()))
+            del ws
+        G = theta_int.view(n, O, nr, 2)
+        yi = torch.as_tensor(self.mech.reaction_yaml_index, device=dev)
+        theta = torch.empty_like(G)
+        theta[:, :, yi] = G
+        return dict(theta=theta, q0=q0g)
+
+    def backward_host(self, traj, outputs=('T_end', 'tau_s')):
+        """The backward sweep of ``backward`` with its step loop in Python over torch operations and the batched
+        primitives (chemistry Jacobians, Newton LU/solves, the parameter adjoint): the same recursion, kept to check
+        the native sweep against."""
         torch = _torch()
         dev = traj.q0.device
         n, neq, tix, nr = traj.q0.shape[0], self.neq, self.tix, self.nr

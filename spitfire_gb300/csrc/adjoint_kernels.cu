@@ -27,11 +27,12 @@ struct AdjParams {
   Progs pg;
   ReactorCfg cfg;
   int n_items, stages, neq;
+  int wsets;                // adjoint vector sets per state (e.g. one per output)
   double pressure;
   const double *pressures;  // [n_items] or null
   const double *q;          // [n_items][stages][neq]
-  const double *w;          // [n_items][stages][neq]
-  double *out;              // [n_items][2 nr], accumulated
+  const double *w;          // [n_items][wsets][stages][neq]
+  double *out;              // [n_items][wsets][2 nr], accumulated
   int groups_per_cta;
 };
 
@@ -96,10 +97,8 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
   NoJ noj;
   for (int it = blockIdx.x * p.groups_per_cta + gid; it < p.n_items; it += gridDim.x * p.groups_per_cta) {
     const double pres = isochoric ? 0. : (p.pressures ? p.pressures[it] : p.pressure);
-    double *out = p.out + (size_t)it * 2 * nr;
     for (int st = 0; st < p.stages; ++st) {
       const double *qs = p.q + ((size_t)it * p.stages + st) * neq;
-      const double *w = p.w + ((size_t)it * p.stages + st) * neq;
       reactor_eval<G, false, default_unroll(G), false>(m, b, L, scr, grp, qs, pres, p.cfg, p.pg, rhs_tmp, noj);
       // state quantities (as in reactor_eval)
       const double T = qs[tix];
@@ -121,8 +120,6 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
       s.mmw = mmw;
       s.invM = sim;
       s.ct = rho * sim;
-      const double wT = w[tix];
-      const double wTc = wT / cmix;
       for (int r = lane; r < nr; r += G) {
         const int info = b.i[m.i_info + r];
         const int kind = (info >> RI_KIND_SHIFT) & 7;
@@ -130,16 +127,21 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
         double sr = scr[L.q + r];
         if (kind == 3 || kind == 4) sr *= falloff_factor(m, b, L, scr, s, r, kind, kform, info);
         const int n0 = b.i[m.i_net_off + r], n1 = b.i[m.i_net_off + r + 1];
-        double B = 0.;
-        for (int j = n0; j < n1; ++j) {
-          const int sp = b.i[m.i_net + j] & 0xFFFF;
-          const double wy = sp < ns - 1 ? w[tix + 1 + sp] : 0.;
-          B += b.d[m.d_netc + j] * (wy - wTc * scr[L.eh + sp]);
-        }
-        const double g = sr * B * s.invRho;
         const int ro = b.i[m.i_orig + r];  // reported in the order the mechanism was described
-        out[2 * ro] += g;
-        out[2 * ro + 1] += -g * s.invT * m.invRu;
+        for (int o = 0; o < p.wsets; ++o) {  // the rates above serve every adjoint vector of this state
+          const double *w = p.w + (((size_t)it * p.wsets + o) * p.stages + st) * neq;
+          double *out = p.out + ((size_t)it * p.wsets + o) * 2 * nr;
+          const double wTc = w[tix] / cmix;
+          double B = 0.;
+          for (int j = n0; j < n1; ++j) {
+            const int sp = b.i[m.i_net + j] & 0xFFFF;
+            const double wy = sp < ns - 1 ? w[tix + 1 + sp] : 0.;
+            B += b.d[m.d_netc + j] * (wy - wTc * scr[L.eh + sp]);
+          }
+          const double g = sr * B * s.invRho;
+          out[2 * ro] += g;
+          out[2 * ro + 1] += -g * s.invT * m.invRu;
+        }
       }
       grp.sync();
     }
@@ -147,6 +149,52 @@ __global__ void __launch_bounds__(256) rate_param_adjoint_kernel(const AdjParams
 }
 
 }  // namespace
+
+void launch_rate_param_adjoint(const HostMech &hm, int configuration, double pressure, int n_items, int wsets,
+                               int stages, const double *q, const double *pressures, const double *w, double *out,
+                               cudaStream_t st)
+{
+  if (n_items == 0) return;
+  constexpr int G = 32;
+  const auto &progs = hm.programs_for(G);
+  AdjParams p{};
+  p.m = hm.dm;
+  p.blob = hm.d_blob;
+  p.status = hm.d_status;
+  p.L = hm.sl;
+  p.pg.w = progs.progs[0];
+  p.pg.full = progs.progs[1];
+  p.pg.j = progs.progs[2];
+  p.cfg.configuration = configuration;
+  p.cfg.heat = 0;
+  p.cfg.option = 0;
+  p.n_items = n_items;
+  p.stages = stages;
+  p.wsets = wsets;
+  p.neq = configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
+  p.pressure = pressure;
+  p.pressures = pressures;
+  p.q = q;
+  p.w = w;
+  p.out = out;
+  int dev, smem_max, nsm;
+  CUDA_THROW(cudaGetDevice(&dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const size_t per = (size_t)(hm.sl.total_rhs + p.neq + 2) * 8;
+  const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
+  const int groups = (int)std::min<size_t>(avail / per, 256 / G);
+  if (groups < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the parameter-adjoint kernel");
+  p.groups_per_cta = groups;
+  const size_t smem = hm.dm.blob_bytes + per * groups;
+  ensure_dynamic_smem((const void *)rate_param_adjoint_kernel<G>, smem);
+  const int bps = std::max(1, (int)((size_t)smem_max / smem));
+  const int grid = (int)std::max<long long>(
+      1, std::min<long long>(((long long)n_items + groups - 1) / groups, (long long)nsm * bps));
+  rate_param_adjoint_kernel<G><<<grid, groups * G, smem, st>>>(p);
+  CUDA_THROW(cudaGetLastError());
+}
+
 }  // namespace sfgb
 
 using namespace sfgb;
@@ -163,45 +211,8 @@ int sf_rate_param_adjoint_batch(const sf_mech *mech, const sf_reactor_params *rp
     if (rp->open || rp->heat_transfer != 0)
       throw sf_error(SF_ERR_UNSUPPORTED, "parameter adjoints cover closed adiabatic reactors");
     if (rp->configuration != 0 && rp->configuration != 1) throw sf_error(SF_ERR_INVALID_ARGUMENT, "bad configuration");
-    if (n_items == 0) return SF_OK;
-    HostMech &hm = const_cast<HostMech &>(mech->m);
-    constexpr int G = 32;
-    const auto &progs = hm.programs_for(G);
-    AdjParams p{};
-    p.m = hm.dm;
-    p.blob = hm.d_blob;
-    p.status = hm.d_status;
-    p.L = hm.sl;
-    p.pg.w = progs.progs[0];
-    p.pg.full = progs.progs[1];
-    p.pg.j = progs.progs[2];
-    p.cfg.configuration = rp->configuration;
-    p.cfg.heat = 0;
-    p.cfg.option = 0;
-    p.n_items = n_items;
-    p.stages = stages;
-    p.neq = rp->configuration == 1 ? hm.dm.ns + 1 : hm.dm.ns;
-    p.pressure = rp->pressure;
-    p.pressures = pressures;
-    p.q = q;
-    p.w = w;
-    p.out = out_grad;
-    int dev, smem_max, nsm;
-    CUDA_THROW(cudaGetDevice(&dev));
-    CUDA_THROW(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t per = (size_t)(hm.sl.total_rhs + p.neq + 2) * 8;
-    const size_t avail = (size_t)smem_max - hm.dm.blob_bytes - 64;
-    const int groups = (int)std::min<size_t>(avail / per, 256 / G);
-    if (groups < 1) throw sf_error(SF_ERR_UNSUPPORTED, "mechanism too large for the parameter-adjoint kernel");
-    p.groups_per_cta = groups;
-    const size_t smem = hm.dm.blob_bytes + per * groups;
-    ensure_dynamic_smem((const void *)rate_param_adjoint_kernel<G>, smem);
-    const int bps = std::max(1, (int)((size_t)smem_max / smem));
-    const int grid = (int)std::max<long long>(
-        1, std::min<long long>(((long long)n_items + groups - 1) / groups, (long long)nsm * bps));
-    rate_param_adjoint_kernel<G><<<grid, groups * G, smem, (cudaStream_t)stream>>>(p);
-    CUDA_THROW(cudaGetLastError());
+    launch_rate_param_adjoint(mech->m, rp->configuration, rp->pressure, n_items, 1, stages, q, pressures, w,
+                              out_grad, (cudaStream_t)stream);
     return SF_OK;
   } catch (sf_error &e) {
     set_error(e.what());

@@ -76,6 +76,11 @@ void ensure_dynamic_smem(const void *kernel, size_t bytes);
 // Thread-per-state chemistry kernels: warps that can be resident at once, and the bytes of interleaved scratch a
 // launch of n states takes (at most one slot per resident warp).
 size_t tps_resident_warps(const HostMech &hm);
+// Parameter adjoint of closed adiabatic reactors (sf_rate_param_adjoint_batch) with `wsets` adjoint vector sets per
+// state: w [n_items][wsets][stages][neq], out [n_items][wsets][2 nr] (accumulated). Throws sf_error.
+void launch_rate_param_adjoint(const HostMech &hm, int configuration, double pressure, int n_items, int wsets,
+                               int stages, const double *q, const double *pressures, const double *w, double *out,
+                               cudaStream_t st);
 size_t tps_scratch_bytes(const HostMech &hm, int mode, long long n);
 
 }  // namespace sfgb
