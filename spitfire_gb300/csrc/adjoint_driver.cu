@@ -7,7 +7,7 @@
 // reactor across the sweep, no compaction or scatter between steps. Per step m, over the na(m) reactors with more
 // than m steps:
 //   1. gather the recorded step (h, six stage states) of each reactor;
-//   2. right-hand sides and Jacobians at the 6 na stage states (the batched chemistry kernels);
+//   2. right-hand sides and Jacobians at the 6 na stage states (the 32-lane batched chemistry kernel);
 //   3. the factors of the transposed implicit stage systems h gamma J_s^T - I, s = 1..5 (one warp per system);
 //   4. the clamp mask of the step update (entries the forward step clamped at 0 carry no derivative);
 //   5. the stage recursion, backwards over the stages, one warp per reactor for all outputs:
@@ -40,8 +40,8 @@ struct AdjBufs {
   int *order, *steps;          // sorted: reactor of slot a, its step count
   double *ps, *T0s;            // sorted pressures and initial temperatures
   double *Y6, *K6, *J6, *pres6, *h;
-  double *LU;
-  int *piv;
+  double *LU, *dinv;  // factors of warp_lu_pd and the reciprocals of their pivots
+  int *perm;          // final row permutation of each factorization
   double *lam, *lamp, *W, *Ybar;
   double *grad;                // [n][O][2 nr], sorted slots
   double quad[8];              // 1 for a smoothed-delay output
@@ -80,15 +80,17 @@ __global__ void k_adj_gather(AdjBufs B, int m, int na)
   if (threadIdx.x == 0) B.h[a] = src[1];
 }
 
-// factors of h gamma J_s^T - I for s = 1..5, system a*5 + s-1, one warp each (the LU of the Newton algebra)
+// factors of h gamma J_s^T - I for s = 1..5, system a*5 + s-1, one warp each: the row permutation and the
+// reciprocals of the pivots are kept, so that the stage solves multiply instead of dividing on their serial sweeps
 __global__ void k_adj_lu(AdjBufs B, int na)
 {
   extern __shared__ __align__(16) unsigned char sm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m = B.neq;
   const size_t mm = (size_t)m * m;
-  double *A = reinterpret_cast<double *>(sm) + (size_t)w * mm;
-  int *pv = reinterpret_cast<int *>(reinterpret_cast<double *>(sm) + (size_t)kWarps * mm) + w * m;
+  double *A = reinterpret_cast<double *>(sm) + (size_t)w * (mm + m);
+  double *di = A + mm;
+  int *pv = reinterpret_cast<int *>(reinterpret_cast<double *>(sm) + (size_t)kWarps * (mm + m)) + w * m;
   for (int sys = blockIdx.x * kWarps + w; sys < na * 5; sys += gridDim.x * kWarps) {
     const int a = sys / 5, s = sys - a * 5 + 1;
     const double g = B.h[a] * kGamma;
@@ -99,10 +101,14 @@ __global__ void k_adj_lu(AdjBufs B, int na)
       A[(size_t)r * m + c] = g * J[f] - (r == c ? 1. : 0.);
     }
     __syncwarp();
-    warp_lu(A, m, pv);
+    warp_lu_pd(A, m, pv, di);
+    __syncwarp();
     double *LU = B.LU + (size_t)sys * mm;
     for (size_t e = lane; e < mm; e += 32) LU[e] = A[e];
-    for (int k = lane; k < m; k += 32) B.piv[(size_t)sys * m + k] = pv[k];
+    for (int k = lane; k < m; k += 32) {
+      B.perm[(size_t)sys * m + k] = pv[k];
+      B.dinv[(size_t)sys * m + k] = di[k];
+    }
     __syncwarp();
   }
 }
@@ -132,16 +138,19 @@ __global__ void k_adj_stages(AdjBufs B, int na)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m = B.neq, O = B.O, tix = B.tix;
   const size_t mm = (size_t)m * m;
-  double *LU = reinterpret_cast<double *>(sm) + (size_t)w * (mm + m);
-  double *x = LU + mm;
-  int *pv = reinterpret_cast<int *>(reinterpret_cast<double *>(sm) + (size_t)kWarps * (mm + m)) + w * m;
+  double *LU = reinterpret_cast<double *>(sm) + (size_t)w * (mm + 3 * m);
+  double *x = LU + mm, *cv = x + m, *di = cv + m;
+  int *pv = reinterpret_cast<int *>(reinterpret_cast<double *>(sm) + (size_t)kWarps * (mm + 3 * m)) + w * m;
   for (int a = blockIdx.x * kWarps + w; a < na; a += gridDim.x * kWarps) {
     const double h = B.h[a];
     for (int s = 5; s >= 0; --s) {
       if (s >= 1) {
         const size_t sys = (size_t)a * 5 + s - 1;
         for (size_t e = lane; e < mm; e += 32) LU[e] = B.LU[sys * mm + e];
-        for (int k = lane; k < m; k += 32) pv[k] = B.piv[sys * m + k];
+        for (int k = lane; k < m; k += 32) {
+          pv[k] = B.perm[sys * m + k];
+          di[k] = B.dinv[sys * m + k];
+        }
       }
       const double Ts = B.Y6[((size_t)a * 6 + s) * m + tix];
       const double sg = 1. / (1. + exp(-((Ts - B.T0s[a] - kDtIgn) / kWidth)));
@@ -156,10 +165,15 @@ __global__ void k_adj_stages(AdjBufs B, int na)
           for (int l = s + 1; l < 6; ++l)
             if (c_a[l][s] != 0.) c = c + (h * c_a[l][s]) * B.Ybar[(base * 6 + l) * m + j];
           if (s >= 1) c = c + (h * kGamma) * (j == tix ? qdT : 0.);
-          x[j] = s >= 1 ? -c : c;
+          cv[j] = s >= 1 ? -c : c;
         }
         __syncwarp();
-        if (s >= 1) warp_lu_solve(LU, m, pv, x);  // (h gamma J_s^T - I) w = -c
+        if (s >= 1) {  // (h gamma J_s^T - I) w = -c, the right-hand side loaded in pivot order
+          for (int i = lane; i < m; i += 32) x[i] = cv[pv[i]];
+          warp_lu_solve_pd(LU, m, di, x);
+        } else {
+          for (int i = lane; i < m; i += 32) x[i] = cv[i];
+        }
         __syncwarp();
         for (int j = lane; j < m; j += 32) B.W[(base * 6 + s) * m + j] = x[j];
         // Ybar_s = J_s^T w + qd_s: lane i walks column i of J (contiguous)
@@ -204,8 +218,8 @@ struct AdjLayout {
   size_t bytes;
 };
 
-// 0 order, 1 steps, 2 ps, 3 T0s, 4 Y6, 5 K6, 6 J6, 7 pres6, 8 h, 9 LU, 10 piv, 11 lam, 12 lamp, 13 W, 14 Ybar,
-// 15 grad, 16 output kinds, 17 the chemistry call's workspace
+// 0 order, 1 steps, 2 ps, 3 T0s, 4 Y6, 5 K6, 6 J6, 7 pres6, 8 h, 9 LU, 10 perm, 11 lam, 12 lamp, 13 W, 14 Ybar,
+// 15 grad, 16 output kinds, 17 dinv
 AdjLayout adj_layout(const sf_mech *mech, int configuration, int n, int O)
 {
   const HostMech &hm = mech->m;
@@ -214,8 +228,7 @@ AdjLayout adj_layout(const sf_mech *mech, int configuration, int n, int O)
   const size_t N = n;
   const size_t sizes[18] = {N * 4, N * 4, N * 8, N * 8, 6 * N * neq * 8, 6 * N * neq * 8, 6 * N * neq * neq * 8,
                             6 * N * 8, N * 8, 5 * N * neq * neq * 8, 5 * N * neq * 4, N * O * neq * 8,
-                            N * O * neq * 8, N * O * 6 * neq * 8, N * O * 6 * neq * 8, N * O * 2 * nr * 8, 64,
-                            sf_chem_workspace_size(mech, SF_CHEM_JAC, 6 * n)};
+                            N * O * neq * 8, N * O * 6 * neq * 8, N * O * 6 * neq * 8, N * O * 2 * nr * 8, 64, 5 * N * neq * 8};
   AdjLayout L{};
   size_t o = 0;
   for (int k = 0; k < 18; ++k) {
@@ -290,15 +303,14 @@ int sf_adjoint_batch(const sf_mech *mech, const sf_reactor_params *params, int n
     B.pres6 = reinterpret_cast<double *>(at(7));
     B.h = reinterpret_cast<double *>(at(8));
     B.LU = reinterpret_cast<double *>(at(9));
-    B.piv = reinterpret_cast<int *>(at(10));
+    B.perm = reinterpret_cast<int *>(at(10));
+    B.dinv = reinterpret_cast<double *>(at(17));
     B.lam = reinterpret_cast<double *>(at(11));
     B.lamp = reinterpret_cast<double *>(at(12));
     B.W = reinterpret_cast<double *>(at(13));
     B.Ybar = reinterpret_cast<double *>(at(14));
     B.grad = reinterpret_cast<double *>(at(15));
     int *kinds_dev = reinterpret_cast<int *>(at(16));
-    void *chem_ws = at(17);
-    const size_t chem_ws_bytes = workspace_bytes - L.off[17];
     for (int o = 0; o < n_outputs; ++o) B.quad[o] = output_kinds[o] == SF_ADJ_TAU_S ? 1. : 0.;
 
     // step counts: the one read back of the sweep
@@ -324,8 +336,8 @@ int sf_adjoint_batch(const sf_mech *mech, const sf_reactor_params *params, int n
     CUDA_THROW(cudaGetDevice(&dev));
     CUDA_THROW(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t mm = (size_t)B.neq * B.neq;
-    const size_t smem_lu = kWarps * (mm * 8 + B.neq * 4);
-    const size_t smem_st = kWarps * ((mm + B.neq) * 8 + B.neq * 4);
+    const size_t smem_lu = kWarps * ((mm + B.neq) * 8 + B.neq * 4);
+    const size_t smem_st = kWarps * ((mm + 3 * B.neq) * 8 + B.neq * 4);
     ensure_dynamic_smem((const void *)k_adj_lu, smem_lu);
     ensure_dynamic_smem((const void *)k_adj_stages, smem_st);
     const int nmax = sorted_steps[0];
@@ -334,9 +346,9 @@ int sf_adjoint_batch(const sf_mech *mech, const sf_reactor_params *params, int n
       while (na > 0 && sorted_steps[na - 1] <= m) --na;
       k_adj_gather<<<na, 128, 0, st>>>(B, m, na);
       CUDA_THROW(cudaGetLastError());
-      const int rc = sf_reactor_jac_batch(mech, params, 0, 6 * na, B.Y6, params->configuration == 0 ? B.pres6 : nullptr,
-                                          B.K6, B.J6, chem_ws, chem_ws_bytes, stream);
-      if (rc != SF_OK) throw sf_error(rc, sf_last_error());
+      // 32 lanes per state: a few thousand stage states are too few for the thread-per-state kernels
+      reactor_jac_lanes(mech, params, 0, 6 * na, B.Y6, params->configuration == 0 ? B.pres6 : nullptr, B.K6, B.J6,
+                        32, st);
       const long long lu_need = ((long long)na * 5 + kWarps - 1) / kWarps;
       k_adj_lu<<<(int)std::min<long long>(lu_need, (long long)nsm * 8), 32 * kWarps, smem_lu, st>>>(B, na);
       CUDA_THROW(cudaGetLastError());

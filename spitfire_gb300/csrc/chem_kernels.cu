@@ -637,3 +637,23 @@ int sf_device_status(const sf_mech *mech, int clear)
 }
 
 }  // extern "C"
+
+// Reactor right-hand sides and Jacobians with an explicit lane width G (8, 16 or 32 lanes per state: shared-memory
+// scratch, no workspace), for callers whose batch is too small for the thread-per-state shape the autotuner may have
+// chosen for large batches.
+void sfgb::reactor_jac_lanes(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n,
+                             const double *q, const double *pressures, double *out_rhs, double *out_jac, int G,
+                             cudaStream_t st)
+{
+  if (G != 8 && G != 16 && G != 32) throw sf_error(SF_ERR_INVALID_ARGUMENT, "lane width must be 8, 16 or 32");
+  KParams p{};
+  fill_reactor(p, rp);
+  p.n = n;
+  p.q = q;
+  p.pressures = pressures;
+  p.option = rates_option;
+  p.out_rhs = out_rhs;
+  p.out_J = out_jac;
+  const int rc = chem_launch(mech->m, MODE_JAC, p, st, G, nullptr, 0);
+  if (rc != SF_OK) throw sf_error(rc, "reactor Jacobian launch failed");
+}

@@ -76,6 +76,9 @@ void ensure_dynamic_smem(const void *kernel, size_t bytes);
 // Thread-per-state chemistry kernels: warps that can be resident at once, and the bytes of interleaved scratch a
 // launch of n states takes (at most one slot per resident warp).
 size_t tps_resident_warps(const HostMech &hm);
+// sf_reactor_jac_batch with an explicit lane width G (8, 16 or 32; no workspace). Throws sf_error.
+void reactor_jac_lanes(const sf_mech *mech, const sf_reactor_params *rp, int rates_option, int n, const double *q,
+                       const double *pressures, double *out_rhs, double *out_jac, int G, cudaStream_t st);
 // Parameter adjoint of closed adiabatic reactors (sf_rate_param_adjoint_batch) with `wsets` adjoint vector sets per
 // state: w [n_items][wsets][stages][neq], out [n_items][wsets][2 nr] (accumulated). Throws sf_error.
 void launch_rate_param_adjoint(const HostMech &hm, int configuration, double pressure, int n_items, int wsets,
