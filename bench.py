@@ -807,6 +807,8 @@ def store_probe(t, pattern):
 #   flamelet   8 steady-flamelet profiles of 64-120 points: one RHS sweep, Jacobian with eigenvalue bounds,
 #              block-Thomas factorization, solve and matvec
 #   adjoint    64 reactors of the adjoint distribution recorded to 1 ms, then the batched adjoint
+#   adjoint_sweep  the benchmark's adjoint workload (2048 reactors to 5 ms, the thread-per-state Jacobian shape the
+#              headline tunes): forward record, then one backward sweep (sf_adjoint_batch), its time printed
 #   fp64issue  warp-level FP64 FMA instructions per second with 1, 2, 4, 8, 16 and 32 active lanes per warp
 #   dmma       FP64 mma.sync (m8n8k4, m16n8k16) throughput beside the DFMA pipe's
 #   sysmem     kernel stores into device memory and into pinned host memory (coalesced, and the thread-per-state
@@ -923,6 +925,26 @@ def case_adjoint():
     return spec
 
 
+def case_adjoint_sweep():
+    import torch
+    from spitfire_gb300 import autotune as AT
+    from spitfire_gb300 import workloads as W
+    from spitfire_gb300.adjoint import ReactorAdjoint
+    spec = _spec()
+    AT.set_tuning(spec, 'group_jac', 1)
+    AT.set_tuning(spec, 'tps_ctas', 2)
+    d = W.adjoint_batch(spec, N_ADJOINT, seed=1005)
+    adj = ReactorAdjoint(spec, 'isobaric')
+    tr = adj.forward(d['q0'], d['p'], 5.e-3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = adj.backward(tr)
+    torch.cuda.synchronize()
+    print(f'backward sweep of {N_ADJOINT} reactors: {time.perf_counter() - t0:.3f} s')
+    assert bool(torch.isfinite(g['theta']).all().item())
+    return spec
+
+
 def case_fp64issue():
     for lanes in (1, 2, 4, 8, 16, 32):
         tf, wi = fp64_fma_probe(4000, lanes)
@@ -960,7 +982,7 @@ def case_sysmem():
 
 PROFILE_CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs,
                  'integrate_2048': case_integrate_2048, 'integrate': case_integrate, 'flamelet': case_flamelet,
-                 'adjoint': case_adjoint, 'fp64issue': case_fp64issue, 'dmma': case_dmma, 'sysmem': case_sysmem}
+                 'adjoint': case_adjoint, 'adjoint_sweep': case_adjoint_sweep, 'fp64issue': case_fp64issue, 'dmma': case_dmma, 'sysmem': case_sysmem}
 
 
 def run_profile_case(name):
