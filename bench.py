@@ -812,7 +812,8 @@ def store_probe(t, pattern):
 #   fp64issue  warp-level FP64 FMA instructions per second with 1, 2, 4, 8, 16 and 32 active lanes per warp
 #   dmma       FP64 mma.sync (m8n8k4, m16n8k16) throughput beside the DFMA pipe's
 #   sysmem     kernel stores into device memory and into pinned host memory (coalesced, and the thread-per-state
-#              Jacobian pattern), beside cudaMemcpy device-to-host of the same 1.5 GB
+#              Jacobian pattern), beside cudaMemcpy device-to-host of the same 1.5 GB, on one stream and split over
+#              2 and 4 streams at once
 def _spec():
     from spitfire_gb300.mechanism import ChemicalMechanismSpec
     return ChemicalMechanismSpec.bundled('methane-gri30')
@@ -977,6 +978,25 @@ def case_sysmem():
     e1.record()
     e1.synchronize()
     print(f'cudaMemcpy device-to-host (pinned): {n * 8 / (e0.elapsed_time(e1) * 1e-3) / 1e9:.1f} GB/s')
+    # the same bytes split over k streams at once: whether more copy engines raise the link's rate
+    for k in (2, 4):
+        streams = [torch.cuda.Stream() for _ in range(k)]
+        part = n // k
+        for rep in range(2):
+            torch.cuda.synchronize()
+            e0.record()
+            for i, s in enumerate(streams):
+                s.wait_event(e0)
+                with torch.cuda.stream(s):
+                    host[i * part:(i + 1) * part].copy_(dev[i * part:(i + 1) * part], non_blocking=True)
+            for s in streams:
+                torch.cuda.current_stream().wait_stream(s)
+            e1.record()
+            e1.synchronize()
+        print(f'device-to-host over {k} streams at once: {part * k * 8 / (e0.elapsed_time(e1) * 1e-3) / 1e9:.1f} GB/s')
+    import glob
+    nodes = sorted(glob.glob('/sys/devices/system/node/node[0-9]*'))
+    print(f'host: {len(os.sched_getaffinity(0))} cores in this process\'s affinity, {len(nodes)} NUMA nodes')
     return None
 
 
@@ -1132,15 +1152,16 @@ def main():
     for _ in range(2):
         e2e_step()
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for k in range(args.steps):
         e2e_step()
-    e1.record(stream)
-    e1.synchronize()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+        ev[k + 1].record(stream)
+    ev[-1].synchronize()
+    e2e_steps = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    e2e_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]) / args.steps, dev)
     e2e = {'value': world * N_STATES / (e2e_ms * 1e-3), 'unit': 'states/s', 'ms_per_step': e2e_ms,
+           'ms_per_step_min_median_max': [min(e2e_steps), statistics.median(e2e_steps), max(e2e_steps)],
            'h2d_bytes_per_step': qpin.numel() * 8, 'd2h_bytes_per_step': (rhs_h.numel() + J_h.numel()) * 8,
            'api': 'PyCombustionKernels.reactor_jac_host_batch -> sf_reactor_jac_host_batch (pinned host buffers; '
                   'chunks of one resident wave, device-to-host copies overlapping the next chunk)'}
