@@ -45,6 +45,27 @@ def test_argument_errors_are_reported_without_a_device():
     assert L.sf_btddod_solve_batch(0, 0, None, None, None, None, None, None, None, None, None, None) == 1
 
 
+def test_c_caller_compiles_links_and_gets_status_codes(tmp_path):
+    """tests/c_abi/abi_smoke.c, plain C99 against include/spitfire_gb300.h, linked to the library by name: the
+    header is valid C and a C caller gets the status codes and messages without a GPU."""
+    import shutil
+    import subprocess
+    from spitfire_gb300 import _native as N
+    from spitfire_gb300 import build
+    build.build()
+    gcc = shutil.which('gcc')
+    if gcc is None:
+        pytest.skip('no C compiler')
+    exe = str(tmp_path / 'abi_smoke')
+    libdir = os.path.dirname(N.LIB_PATH)
+    subprocess.run([gcc, '-std=c99', '-Wall', '-Werror', '-I', os.path.join(ROOT, 'include'),
+                    os.path.join(ROOT, 'tests', 'c_abi', 'abi_smoke.c'), '-L', libdir, '-lspitfire_gb300',
+                    '-Wl,-rpath,' + libdir, '-o', exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith('OK'), r.stdout
+
+
 def test_shard_ranges_cover_contiguously():
     from spitfire_gb300.sharding import shard_range
     for n in (0, 1, 7, 8192, 65537):
