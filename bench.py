@@ -51,6 +51,7 @@ N_STATES = 65536
 N_REACTORS = 8192
 N_FLAMELETS = 64
 N_ADJOINT = 2048
+TUNE_REACTORS = 4096
 # Per GRI state of each Jacobian kernel the autotuner can choose, from ncu on the profiling cases
 # (python bench.py --profile-case jac | jac_tps): executed FP64 flops (thread-level DADD + DMUL + 2*DFMA),
 # warp-level FP64 instructions (smsp__inst_executed_pipe_fp64.sum / states) and DRAM bytes
@@ -298,7 +299,7 @@ def bench_newton(q, rhs, J, gamma_h, stream):
 
 
 # integrator memory placement knob: Griffon scratch and iteration matrix in shared memory or L2-resident global slots
-PLACEMENT = {0: 'shared', 1: 'global scratch', 2: 'global scratch + matrix'}
+PLACEMENT = {3: 'shared', 1: 'global scratch', 2: 'global scratch + matrix'}
 
 
 def bench_ignition(spec, rank, stream, cpu):
@@ -310,8 +311,9 @@ def bench_ignition(spec, rank, stream, cpu):
     from spitfire_gb300 import autotune as AT
     bi = BatchIntegrator(spec, 'isobaric')
     kw = dict(delta_temperature_ignition=400., stop_at_time=0.1)
-    # launch shape from the autotuner, on a 1024-reactor sample of the batch (not timed)
-    best, cand = AT.tune_integrator(bi, d['q0'][:1024], pressures=d['p'][:1024], **kw)
+    # launch shape from the autotuner, on a 4096-reactor sample of the batch (not timed): the sample must fill the
+    # largest candidate's resident warps (16 per SM at 8 warps per block), or it favours the smaller shapes
+    best, cand = AT.tune_integrator(bi, d['q0'][:TUNE_REACTORS], pressures=d['p'][:TUNE_REACTORS], **kw)
     out = bi.run(d['q0'], pressures=d['p'], graph=True, **kw)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -333,7 +335,8 @@ def bench_ignition(spec, rank, stream, cpu):
            'device_status': spec.griffon.device_status(),
            'tau_interpolated': _tau_interp_summary(tau, tau_i, status),
            'autotune': {'chosen': {'placement': PLACEMENT[best[0]], 'warps_per_block': best[1]},
-                        'candidates_ms_1024_reactors': {f'{PLACEMENT[k[0]]}/{k[1]}w': v for k, v in cand.items()}}}
+                        f'candidates_ms_{TUNE_REACTORS}_reactors': {f'{PLACEMENT[k[0]]}/{k[1]}w': v
+                                                                     for k, v in cand.items()}}}
     # comparison point: the plain single-state GPU form (one thread per reactor, same step logic) on the same batch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)

@@ -124,9 +124,9 @@ int sf_mech_info(const sf_mech *mech, int *n_species, int *n_reactions, int *cou
  *     thread-per-state kernels (each lane one state, scratch interleaved across the warp in the caller's
  *     workspace, whose size sf_chem_workspace_size reports; no knob allocates anything);
  *   SF_TUNE_INTEGRATE_WARPS: warps (reactors) per block of sf_integrate_batch, 1..8 (0: as many as fit);
- *   SF_TUNE_INTEGRATE_SCRATCH: 1 keeps each integrating warp's Griffon scratch in global memory (L2-resident)
- *     instead of shared memory, so that more warps fit per SM; 2 also its iteration matrix and FP32 factors
- *     (0: shared memory);
+ *   SF_TUNE_INTEGRATE_SCRATCH: where each integrating warp keeps its data: 3 all in shared memory; 1 its Griffon
+ *     scratch in global memory (L2-resident), so that more warps fit per SM; 2 also its iteration matrix and FP32
+ *     factors (0: the built-in choice, 2);
  *   SF_TUNE_TPS_CTAS: resident 4-warp blocks per SM of the thread-per-state kernels, 1..16 (0: as many as fit);
  *     fewer keep more of their interleaved scratch in L2.
  * The integrator knobs do not change results; the lane-group width changes the order of per-species sums, so those

@@ -132,15 +132,16 @@ def tune_chemistry(mech, states, pressures=None, configuration='isochoric', kind
 
 
 def tune_integrator(integrator, q0, pressures=None, reps=1, **controls):
-    """Choose the integrator's memory placement and warps per block on a sample batch (q0 rows): scratch 0 (all in
+    """Choose the integrator's memory placement and warps per block on a sample batch (q0 rows): scratch 3 (all in
     shared memory), 1 (Griffon scratch in an L2-resident global slot per warp) or 2 (the iteration matrix there
-    too). Returns (best (scratch, warps), {(scratch, warps): ms})."""
+    too). The sample should fill the largest candidate's resident warps (16 per SM at 8 warps per block), or the
+    smaller shapes win on it. Returns (best (scratch, warps), {(scratch, warps): ms})."""
     torch = _torch()
     mech = integrator.mech
     times = {}
     ref = None
     saved = (get_tuning(mech, 'integrate_scratch'), get_tuning(mech, 'integrate_warps'))
-    for scratch in (0, 1, 2):
+    for scratch in (3, 1, 2):  # all in shared memory, Griffon scratch global, matrix global too
         set_tuning(mech, 'integrate_scratch', scratch)
         set_tuning(mech, 'integrate_warps', 0)
         fit = _fitting_warps(integrator)
@@ -170,7 +171,8 @@ def _fitting_warps(integrator):
     # per-warp doubles as the integrator lays them out (integrate_kernels.cu per_warp_doubles)
     lay = h.scratch_layout()
     neq = integrator.mech.n_species + (1 if integrator.configuration == 'isochoric' else 0)
-    place = get_tuning(integrator.mech, 'integrate_scratch')
+    v = get_tuning(integrator.mech, 'integrate_scratch')
+    place = 2 if v == 0 else (0 if v == 3 else v)  # knob value -> placement (0: the built-in choice, 2)
     gs, gm = place >= 1, place == 2
     n2 = neq * neq
     per = (0 if gm else n2) + 12 * neq + (0 if gs else lay['total']) + \

@@ -360,6 +360,7 @@ int sf_mech_set_tuning(sf_mech *mech, int knob, int value)
   const bool ok = (knob <= SF_TUNE_GROUP_JAC) ? (value == 0 || value == 1 || value == 8 || value == 16 || value == 32)
                   : (knob == SF_TUNE_INTEGRATE_WARPS) ? (value >= 0 && value <= 8)
                   : (knob == SF_TUNE_TPS_CTAS) ? (value >= 0 && value <= 16)
+                  : (knob == SF_TUNE_INTEGRATE_SCRATCH) ? (value >= 0 && value <= 3)
                   : (value >= 0 && value <= 2);
   if (!ok) {
     t_err = "sf_mech_set_tuning: value out of range for this knob";
