@@ -598,7 +598,7 @@ int sf_integrate_record_batch(const sf_mech *mech, const sf_reactor_params *rp, 
                               int *out_counts, int *out_status, void *workspace, size_t workspace_bytes,
                               double *trajectory, int capacity_steps, void *stream)
 {
-  if (!trajectory || capacity_steps < 1) {
+  if (n > 0 && (!trajectory || capacity_steps < 1)) {
     set_error("sf_integrate_record_batch: trajectory buffer and a positive capacity are required");
     return SF_ERR_INVALID_ARGUMENT;
   }
