@@ -1152,8 +1152,9 @@ def main():
         # chunk overlapping the next chunk's kernel
         g.reactor_jac_host_batch(P, qpin, rhs_h, J_h)
 
-    for _ in range(2):
+    for _ in range(max(args.warmup, 3)):
         e2e_step()
+    torch.cuda.synchronize()
     barrier()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     ev[0].record(stream)
@@ -1165,6 +1166,7 @@ def main():
     e2e_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]) / args.steps, dev)
     e2e = {'value': world * N_STATES / (e2e_ms * 1e-3), 'unit': 'states/s', 'ms_per_step': e2e_ms,
            'ms_per_step_min_median_max': [min(e2e_steps), statistics.median(e2e_steps), max(e2e_steps)],
+           'ms_each_step': [round(x, 3) for x in e2e_steps],
            'h2d_bytes_per_step': qpin.numel() * 8, 'd2h_bytes_per_step': (rhs_h.numel() + J_h.numel()) * 8,
            'api': 'PyCombustionKernels.reactor_jac_host_batch -> sf_reactor_jac_host_batch (pinned host buffers; '
                   'chunks of one resident wave, device-to-host copies overlapping the next chunk)'}
