@@ -547,6 +547,29 @@ int sf_flamelet_steady_psitc_batch(const sf_mech *mech, const sf_flamelet_batch 
                                    int *out_converged, int *out_iterations, double *out_min_ds, void *workspace,
                                    size_t workspace_bytes, void *stream);
 
+/* One ESDIRK64 step attempt (time/methods.py:441-612 with SimpleNewtonSolver, time/nonlinear.py:185-268) of every
+ * running flamelet of a batch, each with its own step size: the transient flamelet integration of Flamelet.integrate
+ * (flamelet.py:1046-1213) without its step-size control, which the caller keeps (one call per attempt):
+ *   - where setup[f] (any_setup != 0 when any is set): the iteration matrix gamma dt_f J - I and its block-Thomas
+ *     factors, kept in the workspace for the following attempts (pass the same workspace to every attempt);
+ *   - k_0 = F(state); for s = 1..5 the implicit stage Y_s = state + dt (gamma F(Y_s) + sum_{j<s} a_sj k_j) by the
+ *     simplified Newton iteration with those factors, at most max_nonlinear_iter iterations, converged when the
+ *     weighted infinity norm of its residual (temperature rows divided by 1e3) is below nonlinear_tolerance;
+ *   - the step dt sum_s b_s k_s and the error estimate dt sum_s (b_s - bhat_s) k_s.
+ * A running flamelet whose step is finite gets state <- max(state + step, 0). Per flamelet (DEVICE [n_flamelets]):
+ * out_err the weighted norm of the error estimate, out_step_norm that of the step, out_nonfinite 1.0 if the step has
+ * a non-finite entry, out_nl_ok 0 if a stage's Newton iteration did not converge; inout_newton += iterations.
+ * state DEVICE [points][ns] in/out; dt DEVICE [n_flamelets]; run, setup DEVICE int [n_flamelets]. The arithmetic
+ * is evaluated with one rounding per operation in the order of the reference's vector expressions. The call reads
+ * back one flag per Newton iteration (whether any flamelet still iterates). workspace: DEVICE,
+ * sf_flamelet_esdirk_workspace_size bytes. */
+size_t sf_flamelet_esdirk_workspace_size(const sf_mech *mech, const sf_flamelet_batch *fb);
+int sf_flamelet_esdirk_attempt_batch(const sf_mech *mech, const sf_flamelet_batch *fb, double *state,
+                                     const double *dt, const int *run, const int *setup, int any_setup,
+                                     double nonlinear_tolerance, int max_nonlinear_iter, int rates_option,
+                                     double *out_err, double *out_step_norm, double *out_nonfinite, int *out_nl_ok,
+                                     int *inout_newton, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

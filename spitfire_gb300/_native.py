@@ -83,6 +83,11 @@ def _declare(L):
     L.sf_adjoint_workspace_size.restype = C.c_size_t
     L.sf_adjoint_batch.argtypes = [_vp, C.POINTER(SfReactorParams), _ip, _vp, _ip, _vp, _vp, _vp, _ip, _vp, _vp, _vp,
                                    _vp, C.c_size_t, _vp]
+    L.sf_flamelet_esdirk_workspace_size.argtypes = [_vp, C.POINTER(SfFlameletBatch)]
+    L.sf_flamelet_esdirk_workspace_size.restype = C.c_size_t
+    L.sf_flamelet_esdirk_attempt_batch.argtypes = [_vp, C.POINTER(SfFlameletBatch), _vp, _vp, _vp, _vp, _ip,
+                                                   C.c_double, _ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp, C.c_size_t,
+                                                   _vp]
     L.sf_flamelet_steady_workspace_size.argtypes = [_vp, C.POINTER(SfFlameletBatch)]
     L.sf_flamelet_steady_workspace_size.restype = C.c_size_t
     _d = C.c_double
@@ -110,7 +115,7 @@ EXPORTED = ['sf_last_error', 'sf_version', 'sf_mech_create', 'sf_mech_destroy', 
             'sf_btddod_scale_and_add_block_diagonal_batch', 'sf_chem_workspace_size',
             'sf_flamelet_jac_workspace_size', 'sf_flamelet_steady_workspace_size',
             'sf_flamelet_steady_newton_batch', 'sf_flamelet_steady_psitc_batch', 'sf_adjoint_workspace_size',
-            'sf_adjoint_batch']
+            'sf_adjoint_batch', 'sf_flamelet_esdirk_workspace_size', 'sf_flamelet_esdirk_attempt_batch']
 
 
 def load(path=None):

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <vector>
 
+#include "esdirk64.cuh"
 #include "sf_internal.h"
 
 namespace sfgb {
@@ -443,6 +444,135 @@ struct Solver {
   }
 };
 
+// ------------------------------------------------------------------------- transient step attempt (ESDIRK64)
+// Elementwise arithmetic below is written with explicit roundings (no fused multiply-adds), in the order the
+// batch's host-loop integrator evaluates it with separate tensor operations, so both give the same bits.
+struct AttBufs {
+  long long N;
+  int ns, nf;
+  const int *map;
+  double *k;  // 6 stage derivatives, N each
+  double *Y, *fs, *resid, *prior, *dx, *dstate, *eterm;
+  const double *dt;  // [nf]
+  double *state;
+};
+
+__global__ void k_att_stage_start(AttBufs a, int st)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x) {
+    const double dtd = a.dt[a.map[i / a.ns]];
+    double pr = __dmul_rn(c_a[st][0], a.k[i]);
+    for (int j = 1; j < st; ++j) pr = __dadd_rn(pr, __dmul_rn(c_a[st][j], a.k[(long long)j * a.N + i]));
+    a.prior[i] = pr;
+    const double f = a.k[(long long)(st - 1) * a.N + i];
+    a.fs[i] = f;
+    a.resid[i] = __dsub_rn(__dmul_rn(dtd, __dadd_rn(__dmul_rn(kGamma, f), pr)), __dsub_rn(a.Y[i], a.state[i]));
+  }
+}
+
+// Y <- Y - dx where go
+__global__ void k_att_newton_update(AttBufs a, const int *go)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x)
+    if (go[a.map[i / a.ns]]) a.Y[i] = __dsub_rn(a.Y[i], a.dx[i]);
+}
+
+// residual at the new iterate where go
+__global__ void k_att_newton_resid(AttBufs a, const int *go)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x) {
+    const int f = a.map[i / a.ns];
+    if (go[f])
+      a.resid[i] = __dsub_rn(__dmul_rn(a.dt[f], __dadd_rn(__dmul_rn(kGamma, a.fs[i]), a.prior[i])),
+                             __dsub_rn(a.Y[i], a.state[i]));
+  }
+}
+
+// the step dt * sum_s b_s k_s and the error term dt * sum_s (b_s - bhat_s) k_s
+__global__ void k_att_step(AttBufs a)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x) {
+    const double dtd = a.dt[a.map[i / a.ns]];
+    double ds = __dmul_rn(c_b[0], a.k[i]);
+    double de = __dmul_rn(__dsub_rn(c_b[0], c_bh[0]), a.k[i]);
+    for (int j = 1; j < 6; ++j) {
+      const double kj = a.k[(long long)j * a.N + i];
+      ds = __dadd_rn(ds, __dmul_rn(c_b[j], kj));
+      de = __dadd_rn(de, __dmul_rn(__dsub_rn(c_b[j], c_bh[j]), kj));
+    }
+    a.dstate[i] = __dmul_rn(dtd, ds);
+    a.eterm[i] = __dmul_rn(dtd, de);
+  }
+}
+
+// state <- max(state + step, 0) where the flamelet runs and its step is finite (fin[f] == 0: no non-finite entry)
+__global__ void k_att_accept(AttBufs a, const int *run, const double *nonfinite)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x) {
+    const int f = a.map[i / a.ns];
+    if (run[f] && nonfinite[f] == 0.) {
+      const double v = __dadd_rn(a.state[i], a.dstate[i]);
+      a.state[i] = v < 0. ? 0. : v;
+    }
+  }
+}
+
+// per-flamelet bookkeeping of the attempt: 0 start (go = run, conv = 0, nl_ok = 1 on the first stage),
+// 1 newton += go, 2 convergence test (nrm < tol) and the any-go flag, 3 end of stage (nl_ok &= conv | !run),
+// 4 prefactors gamma * dt
+struct AttCtl {
+  const int *run;
+  int *go, *conv, *nl_ok, *newton, *flags;
+  double *nrm, *pref;
+  const double *dt;
+};
+
+__global__ void k_att_ctl(AttCtl c, int nf, int op, double tol)
+{
+  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+    switch (op) {
+    case 0: c.go[f] = c.run[f] != 0; c.conv[f] = 0; break;
+    case 1: c.newton[f] += c.go[f]; break;
+    case 2:
+      if (c.go[f] && c.nrm[f] < tol) {
+        c.conv[f] = 1;
+        c.go[f] = 0;
+      }
+      if (c.go[f]) atomicOr(&c.flags[0], 1);
+      break;
+    case 3: c.nl_ok[f] = c.nl_ok[f] && (c.conv[f] || !c.run[f]); break;
+    case 4: c.pref[f] = __dmul_rn(c.dt[f], kGamma); c.nl_ok[f] = 1; break;
+    }
+  }
+}
+
+// Workspace of an attempt: 0 values, 1 lvalues, 2 pivots (the iteration matrix factors, kept from one attempt to
+// the next), 3 stage derivatives (6 N), 4 Y, 5 fs, 6 resid, 7 prior, 8 dx, 9 dstate, 10 eterm, 11 map,
+// 12 ints (go, conv, flags), 13 doubles (nrm, pref, nonfinite)
+Layout att_layout(const sf_mech *mech, const sf_flamelet_batch *fb)
+{
+  Layout L{};
+  const int ns = mech->m.dm.ns;
+  L.nf = fb->n_flamelets;
+  L.P = fb->offsets_z_host[L.nf];
+  L.N = L.P * ns;
+  L.V = 0;
+  for (int f = 0; f < L.nf; ++f) {
+    const long long nb = fb->offsets_z_host[f + 1] - fb->offsets_z_host[f];
+    L.V += (long long)ns * (nb * ns + 2 * (nb - 1));
+  }
+  const size_t N8 = (size_t)L.N * 8;
+  const size_t sizes[14] = {(size_t)L.V * 8, (size_t)L.P * ns * ns * 8, (size_t)L.P * ns * 4, 6 * N8, N8, N8, N8,
+                            N8, N8, N8, N8, (size_t)L.P * 4, (size_t)(2 * L.nf + 16) * 4, (size_t)3 * L.nf * 8};
+  size_t o = 0;
+  for (int k = 0; k < 14; ++k) {
+    L.off[k] = o;
+    o += up(sizes[k]);
+  }
+  L.bytes = o;
+  return L;
+}
+
 }  // namespace
 }  // namespace sfgb
 
@@ -646,6 +776,129 @@ int sf_flamelet_steady_psitc_batch(const sf_mech *mech, const sf_flamelet_batch 
     a.out_it = out_iterations;
     S.ctl(a);
     if (out_min_ds) S.reduce(S.ds, 1, out_min_ds);
+    return SF_OK;
+  } catch (sf_error &e) {
+    set_error(e.what());
+    return e.code;
+  }
+}
+
+size_t sf_flamelet_esdirk_workspace_size(const sf_mech *mech, const sf_flamelet_batch *fb)
+{
+  if (!mech || !fb || fb->n_flamelets < 1 || !fb->offsets_z_host) return 0;
+  return att_layout(mech, fb).bytes;
+}
+
+int sf_flamelet_esdirk_attempt_batch(const sf_mech *mech, const sf_flamelet_batch *fb, double *state,
+                                     const double *dt, const int *run, const int *setup, int any_setup,
+                                     double nonlinear_tolerance, int max_nonlinear_iter, int rates_option,
+                                     double *out_err, double *out_step_norm, double *out_nonfinite, int *out_nl_ok,
+                                     int *inout_newton, void *workspace, size_t workspace_bytes, void *stream)
+{
+  try {
+    if (!mech || !fb || !state || !dt || !run || !setup || !out_err || !out_step_norm || !out_nonfinite ||
+        !out_nl_ok || !inout_newton || max_nonlinear_iter < 1)
+      throw sf_error(SF_ERR_INVALID_ARGUMENT, "sf_flamelet_esdirk_attempt_batch: bad argument");
+    if (!workspace || workspace_bytes < sf_flamelet_esdirk_workspace_size(mech, fb))
+      throw sf_error(SF_ERR_WORKSPACE, "workspace smaller than sf_flamelet_esdirk_workspace_size reports");
+    const Layout L = att_layout(mech, fb);
+    const int ns = mech->m.dm.ns, nf = L.nf;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *w = static_cast<char *>(workspace);
+    double *values = reinterpret_cast<double *>(w + L.off[0]);
+    double *lvalues = reinterpret_cast<double *>(w + L.off[1]);
+    int *pivots = reinterpret_cast<int *>(w + L.off[2]);
+    AttBufs a{};
+    a.N = L.N;
+    a.ns = ns;
+    a.nf = nf;
+    a.k = reinterpret_cast<double *>(w + L.off[3]);
+    a.Y = reinterpret_cast<double *>(w + L.off[4]);
+    a.fs = reinterpret_cast<double *>(w + L.off[5]);
+    a.resid = reinterpret_cast<double *>(w + L.off[6]);
+    a.prior = reinterpret_cast<double *>(w + L.off[7]);
+    a.dx = reinterpret_cast<double *>(w + L.off[8]);
+    a.dstate = reinterpret_cast<double *>(w + L.off[9]);
+    a.eterm = reinterpret_cast<double *>(w + L.off[10]);
+    int *map = reinterpret_cast<int *>(w + L.off[11]);
+    a.map = map;
+    a.dt = dt;
+    a.state = state;
+    int *ci = reinterpret_cast<int *>(w + L.off[12]);
+    double *cd = reinterpret_cast<double *>(w + L.off[13]);
+    AttCtl c{};
+    c.run = run;
+    c.go = ci;
+    c.conv = ci + nf;
+    c.flags = ci + 2 * nf;
+    c.nl_ok = out_nl_ok;
+    c.newton = inout_newton;
+    c.nrm = cd;
+    c.pref = cd + nf;
+    c.dt = dt;
+    const int grid = grid_for(L.N);
+    auto cuda = [] { CUDA_THROW(cudaGetLastError()); };
+    auto ctl = [&](int op) {
+      k_att_ctl<<<1, 1024, 0, st>>>(c, nf, op, nonlinear_tolerance);
+      cuda();
+    };
+    auto reduce = [&](const double *v, int mode, double *out) {
+      k_reduce<<<nf, kThreads, 0, st>>>(nf, ns, fb->offsets_z, v, mode, out);
+      cuda();
+    };
+    auto check = [](int rc) {
+      if (rc != SF_OK) throw sf_error(rc, sf_last_error());
+    };
+    sf_flamelet_batch b = *fb;
+    b.diffterm = nullptr;
+    b.prefactor = nullptr;
+    k_point_map<<<nf, kThreads, 0, st>>>(nf, fb->offsets_z, map);
+    cuda();
+    ctl(4);  // prefactors gamma * dt; nl_ok = 1
+    if (any_setup) {
+      // the iteration matrix gamma dt J - I of every flamelet that needs a new one, with its own prefactor
+      b.active = setup;
+      b.prefactor = c.pref;
+      check(sf_flamelet_jac_batch(mech, &b, state, rates_option, 1, 0., 0., nullptr, values, nullptr, 0, stream));
+      b.prefactor = nullptr;
+      check(sf_btddod_factor_batch(nf, ns, fb->offsets_z, fb->offsets_v, fb->offsets_z_host, values, lvalues, pivots,
+                                   setup, stream));
+    }
+    b.active = run;
+    check(sf_flamelet_rhs_batch(mech, &b, state, a.k, stream));  // k_0
+    CUDA_THROW(cudaMemcpyAsync(a.Y, state, (size_t)L.N * 8, cudaMemcpyDeviceToDevice, st));
+    int hflag = 0;
+    for (int s = 1; s < 6; ++s) {
+      k_att_stage_start<<<grid, kThreads, 0, st>>>(a, s);
+      cuda();
+      ctl(0);
+      for (int it = 0; it < max_nonlinear_iter; ++it) {
+        ctl(1);
+        check(sf_btddod_solve_batch(nf, ns, fb->offsets_z, fb->offsets_v, fb->offsets_z_host, values, lvalues,
+                                    pivots, a.resid, a.dx, c.go, stream));
+        k_att_newton_update<<<grid, kThreads, 0, st>>>(a, c.go);
+        cuda();
+        b.active = c.go;
+        check(sf_flamelet_rhs_batch(mech, &b, a.Y, a.fs, stream));
+        k_att_newton_resid<<<grid, kThreads, 0, st>>>(a, c.go);
+        cuda();
+        reduce(a.resid, 0, c.nrm);
+        CUDA_THROW(cudaMemsetAsync(c.flags, 0, sizeof(int), st));
+        ctl(2);
+        CUDA_THROW(cudaMemcpyAsync(&hflag, c.flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_THROW(cudaStreamSynchronize(st));
+        if (!hflag) break;
+      }
+      CUDA_THROW(cudaMemcpyAsync(a.k + (size_t)s * L.N, a.fs, (size_t)L.N * 8, cudaMemcpyDeviceToDevice, st));
+      ctl(3);
+    }
+    k_att_step<<<grid, kThreads, 0, st>>>(a);
+    cuda();
+    reduce(a.eterm, 0, out_err);
+    reduce(a.dstate, 0, out_step_norm);
+    reduce(a.dstate, 2, out_nonfinite);
+    k_att_accept<<<grid, kThreads, 0, st>>>(a, run, out_nonfinite);
+    cuda();
     return SF_OK;
   } catch (sf_error &e) {
     set_error(e.what());

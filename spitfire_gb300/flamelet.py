@@ -705,7 +705,7 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
                      first_time_step=1.e-6, max_time_step=1.e-3, minimum_time_step_count=40,
                      maximum_time_step_count=None, transient_tolerance=1.e-10, maximum_steps_per_jacobian=10,
                      nonlinear_solve_tolerance=1.e-12, max_nonlinear_iter=20, save_each_step=True, active=None,
-                     max_attempts=1000000):
+                     max_attempts=1000000, host_attempts=False):
     """Transient integration of every flamelet of the batch b, each with its own time, step size and Jacobian.
 
     Batched restatement of Flamelet.integrate (flamelet.py:1046-1213) with its defaults: odesolve
@@ -723,7 +723,13 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
     minimum_time_step_count steps, as odesolve does (integrator.py:629-641). Returns (trajectories, stats):
     trajectories[f] = (times [nt], states [nt, nzi*ns]) with every accepted step (first and last only without
     save_each_step); stats: per-flamelet steps, failed_steps, newton_iters,
-    jac_setups and status (1 stop_at_time, 3 steady, 4 step limit, 7 stop criteria)."""
+    jac_setups and status (1 stop_at_time, 3 steady, 4 step limit, 7 stop criteria).
+
+    Each step attempt of the running flamelets (iteration matrices where needed, the five implicit stages with
+    their Newton iterations, the error and step norms, the acceptance) is one native call,
+    sf_flamelet_esdirk_attempt_batch; the step-size control, the stop rules and the recorded trajectory stay here.
+    host_attempts=True runs the same attempt as torch operations over the batch's primitives instead: the same
+    arithmetic in the same order, kept to check the native attempt against."""
     torch = _torch()
     dev = b.values.device
     nf, ns = b.nf, b.ns
@@ -748,22 +754,13 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
     k = [torch.zeros_like(state) for _ in range(6)]
     coerce = stop_at_time is not None
     mask = lambda m: torch.from_numpy(np.ascontiguousarray(m)).to(dev)
-    while run.any():
-        attempts[run] += 1
-        over = run & (attempts > max_attempts)
-        status[over] = 4
-        run &= ~over
-        if not run.any():
-            break
-        if coerce:
-            dt = np.where(run & (t + dt > stop_at_time), stop_at_time - t, dt)
-        need = run & eval_setup
+
+    def host_attempt(state, dt, run, need):
+        """One step attempt of the running flamelets as torch operations (the native attempt's check)."""
         if need.any():
             # one launch for every flamelet that needs a setup, each with its own prefactor gamma * dt
             b.jacobian(state, scale_and_offset=True, prefactor=torch.from_numpy(dt * G).to(dev), active=mask(need))
             b.factor(active=mask(need))
-            jac_setups[need] += 1
-        setup_count[run] += 1
         runm = mask(run)
         dtd = b.expand(torch.from_numpy(dt).to(dev))
         k[0] = b.rhs(state, out=k[0], active=runm)
@@ -778,7 +775,7 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
             go = runm.clone()
             conv = torch.zeros(nf, dtype=torch.bool, device=dev)
             for _ in range(max_nonlinear_iter):
-                newton += go.cpu().numpy()
+                newton[:] += go.cpu().numpy()
                 god = b.expand(go)
                 dx = b.solve(resid, active=go)
                 Y = torch.where(god, Y - dx, Y)
@@ -805,6 +802,47 @@ def _integrate_batch(b, state=None, stop_criteria=None, stop_at_time=None, stop_
             new = state + dstate
             new = torch.where(new < 0., torch.zeros_like(new), new)
             state = torch.where(b.expand(mask(acc)), new, state)
+        return state, err, residual, fin, nl_ok
+
+    if not host_attempts:
+        L = N.load()
+        nb = int(L.sf_flamelet_esdirk_workspace_size(b.g.handle, C.byref(b.fb)))
+        att_ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=dev)
+        dtt = torch.empty(nf, dtype=torch.float64, device=dev)
+        runi = torch.empty(nf, dtype=torch.int32, device=dev)
+        needi = torch.empty(nf, dtype=torch.int32, device=dev)
+        att_err, att_norm, att_bad = (torch.empty(nf, dtype=torch.float64, device=dev) for _ in range(3))
+        att_nlok = torch.empty(nf, dtype=torch.int32, device=dev)
+        att_newton = torch.zeros(nf, dtype=torch.int32, device=dev)
+        state = state.contiguous()
+    while run.any():
+        attempts[run] += 1
+        over = run & (attempts > max_attempts)
+        status[over] = 4
+        run &= ~over
+        if not run.any():
+            break
+        if coerce:
+            dt = np.where(run & (t + dt > stop_at_time), stop_at_time - t, dt)
+        need = run & eval_setup
+        setup_count[run] += 1
+        jac_setups[need] += 1
+        if host_attempts:
+            state, err, residual, fin, nl_ok = host_attempt(state, dt, run, need)
+        else:
+            dtt.copy_(torch.from_numpy(dt))
+            runi.copy_(torch.from_numpy(run.astype(np.int32)))
+            needi.copy_(torch.from_numpy(need.astype(np.int32)))
+            N.check(L.sf_flamelet_esdirk_attempt_batch(
+                b.g.handle, C.byref(b.fb), N.ptr(state), N.ptr(dtt), N.ptr(runi), N.ptr(needi), int(need.any()),
+                float(nonlinear_solve_tolerance), int(max_nonlinear_iter), int(b.rates_option), N.ptr(att_err),
+                N.ptr(att_norm), N.ptr(att_bad), N.ptr(att_nlok), N.ptr(att_newton), N.ptr(att_ws),
+                att_ws.numel() * 8, N.stream_handle()))
+            outs = torch.cat([att_err, att_norm, att_bad, att_nlok.double(), att_newton.double()]).cpu().numpy()
+            err, residual = outs[:nf], outs[nf:2 * nf] / dt
+            fin = outs[2 * nf:3 * nf] == 0.
+            nl_ok = outs[3 * nf:4 * nf] != 0.
+            newton[:] = outs[4 * nf:5 * nf].astype(np.int64)
         # the states reach the host only for the recorded trajectory or a stop criterion
         host = state.cpu().numpy() if (save_each_step or stop_criteria is not None) else None
         for f in np.flatnonzero(run):

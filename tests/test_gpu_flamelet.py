@@ -505,3 +505,41 @@ def test_native_steady_solvers_match_host_loop(cuda, name):
         assert torch.equal(a[0], h[0]), kw
         assert torch.equal(mds_a, mds_h), (kw, mds_a, mds_h)
     assert spec.griffon.device_status() == 0
+
+
+def test_native_transient_attempts_match_host_attempts(cuda):
+    """The transient integrator's native step attempt (sf_flamelet_esdirk_attempt_batch) against the same attempt as
+    torch operations (host_attempts=True) on a ragged batch of a nonadiabatic and an adiabatic H2 flamelet of
+    different grids and dissipation rates: bit-identical step times, states and counters over the whole run, with
+    Jacobian reuse, rejected steps and an end time."""
+    import os
+    from spitfire_gb300.flamelet import FlameletBatch, FlameletSetup, FlameletSpec, _integrate_batch
+    from spitfire_gb300.mechanism import ChemicalMechanismSpec
+    g = np.load(os.path.join(FC.GOLD, 'nonadiabatic_transient_slfm_gold.npz'))
+    m = ChemicalMechanismSpec.bundled('h2-burke')
+    air = m.stream(stp_air=True)
+    air.TP = 1200., 101325.
+    fuel = m.stream('TPY', (300., 101325., 'H2:1'))
+    common = dict(mech_spec=m, oxy_stream=air, fuel_stream=fuel)
+    heat = FlameletSetup(FlameletSpec(grid_points=34, initial_condition=g['adiabatic_state'],
+                                      stoich_dissipation_rate=1., heat_transfer='nonadiabatic',
+                                      scale_heat_loss_by_temp_range=True, scale_convection_by_dissipation=True,
+                                      use_linear_ref_temp_profile=True, convection_coefficient=1.e7,
+                                      radiative_emissivity=0., **common))
+    ign = FlameletSetup(FlameletSpec(grid_points=21, initial_condition='linear-TY', stoich_dissipation_rate=3.,
+                                     **common))
+    # 2e-5 s: the heat-loss flamelet is still burning (its loss coefficient is divided by max T - T_conv, which
+    # vanishes once it has cooled to the oxidizer temperature), the other is igniting
+    kw = dict(stop_at_time=2.e-5, first_time_step=1.e-8, max_time_step=1.e-4, transient_tolerance=1.e-10,
+              maximum_steps_per_jacobian=5, max_attempts=5000)
+    b = FlameletBatch([heat, ign])
+    tn, sn = _integrate_batch(b, **kw)
+    b2 = FlameletBatch([heat, ign])
+    th, sh = _integrate_batch(b2, host_attempts=True, **kw)
+    for key in ('steps', 'failed_steps', 'newton_iters', 'jac_setups', 'status'):
+        assert np.array_equal(sn[key], sh[key]), (key, sn[key], sh[key])
+    assert sn['steps'].min() > 20 and (sn['status'] == 1).all()
+    for f in range(2):
+        assert np.array_equal(tn[f][0], th[f][0]), f
+        assert np.array_equal(tn[f][1], th[f][1]), f
+    assert m.griffon.device_status() == 0

@@ -104,8 +104,8 @@ def test_integrate_batch_host_logic_reproduces_reference_trajectory():
     from spitfire_gb300.flamelet import _integrate_batch
     g, spec, og, s, Tb = _case()
     b = CpuBatch([_heat_op(og, s)], [g['adiabatic_state']])
-    traj, stats = _integrate_batch(b, stop_criteria=_stop(Tb), first_time_step=1.e-9, max_time_step=1.e-1,
-                                   transient_tolerance=1.e-10)
+    traj, stats = _integrate_batch(b, host_attempts=True, stop_criteria=_stop(Tb), first_time_step=1.e-9,
+                                   max_time_step=1.e-1, transient_tolerance=1.e-10)
     times, states = traj[0]
     assert stats['steps'][0] == g['times'].size - 1
     assert stats['status'][0] == 7
@@ -122,9 +122,9 @@ def test_integrate_batch_ragged_flamelets_match_their_own_runs():
     ops = [_heat_op(og, s1), _heat_op(og, s2)]
     st = [g['adiabatic_state'], g['adiabatic_state']]
     kw = dict(stop_criteria=_stop(Tb), first_time_step=1.e-9, max_time_step=1.e-1, transient_tolerance=1.e-10)
-    both, sb = _integrate_batch(CpuBatch(ops, st), **kw)
+    both, sb = _integrate_batch(CpuBatch(ops, st), host_attempts=True, **kw)
     for f in range(2):
-        alone, sa = _integrate_batch(CpuBatch([ops[f]], [st[f]]), **kw)
+        alone, sa = _integrate_batch(CpuBatch([ops[f]], [st[f]]), host_attempts=True, **kw)
         assert sb['steps'][f] == sa['steps'][0]
         np.testing.assert_array_equal(both[f][0], alone[0][0])
         np.testing.assert_array_equal(both[f][1], alone[0][1])
@@ -162,7 +162,8 @@ def test_integrate_batch_stop_at_time_active_mask_and_first_last_output():
     ops = [_heat_op(og, s1), _heat_op(og, s2)]
     st = [g['adiabatic_state'], g['adiabatic_state']]
     kw = dict(stop_at_time=2.e-5, first_time_step=1.e-9, max_time_step=1.e-1, transient_tolerance=1.e-10)
-    traj, stats = _integrate_batch(CpuBatch(ops, st), active=np.array([True, False]), save_each_step=False, **kw)
+    traj, stats = _integrate_batch(CpuBatch(ops, st), host_attempts=True, active=np.array([True, False]),
+                                   save_each_step=False, **kw)
     ref = integrate(FT.FlameletTransientProblem(ops[0]), st[0], **kw)
     assert stats['status'][0] == 1 and stats['steps'][0] == ref['steps']
     times, states = traj[0]
