@@ -517,9 +517,9 @@ __global__ void k_att_accept(AttBufs a, const int *run, const double *nonfinite)
   }
 }
 
-// per-flamelet bookkeeping of the attempt: 0 start (go = run, conv = 0, nl_ok = 1 on the first stage),
-// 1 newton += go, 2 convergence test (nrm < tol) and the any-go flag, 3 end of stage (nl_ok &= conv | !run),
-// 4 prefactors gamma * dt
+// per-flamelet bookkeeping of the attempt: 0 start of a stage (go = run, conv = 0), 1 newton += go,
+// 2 convergence test (nrm < tol) and the any-go flag, 3 end of a stage (nl_ok &= conv | !run),
+// 4 start of the attempt (prefactors gamma * dt, nl_ok = 1)
 struct AttCtl {
   const int *run;
   int *go, *conv, *nl_ok, *newton, *flags;
@@ -548,7 +548,7 @@ __global__ void k_att_ctl(AttCtl c, int nf, int op, double tol)
 
 // Workspace of an attempt: 0 values, 1 lvalues, 2 pivots (the iteration matrix factors, kept from one attempt to
 // the next), 3 stage derivatives (6 N), 4 Y, 5 fs, 6 resid, 7 prior, 8 dx, 9 dstate, 10 eterm, 11 map,
-// 12 ints (go, conv, flags), 13 doubles (nrm, pref, nonfinite)
+// 12 ints (go, conv, flags), 13 doubles (nrm, pref)
 Layout att_layout(const sf_mech *mech, const sf_flamelet_batch *fb)
 {
   Layout L{};
@@ -563,7 +563,7 @@ Layout att_layout(const sf_mech *mech, const sf_flamelet_batch *fb)
   }
   const size_t N8 = (size_t)L.N * 8;
   const size_t sizes[14] = {(size_t)L.V * 8, (size_t)L.P * ns * ns * 8, (size_t)L.P * ns * 4, 6 * N8, N8, N8, N8,
-                            N8, N8, N8, N8, (size_t)L.P * 4, (size_t)(2 * L.nf + 16) * 4, (size_t)3 * L.nf * 8};
+                            N8, N8, N8, N8, (size_t)L.P * 4, (size_t)(2 * L.nf + 16) * 4, (size_t)2 * L.nf * 8};
   size_t o = 0;
   for (int k = 0; k < 14; ++k) {
     L.off[k] = o;
