@@ -603,10 +603,17 @@ def bench_flamelet(spec, rank, stream, cpu):
     rhs_bytes = pts * 4 * ns * 8
     # per point: LU 2/3 ns^3 flops, the inverse from the LU factors 4/3 ns^3 (identity right-hand sides)
     fac_flops = pts * 2. * ns ** 3
+    mv_fmas = float(nvals)  # one FMA per matrix value (diagonal blocks and the sub/super-diagonal values)
+    _, issue_peak = fp64_fma_probe(20000, 32)
     k['roofline'] = {
         'matvec': {'bound': 'hbm', 'algorithmic_bytes': mv_bytes, 'achieved': mv_bytes / (k['matvec_ms'] * 1e-3)
                    / 1e9, 'peak': hbm, 'unit': 'GB/s', 'frac': mv_bytes / (k['matvec_ms'] * 1e-3) / 1e9 / hbm,
-                   'peak_source': hbm_src},
+                   'peak_source': hbm_src,
+                   # one FMA per 8-byte value is 0.25 flop/byte, above GB300's FP64 balance: FP64 issue binds first
+                   'fp64_issue': {'warp_instr': mv_fmas / 32., 'achieved_per_s': mv_fmas / 32. / (k['matvec_ms'] * 1e-3),
+                                  'peak_per_s': issue_peak,
+                                  'frac': mv_fmas / 32. / (k['matvec_ms'] * 1e-3) / issue_peak,
+                                  'peak_source': 'bench_fp64_fma (bench_probes.cu), measured live'}},
         'rhs_sweep': {'bound': 'fp64 (rates per point); HBM bytes reported', 'algorithmic_bytes': rhs_bytes,
                       'achieved_gbs': rhs_bytes / (k['rhs_ms'] * 1e-3) / 1e9,
                       'points_per_s': pts / (k['rhs_ms'] * 1e-3)},
