@@ -47,20 +47,26 @@ __device__ void warp_balance(double *A, int n, int max_sweeps = 32)
       c = warp_sum_all(c);
       r = warp_sum_all(r);
       if (c == 0. || r == 0. || !isfinite(c) || !isfinite(r)) continue;
-      double g = r * 0.5, f = 1.;
+      // the scaling f = 2^m; m is counted in an integer and f, 1 / f built from it: the same powers of two the
+      // repeated doublings and halvings give, without their FP64 multiplies and the division
+      double g = r * 0.5;
+      int m = 0;
       const double s = c + r;
       for (int t = 0; t < 1100 && c < g; ++t) {
-        f *= 2.;
         c *= 4.;
+        ++m;
       }
       g = r * 2.;
       for (int t = 0; t < 1100 && c >= g; ++t) {
-        f *= 0.5;
         c *= 0.25;
+        --m;
       }
-      if ((c + r) / f < 0.95 * s) {
+      const bool normal = m >= -1000 && m <= 1000;
+      const double f = normal ? __longlong_as_double((long long)(1023 + m) << 52) : ldexp(1., m);
+      const double fi = normal ? __longlong_as_double((long long)(1023 - m) << 52) : 1. / f;
+      // (c + r) / f, exactly, as a product with the exact reciprocal
+      if ((normal ? (c + r) * fi : (c + r) / f) < 0.95 * s) {
         changed = true;
-        const double fi = 1. / f;  // a power of two: exact
         for (int j = lane; j < n; j += 32) {
           A[i + j * n] *= fi;
           A[j + i * n] *= f;
