@@ -24,6 +24,19 @@ __device__ __forceinline__ double warp_sum_all(double v)
   return v;
 }
 
+// Both sums of two per-lane values in every lane, with five FP64 additions per lane instead of ten: the first
+// exchange leaves the half-sums of a in lanes 0-15 and of b in lanes 16-31, and each half then reduces its own.
+__device__ __forceinline__ void warp_sum_pair(double &a, double &b)
+{
+  const int lane = threadIdx.x & 31;
+  const bool lo = lane < 16;
+  double v = lo ? a : b;
+  v += __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  a = __shfl_sync(0xffffffffu, v, 0);
+  b = __shfl_sync(0xffffffffu, v, 16);
+}
+
 __device__ __forceinline__ double warp_max_all(double v)
 {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -44,8 +57,7 @@ __device__ void warp_balance(double *A, int n, int max_sweeps = 32)
           c += fabs(A[j + i * n]);
           r += fabs(A[i + j * n]);
         }
-      c = warp_sum_all(c);
-      r = warp_sum_all(r);
+      warp_sum_pair(c, r);
       if (c == 0. || r == 0. || !isfinite(c) || !isfinite(r)) continue;
       // the scaling f = 2^m; m is counted in an integer and f, 1 / f built from it: the same powers of two the
       // repeated doublings and halvings give, without their FP64 multiplies and the division
