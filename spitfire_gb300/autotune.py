@@ -156,10 +156,19 @@ def tune_integrator(integrator, q0, pressures=None, reps=1, **controls):
                 set_tuning(mech, 'integrate_warps', saved[1])
                 raise RuntimeError(f'integrator shape {(scratch, warps)} changed the results')
             times[(scratch, warps)] = _time(lambda: integrator.run(q0, pressures=pressures, **controls), reps)
-    best = min(times, key=times.get)
+    best = pick_integrator_shape(times)
     set_tuning(mech, 'integrate_scratch', best[0])
     set_tuning(mech, 'integrate_warps', best[1])
     return best, times
+
+
+def pick_integrator_shape(times, within=0.02):
+    """The integrator shape to keep from {(scratch, warps): ms} of a tuning sample. The sample is smaller than the
+    batches the tuning serves, and the larger shapes gain on larger batches (8192 GRI ignitions: 8 warps per block
+    3-4 % faster than 6, which tie on 4096 reactors), so among the shapes within `within` of the fastest the one
+    with the most warps per block wins, the faster one on equal warps."""
+    fastest = min(times.values())
+    return max((k for k in times if times[k] <= (1. + within) * fastest), key=lambda k: (k[1], -times[k]))
 
 
 def _fitting_warps(integrator):

@@ -145,3 +145,16 @@ def test_two_rank_gloo_sharding_matches_single_process():
     rhs, J = og.reactor_jac_batch(P, q, 0)
     assert np.array_equal(full, np.hstack([rhs, J]))
     assert t == 1.5 and n == 37
+
+
+def test_integrator_shape_choice_prefers_more_warps_among_near_ties():
+    """The tuner keeps the shape with the most warps per block among those within 2 % of the fastest on its sample
+    (larger shapes gain on batches larger than the sample), and the fastest shape otherwise."""
+    from spitfire_gb300.autotune import pick_integrator_shape
+    times = {(3, 1): 7982.8, (3, 2): 4204.8, (1, 3): 2994.2, (1, 5): 2447.3, (2, 4): 2214.2, (2, 6): 1971.6,
+             (2, 8): 1984.3}
+    assert pick_integrator_shape(times) == (2, 8)
+    times[(2, 8)] = 2030.
+    assert pick_integrator_shape(times) == (2, 6)
+    assert pick_integrator_shape({(1, 5): 10., (2, 5): 10.1, (2, 4): 9.9}) == (1, 5)
+    assert pick_integrator_shape({(2, 6): 5.}) == (2, 6)
