@@ -728,7 +728,9 @@ def build_probes():
     out_dir = os.path.join(ROOT, '_build')
     lib = os.path.join(out_dir, 'libbench_probes.so')
     stamp = lib + '.stamp'
-    h = hashlib.sha256(open(src, 'rb').read() + ' '.join(B.ARCH).encode() + os.uname().machine.encode()).hexdigest()
+    deps = [src] + [os.path.join(B.CSRC, f) for f in ('chem_device.cuh', 'exp_table.h', 'sf_mech.h')]
+    h = hashlib.sha256(b''.join(open(f, 'rb').read() for f in deps) + ' '.join(B.ARCH).encode() +
+                       os.uname().machine.encode()).hexdigest()
     if os.path.exists(lib) and os.path.exists(stamp) and open(stamp).read() == h:
         return lib
     os.makedirs(out_dir, exist_ok=True)
@@ -750,6 +752,8 @@ def _probes():
         L.bench_fp64_dmma.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
         L.bench_fp64_mixed.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
         L.bench_store.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_double), C.c_void_p]
+        L.bench_exp.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        L.bench_exp_values.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
         _PROBES = L
     return _PROBES
 
@@ -884,23 +888,13 @@ def case_rates_rhs():
     return spec
 
 
-def case_integrate():
-    from spitfire_gb300 import workloads as W
-    from spitfire_gb300.reactors import BatchIntegrator
-    spec = _spec()
-    d = W.ignition_batch(spec, 256, seed=1003)
-    BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
-                                          stop_at_time=0.1)
-    return spec
-
-
 def case_integrate_2048():
     from spitfire_gb300 import autotune as AT
     from spitfire_gb300 import workloads as W
     from spitfire_gb300.reactors import BatchIntegrator
     spec = _spec()
-    AT.set_tuning(spec, 'integrate_scratch', 1)
-    AT.set_tuning(spec, 'integrate_warps', 6)
+    AT.set_tuning(spec, 'integrate_scratch', 2)
+    AT.set_tuning(spec, 'integrate_warps', 8)
     d = W.ignition_batch(spec, 2048, seed=1003)
     BatchIntegrator(spec, 'isobaric').run(d['q0'], pressures=d['p'], delta_temperature_ignition=400.,
                                           stop_at_time=0.1)
@@ -972,6 +966,59 @@ def case_dmma():
     return None
 
 
+def case_exp():
+    """CUDA's exp against the library's table-driven tab_exp: FP64 instructions per call in throughput loops, and
+    accuracy in ulps against numpy's long double exponential (113-bit on the Arm host, 64-bit on x86)."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    L = _probes()
+    sink = torch.zeros(1, dtype=torch.float64, device='cuda')
+    st = torch.cuda.current_stream().cuda_stream
+    _, wi = fp64_fma_probe(4000, 32)
+    iters = 1024
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    calls = 4. * iters * nsm * 8 * 256
+    ms = []
+    for which in (0, 1, 2):
+        v = C.c_double()
+        if L.bench_exp(which, iters, C.byref(v), sink.data_ptr(), st):
+            raise RuntimeError('bench_exp failed')
+        ms.append(v.value)
+    per = [(m - ms[0]) * 1e-3 * wi / (calls / 32.) for m in ms]
+    print(f'warp FP64 instructions/s (bench_fp64_fma): {wi:.4e}')
+    print(f'loop alone {ms[0]:.3f} ms; CUDA exp {ms[1]:.3f} ms, {per[1]:.2f} warp FP64 instructions per call beyond '
+          f'the loop; tab_exp {ms[2]:.3f} ms, {per[2]:.2f}')
+    rng = np.random.default_rng(7)
+    n = 1 << 21
+    x = np.concatenate([rng.uniform(-745.1, 709.7, n), rng.uniform(-80., 5., n), rng.uniform(-0.02, 0.02, n)])
+    xd = torch.from_numpy(x).cuda()
+    oc, ot = torch.empty_like(xd), torch.empty_like(xd)
+    if L.bench_exp_values(xd.data_ptr(), oc.data_ptr(), ot.data_ptr(), xd.numel(), st):
+        raise RuntimeError('bench_exp_values failed')
+    c, t = oc.cpu().numpy(), ot.cpu().numpy()
+    sel = np.arange(0, x.size, 3)
+    ref = np.exp(x[sel].astype(np.longdouble))
+    ok = np.isfinite(ref) & (ref >= np.longdouble(np.finfo(np.float64).tiny)) & \
+        (ref < np.longdouble(np.finfo(np.float64).max))
+    ulp = np.spacing(ref[ok].astype(np.float64)).astype(np.longdouble)
+    print(f'accuracy on {int(ok.sum())} normal results (reference: numpy long double, '
+          f'{np.finfo(np.longdouble).nmant + 1}-bit):')
+    for name, v in (('CUDA exp', c), ('tab_exp', t)):
+        e = np.abs((v[sel][ok].astype(np.longdouble) - ref[ok]) / ulp).astype(np.float64)
+        cr = float(np.mean(v[sel][ok] == ref[ok].astype(np.float64)))
+        print(f'  {name}: max {e.max():.3f} ulp, mean {e.mean():.4f} ulp, correctly rounded {cr:.4f}')
+    print(f'tab_exp equal to CUDA exp bit for bit: {float(np.mean(c == t)):.4f} of {x.size}')
+    special = np.array([0., -0., np.inf, -np.inf, np.nan, 709.78, -745.2, -708.5, 1e-300])
+    sd = torch.from_numpy(special).cuda()
+    sc, stt = torch.empty_like(sd), torch.empty_like(sd)
+    L.bench_exp_values(sd.data_ptr(), sc.data_ptr(), stt.data_ptr(), sd.numel(), st)
+    print('special arguments (x, CUDA exp, tab_exp):')
+    for a, b, d in zip(special, sc.cpu().numpy(), stt.cpu().numpy()):
+        print(f'  {a!r}: {b!r} {d!r}')
+    return None
+
+
 def case_sysmem():
     import torch
     n = 1536 * 1024 * 1024 // 8
@@ -1011,7 +1058,7 @@ def case_sysmem():
 
 
 PROFILE_CASES = {'jac': case_jac, 'jac_tps': case_jac_tps, 'rates_rhs': case_rates_rhs,
-                 'integrate_2048': case_integrate_2048, 'integrate': case_integrate, 'flamelet': case_flamelet,
+                 'integrate_2048': case_integrate_2048, 'exp': case_exp, 'flamelet': case_flamelet,
                  'adjoint': case_adjoint, 'adjoint_sweep': case_adjoint_sweep, 'fp64issue': case_fp64issue, 'dmma': case_dmma, 'sysmem': case_sysmem}
 
 

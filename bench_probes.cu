@@ -12,6 +12,12 @@
 //   bench_fp64_mixed  even warps run the DFMA chains, odd warps the m8n8k4 MMAs, with equal flops per warp: about
 //                     the DFMA rate if the two share one FP64 unit, about twice it if they issue side by side
 //
+//   bench_exp         e^x throughput in register loops (8 blocks of 256 threads per SM, four independent sums per
+//                     thread): 0 the loop alone, 1 CUDA's exp, 2 the library's table-driven tab_exp
+//                     (spitfire_gb300/csrc/chem_device.cuh); the caller turns the times into FP64 instructions per call
+//                     with the issue rate of bench_fp64_fma
+//   bench_exp_values  both exponentials of n device values, for their accuracy against a wider reference
+//
 //   bench_store       stores from the SMs into a buffer, device memory or pinned host memory reached over the host
 //                     link (the device address of a pinned allocation comes from cudaHostGetDevicePointer, and the
 //                     call refuses host memory without one): pattern 0 coalesced (consecutive lanes, consecutive
@@ -25,7 +31,52 @@
 
 #include <algorithm>
 
+#include "spitfire_gb300/csrc/chem_device.cuh"
+
 namespace {
+
+__constant__ double cExpTab[128];  // sfgb::kExpTable, copied by exp_table_ready()
+
+int exp_table_ready()
+{
+  static bool done = false;
+  if (!done && cudaMemcpyToSymbol(cExpTab, sfgb::kExpTable, sizeof(sfgb::kExpTable)) == cudaSuccess) done = true;
+  return done ? 0 : 1;
+}
+
+template <int WHICH>
+__global__ void __launch_bounds__(256) exp_probe_kernel(int iters, double x0, double dx, double *sink)
+{
+  __shared__ __align__(16) double tab[128];
+  if (threadIdx.x < 128) tab[threadIdx.x] = cExpTab[threadIdx.x];
+  __syncthreads();
+  double x = x0 - 40. * (double)((blockIdx.x * blockDim.x + threadIdx.x) & 1023) / 1024.;
+  double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
+  for (int i = 0; i < iters; ++i) {
+    if (WHICH == 0) {
+      a0 += x; a1 += x + dx; a2 += x + 2. * dx; a3 += x + 3. * dx;
+    } else if (WHICH == 1) {
+      a0 += exp(x); a1 += exp(x + dx); a2 += exp(x + 2. * dx); a3 += exp(x + 3. * dx);
+    } else {
+      a0 += sfgb::tab_exp(x, tab); a1 += sfgb::tab_exp(x + dx, tab);
+      a2 += sfgb::tab_exp(x + 2. * dx, tab); a3 += sfgb::tab_exp(x + 3. * dx, tab);
+    }
+    x += 4. * dx;
+  }
+  const double v = a0 + a1 + a2 + a3;
+  if (v == 12345.678) sink[0] = v;  // keeps the sums live
+}
+
+__global__ void exp_values_kernel(const double *x, double *oc, double *ot, long long n)
+{
+  __shared__ __align__(16) double tab[128];
+  if (threadIdx.x < 128) tab[threadIdx.x] = cExpTab[threadIdx.x];
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    oc[i] = exp(x[i]);
+    ot[i] = sfgb::tab_exp(x[i], tab);
+  }
+}
 
 __global__ void fma_probe_kernel(int iters, double seed, double *sink, int active_lanes)
 {
@@ -227,6 +278,37 @@ int bench_fp64_mixed(int iters, double *out_tflops, double *sink, void *stream)
   const double flops = 512.0 * (double)iters * blocks * (threads / 32);
   *out_tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
+}
+
+// Milliseconds of one exp_probe_kernel launch (4 iters exponentials per thread), which = 0, 1, 2 as above.
+int bench_exp(int which, int iters, double *out_ms, double *sink, void *stream)
+{
+  if (which < 0 || which > 2 || iters < 1 || !out_ms || !sink) return 2;
+  if (exp_table_ready()) return 1;
+  int blocks, threads;
+  shape(&blocks, &threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  float ms = 0.f;
+  const int rc = timed(st, [&](int it) {
+    const int n = it < 0 ? iters : it;
+    if (which == 0) exp_probe_kernel<0><<<blocks, threads, 0, st>>>(n, -1., 1.e-6, sink);
+    if (which == 1) exp_probe_kernel<1><<<blocks, threads, 0, st>>>(n, -1., 1.e-6, sink);
+    if (which == 2) exp_probe_kernel<2><<<blocks, threads, 0, st>>>(n, -1., 1.e-6, sink);
+  }, &ms);
+  *out_ms = ms;
+  return rc;
+}
+
+// exp (CUDA) and tab_exp of n device values into two device arrays.
+int bench_exp_values(const double *x, double *out_cuda, double *out_tab, long long n, void *stream)
+{
+  if (!x || !out_cuda || !out_tab || n < 0) return 2;
+  if (n == 0) return 0;
+  if (exp_table_ready()) return 1;
+  int blocks, threads;
+  shape(&blocks, &threads);
+  exp_values_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(x, out_cuda, out_tab, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
 // GB/s of stores into `buffer` (bytes, a device allocation or a pinned host allocation).

@@ -47,7 +47,7 @@ __device__ double falloff_factor(const DevMech &m, const Blob &b, const ScratchL
   case 1: kf = kc[0] * s.T; break;
   case 2: kf = kc[0] * s.T * s.T; break;
   case 3: kf = kc[0] * s.invT; break;
-  default: kf = kc[0] * exp(kc[1] * s.logT - kc[2] * s.invT); break;
+  default: kf = kc[0] * tab_exp(kc[1] * s.logT - kc[2] * s.invT, b.d + m.d_exptab); break;
   }
   const double *y = scr + L.y;
   const int t0 = b.i[m.i_tb_off + r], t1 = b.i[m.i_tb_off + r + 1];
@@ -56,15 +56,15 @@ __device__ double falloff_factor(const DevMech &m, const Blob &b, const ScratchL
   const double M = b.d[m.d_beff + r] * s.ct + s.rho * sumtb;
   const int f = b.i[m.i_fall + r];
   const double *kp = b.d + m.d_kp + 3 * f;
-  const double pr = kp[0] * exp(kp[1] * s.logT - kp[2] * s.invT) / kf * M;
+  const double pr = kp[0] * tab_exp(kp[1] * s.logT - kp[2] * s.invT, b.d + m.d_exptab) / kf * M;
   double fac = pr / (1. + pr);
   if (kind == 4 && pr > 1.e-300) {
     const double *tr = b.d + m.d_troe + 4 * f;
     const int terms = (info >> RI_TROE_SHIFT) & 7;
     double fc = 0.;
-    if (terms & 1) fc += (1 - tr[0]) * exp(-s.T / tr[1]);
-    if (terms & 2) fc += tr[0] * exp(-s.T / tr[2]);
-    if (terms & 4) fc += exp(-s.invT * tr[3]);
+    if (terms & 1) fc += (1 - tr[0]) * tab_exp(-s.T / tr[1], b.d + m.d_exptab);
+    if (terms & 2) fc += tr[0] * tab_exp(-s.T / tr[2], b.d + m.d_exptab);
+    if (terms & 4) fc += tab_exp(-s.invT * tr[3], b.d + m.d_exptab);
     const double lfc = log10(fc);
     const double nn = 0.75 - 1.27 * lfc;
     const double lpc = log10(pr) + (-0.4 - 0.67 * lfc);

@@ -8,6 +8,7 @@
 //   dense/sparse sensitivity classification                       (:543-602)
 //   rate-constant temperature form and Troe term flags            (:670-730)
 #include "sf_internal.h"
+#include "exp_table.h"
 
 #include <algorithm>
 #include <cmath>
@@ -241,6 +242,9 @@ void HostMech::build(const sf_mech_desc *d)
   D[m.d_one] = 1.;
   m.d_smallint = dsec(64);
   for (int k = 0; k < 64; ++k) D[m.d_smallint + k] = k - 32;
+  while (D.size() % 2) D.push_back(0.);  // 16-byte boundary: the table is read as (head, tail) pairs
+  m.d_exptab = dsec(128);
+  std::copy(kExpTable, kExpTable + 128, D.begin() + m.d_exptab);
   m.i_info = isec(nr);
   m.i_orig = isec(nr);
   for (int r = 0; r < nr; ++r) I[m.i_orig + r] = orig_index[r];

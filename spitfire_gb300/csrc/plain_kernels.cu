@@ -63,7 +63,7 @@ __device__ void plain_state(const DevMech &m, const Blob &b, const ScratchLayout
     const double invmw = b.d[m.d_invmw + i];
     scr[L.C + i] = scr[L.y + i] * rho * invmw;
     const SpeciesThermo th = species_thermo(m, b, i, T, s.logT, s.invT, JAC);
-    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu);
+    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu, b.d + m.d_exptab);
     scr[L.eh + i] = iso ? th.h - m.Ru * T * invmw : th.h;
     scr[L.cpv + i] = iso ? th.cp - m.Ru * invmw : th.cp;
     if (JAC) {

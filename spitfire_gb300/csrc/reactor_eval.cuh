@@ -46,7 +46,7 @@ __device__ __forceinline__ SpeciesSums prep_species(const DevMech &m, const Blob
     const double invmw = b.d[m.d_invmw + i];
     scr[L.C + i] = yi * s.rho * invmw;
     const SpeciesThermo th = species_thermo(m, b, i, s.T, s.logT, s.invT, JAC);
-    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu);
+    store_gibbs_factor(scr, L, i, th.g * s.invT * m.invRu, b.d + m.d_exptab);
     if (want_eh) {
       scr[L.eh + i] = isochoric ? th.h - m.Ru * s.T * invmw : th.h;
       scr[L.cpv + i] = isochoric ? th.cp - m.Ru * invmw : th.cp;

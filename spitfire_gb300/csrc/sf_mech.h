@@ -46,6 +46,7 @@ struct DevMech {
   int d_one;     // 1.0
   int d_smallint;  // [64] the integer k - 32 at index k (stoichiometric coefficients without conversions); kept
                    // small because every kernel stages the blob into shared memory
+  int d_exptab;    // [128] 2^(j/64) as (head, tail) pairs, j = 0..63, for the table-driven exponential; even offset
 
   // ---- int section offsets ----
   int i_info;    // [nr]
