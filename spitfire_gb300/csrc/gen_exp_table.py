@@ -13,7 +13,8 @@ import os
 import mpmath as mp
 
 
-def main():
+def header_text():
+    """The text of exp_table.h."""
     mp.mp.prec = 300
     ln2 = mp.log(2)
     inv_l = float(64 / ln2)
@@ -36,9 +37,13 @@ def main():
     for j in range(64):
         lines.append(f'    {tab[2 * j].hex()}, {tab[2 * j + 1].hex()},')
     lines += ['};', '', '}  // namespace sfgb', '']
+    return '\n'.join(lines)
+
+
+def main():
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'exp_table.h')
     with open(out, 'w') as f:
-        f.write('\n'.join(lines))
+        f.write(header_text())
     print(out)
 
 
