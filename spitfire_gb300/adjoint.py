@@ -97,9 +97,10 @@ class ReactorAdjoint:
         self.integrator = BatchIntegrator(mech, configuration, pressure=pressure)
 
     # ------------------------------------------------------------------------------------------------- forward
-    def forward(self, q0, pressures=None, t_end=5.e-3, capacity=512, **controls):
-        """Integrate every row of q0 to t_end, recording the steps. Grows the record capacity until no reactor
-        runs out of it."""
+    def forward(self, q0, pressures=None, t_end=5.e-3, capacity=None, **controls):
+        """Integrate every row of q0 to t_end, recording the steps. The record starts at `capacity` steps per
+        reactor (None: BatchIntegrator.default_record_capacity, up to 1024 within a quarter of the free device
+        memory) and grows for the reactors that run out of it, which alone are integrated again."""
         torch = _torch()
         q0 = self.g._dev(q0)
         n = q0.shape[0]
@@ -107,18 +108,8 @@ class ReactorAdjoint:
             pressures = torch.full((n,), float(self.pressure), dtype=torch.float64, device=q0.device)
         pressures = self.g._dev(pressures)
         ip = self.integrator.controls(stop_at_time=t_end, **controls)
-        L = N.load()
-        while True:
-            out = self.integrator.allocate(n)
-            rec = torch.empty((n, capacity, 2 + 6 * self.neq), dtype=torch.float64, device=q0.device)
-            N.check(L.sf_integrate_record_batch(self.g.handle, C.byref(self.params), C.byref(ip), n, N.ptr(q0),
-                                                N.ptr(pressures), N.ptr(out['q']), N.ptr(out['t']),
-                                                N.ptr(out['counts']), N.ptr(out['status']), N.ptr(out['ws']),
-                                                out['ws'].numel() * 4, N.ptr(rec), capacity, N.stream_handle()))
-            if not bool((out['status'] == 7).any()):
-                break
-            del rec
-            capacity *= 2
+        out, rec = self.integrator.record(q0, pressures, ip, capacity or self.integrator.default_record_capacity(n))
+        capacity = rec.shape[1]
         steps = out['counts'][:, 0].long()
         T0 = q0[:, self.tix].clone()
         # smoothed ignition delay by the ESDIRK64 quadrature of the recorded stages

@@ -198,6 +198,45 @@ class BatchIntegrator:
                                                 out['ws'].numel() * 4, N.ptr(record), record.shape[1],
                                                 N.stream_handle()))
 
+    def record(self, q0, pressures, ip, capacity):
+        """Recording integration (sf_integrate_record_batch) of every row of q0, into a record of `capacity` steps per
+        reactor to start with. Reactors that fill their record (status 7) are integrated again, by themselves, into a
+        record of twice the capacity, until every reactor fits; the others keep the results of the first launch. A
+        reactor's integration does not depend on the rest of its batch, so the results are those of a single run
+        with the final capacity, without integrating the whole batch again. Returns (out, record)."""
+        torch = _torch()
+        n, neq = q0.shape
+        row = 2 + 6 * neq
+        out = self.allocate(n)
+        rec = torch.empty((n, capacity, row), dtype=torch.float64, device=q0.device)
+        self.launch(q0, pressures, out, ip, record=rec)
+        full = torch.nonzero(out['status'] == 7).flatten()
+        while full.numel():
+            capacity *= 2
+            sub = self.allocate(full.numel())
+            sub_rec = torch.empty((full.numel(), capacity, row), dtype=torch.float64, device=q0.device)
+            self.launch(q0[full].contiguous(), None if pressures is None else pressures[full].contiguous(), sub, ip,
+                        record=sub_rec)
+            grown = torch.empty((n, capacity, row), dtype=torch.float64, device=q0.device)
+            grown[:, :rec.shape[1]] = rec
+            grown[full] = sub_rec
+            rec = grown
+            for k in ('q', 't', 't_interp', 'counts', 'status'):
+                out[k][full] = sub[k]
+            full = full[torch.nonzero(sub['status'] == 7).flatten()]
+        return out, rec
+
+    def default_record_capacity(self, n, most=1024, share=0.25):
+        """Starting record capacity for n reactors: the largest power of two up to `most` steps whose record takes at
+        most `share` of the device memory that is free now (at least 64 steps)."""
+        torch = _torch()
+        neq = self.mech.n_species + (1 if self.configuration == 'isochoric' else 0)
+        free, _ = torch.cuda.mem_get_info()
+        cap = most
+        while cap > 64 and n * cap * (2 + 6 * neq) * 8 > share * free:
+            cap //= 2
+        return cap
+
     def run(self, q0, pressures=None, graph=False, **controls):
         """Integrate every row of q0 (isobaric [T, Y_0..Y_{ns-2}] or isochoric [rho, T, Y...]).
 
@@ -225,23 +264,15 @@ class BatchIntegrator:
         self._graph = (g, q0, pr, out, ip, self._table)
         return out
 
-    def run_recorded(self, q0, pressures=None, capacity=1024, **controls):
+    def run_recorded(self, q0, pressures=None, capacity=None, **controls):
         """run() that also returns every accepted step: 'times' [n, steps + 1] and 'states' [n, steps + 1, neq]
         (host arrays, padded past each reactor's own step count with its final time and state), 'steps' [n].
-        The record grows until every reactor fits."""
-        torch = _torch()
+        The record grows until every reactor fits (see record; capacity None: default_record_capacity)."""
         q0 = self.g._dev(q0)
         pr = self.g._dev(pressures) if pressures is not None else None
         ip = self.controls(**controls)
         n, neq = q0.shape
-        out = self.allocate(n)
-        while True:
-            rec = torch.empty((n, capacity, 2 + 6 * neq), dtype=torch.float64, device=q0.device)
-            self.launch(q0, pr, out, ip, record=rec)
-            if not bool((out['status'] == 7).any()):
-                break
-            del rec
-            capacity *= 2
+        out, rec = self.record(q0, pr, ip, capacity or self.default_record_capacity(n))
         steps = out['counts'][:, 0].cpu().numpy()
         smax = int(steps.max()) if n else 0
         r = rec[:, :smax].cpu().numpy()

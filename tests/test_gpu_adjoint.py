@@ -80,6 +80,30 @@ def test_recording_does_not_change_the_integration(cuda):
         assert rec[i, 0, 0] == 0. and np.all(np.diff(rec[i, :st[i], 0]) > 0)
 
 
+def test_record_growth_reintegrates_only_the_reactors_that_ran_out(cuda):
+    """A record too small for some reactors: those alone are integrated again into a larger record, and every
+    reactor's record, counts and end state equal those of one run with a record that fits the whole batch."""
+    from spitfire_gb300.adjoint import ReactorAdjoint
+    spec, og = pair('h2-burke')
+    q0 = _h2_reactors(spec, 8)
+    adj = ReactorAdjoint(spec, 'isobaric')
+    big = adj.forward(q0, t_end=2.e-4, capacity=4096)
+    steps = big.steps.cpu().numpy()
+    lo, hi = int(steps.min()), int(steps.max())
+    cap = lo if lo < hi else lo - 1  # the shortest fit (when the counts differ), the others run out
+    small = adj.forward(q0, t_end=2.e-4, capacity=cap)
+    assert small.rec.shape[1] >= hi
+    for a in ('steps', 'status', 'counts', 'q_end', 't_end'):
+        assert np.array_equal(getattr(small, a).cpu().numpy(), getattr(big, a).cpu().numpy()), a
+    # the smoothed delay sums over the record's whole length: another length may associate the sum differently
+    assert np.allclose(small.tau_s.cpu().numpy(), big.tau_s.cpu().numpy(), rtol=1e-13, atol=0.)
+    rb, rs = big.rec.cpu().numpy(), small.rec.cpu().numpy()
+    for i in range(8):
+        assert np.array_equal(rs[i, :steps[i]], rb[i, :steps[i]])
+    g_big, g_small = adj.backward(big), adj.backward(small)
+    assert np.array_equal(g_big['theta'].cpu().numpy(), g_small['theta'].cpu().numpy())
+
+
 def _mid_ignition_gri(spec, seed):
     """A GRI-3.0 reactor of the adjoint workload and an end time inside its ignition: of 8 seeded reactors the one
     that ignites first, t_end = its smoothed ignition delay (both outputs then respond to the kinetics; after
