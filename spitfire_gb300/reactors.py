@@ -32,6 +32,15 @@ def _torch():
     return torch
 
 
+def record_capacity(n, neq, free_bytes, most=1024, share=0.25):
+    """The largest power of two up to `most` steps whose trajectory record for n reactors of neq equations
+    ((2 + 6 neq) doubles per step) takes at most `share` of free_bytes; at least 64 steps."""
+    cap = most
+    while cap > 64 and n * cap * (2 + 6 * neq) * 8 > share * free_bytes:
+        cap //= 2
+    return cap
+
+
 class BatchIntegrator:
     """Batched ESDIRK64 integration of reactors that share a mechanism, configuration, heat transfer and feed.
 
@@ -227,15 +236,10 @@ class BatchIntegrator:
         return out, rec
 
     def default_record_capacity(self, n, most=1024, share=0.25):
-        """Starting record capacity for n reactors: the largest power of two up to `most` steps whose record takes at
-        most `share` of the device memory that is free now (at least 64 steps)."""
+        """Starting record capacity for n reactors: record_capacity with the device memory that is free now."""
         torch = _torch()
         neq = self.mech.n_species + (1 if self.configuration == 'isochoric' else 0)
-        free, _ = torch.cuda.mem_get_info()
-        cap = most
-        while cap > 64 and n * cap * (2 + 6 * neq) * 8 > share * free:
-            cap //= 2
-        return cap
+        return record_capacity(n, neq, torch.cuda.mem_get_info()[0], most, share)
 
     def run(self, q0, pressures=None, graph=False, **controls):
         """Integrate every row of q0 (isobaric [T, Y_0..Y_{ns-2}] or isochoric [rho, T, Y...]).

@@ -76,3 +76,13 @@ def test_growth_without_pressures_and_for_an_empty_batch():
     e = FakeIntegrator()
     out, rec = BatchIntegrator.record(e, torch.empty((0, NEQ), dtype=torch.float64), None, None, 16)
     assert rec.shape == (0, 16, 2 + 6 * NEQ) and e.launched == [(0, 16)]
+
+
+def test_starting_capacity_fits_a_share_of_free_memory():
+    from spitfire_gb300.reactors import record_capacity
+    row = (2 + 6 * 53) * 8
+    assert record_capacity(2048, 53, 270e9) == 1024                    # 5.4 GB of a 67.5 GB share
+    assert record_capacity(100000, 53, 270e9) == 256                   # 100 k reactors: 65.5 GB at 256 steps
+    assert 100000 * 256 * row <= 0.25 * 270e9 < 100000 * 512 * row
+    assert record_capacity(10 ** 7, 53, 1e9) == 64                     # never below 64 steps
+    assert record_capacity(1, 53, 270e9, most=4096) == 4096
