@@ -189,7 +189,7 @@ __device__ __forceinline__ double ipow(double x, int n)
 //   e^x = 2^m (T_j + T_j p), T_j = 2^(j/64) as a head and a tail (the blob's table, 16-byte pairs), the power of two
 //   applied to the exponent field while the result stays normal (|x| < 708), else by two exact factors.
 // Against a 113-bit reference on 2M arguments over the whole range: at most 0.51 ulp for normal results (CUDA's exp:
-// 0.88), 99.8 % correctly rounded; about 11.7 warp FP64 instructions per call against 15.0 for CUDA's exp
+// 0.86-0.88), 99.8 % correctly rounded; about 11.7 warp FP64 instructions per call against 15.0 for CUDA's exp
 // (throughput loops on a GB300). NaN in, NaN out; beyond the range, 0 or +inf.
 __device__ __forceinline__ double exp_parts(double x, double &r, int &N)
 {
@@ -232,7 +232,8 @@ __device__ __forceinline__ double tab_exp(double x, const double *tab)
 //   m = 2^(j/64) e^r in [1, 2) (to rounding), and the reciprocal mantissa 2^(-j/64) e^-r = m^-1 (the factor of a
 //   product: every m^-1 2^-k is e^-x), from the same reduction: 2^(-j/64) = T_(64-j) / 2 for j > 0, and e^r, e^-r
 //   from the even and odd parts of the polynomial, without a division.
-// |x| stays far below 708 for any thermodynamic state (g/RT of a species is at most a few hundred).
+// The power of two stays an integer (k = N >> 6), so any |x| below 2^31 ln2/64 = 2.3e7, where N fits an int, is
+// represented exactly; g/RT of a species is at most a few thousand even at 10 K.
 template <class S>
 __device__ __forceinline__ void store_gibbs_factor(S scr, const ScratchLayout &L, int i, double gRT, const double *tab)
 {
